@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 pressure-projection step.
+
+One step = the pressure section of the reference's Flow_Solver
+(solvers.c:871-931) on one grid: IB flux balance, PoissonRHS, the
+multigrid-preconditioned FGMRES solve, UpdatePressure, Projection (with
+Contra2Cart) and the divergence check.  The default workload is the
+256x128x128 channel with an immersed sphere (mixed FP32-MG / FP64-FGMRES,
+rtol 1e-9, 5 multigrid levels), seeded synthetic inputs of that shape.
+
+value : projection steps (pressure solves) per second with U* resident in
+        HBM when the timed region starts, mixed precision.
+e2e   : the same through vfs_projection_step with page-locked host buffers:
+        H2D of U* and p, the step, D2H of the corrected U and p, every step.
+Also reported: the plain FP64 solve rate on the same grid, p50/p99 step
+latency, the live-probed roofline of the dominant kernel, the CPU oracle
+baseline, clocks during the timed region and the kernel launch count.
+
+--gpus N (launched with torchrun for N > 1) runs N independent replicas,
+one per GPU: the pressure step has no cross-solve exchange, so scaling is
+weak and no data-path collective exists.  --impl reference times the
+reference's algorithm on the host cores instead (the CPU oracle port: the
+reference itself needs PETSc, HYPRE and MPI, which this image lacks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="sphere", choices=["channel", "sphere", "terrain"])
+    ap.add_argument("--scale", type=int, default=1, help="divide each grid extent (quick runs)")
+    ap.add_argument("--rtol", type=float, default=1e-11)
+    ap.add_argument("--nu", type=int, default=2)
+    ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_case(args):
+    from vfs_v3p2_gb300 import synth
+    if args.config == "channel":
+        return synth.c1_channel(args.scale)
+    if args.config == "terrain":
+        return synth.c3_terrain(args.scale)
+    return synth.c2_sphere(args.scale)
+
+
+WORKLOAD = {
+    "channel": "channel 64x64x64, tanh beta 2.0, skew 0.05 sin(z), no body, U ~ N(0,1) per face",
+    "sphere": "channel 256x128x128 + sphere r=0.3 at (pi,0,pi/2), Poiseuille + N(0,0.1^2)",
+    "terrain": "terrain 512x256x256 over a Gaussian hill, log-law + N(0,0.05^2)",
+}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return dist, rank, local, ws
+    return None, rank, local, ws
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons (every 200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}", "--format=csv,noheader",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                mx = max(mx, float(parts[2].split()[0]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_key: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/traffic.json), scaled to this workload, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(kernel_key)
+    except Exception:
+        return None
+
+
+def cpu_baseline(case, args, steps=2):
+    """The CPU oracle (same discretisation, FP64 FGMRES + GMG, OpenMP over all
+    host cores) on the same workload; returns steps/s and the sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    import oracle as O
+    O.build()
+    g = case.grid
+    d = O.dims_of(g)
+    mg = O.MG(d, g.coor, g.nvert, case.levels)
+    mg.set_params(2, 2, 32, 0.8, 0.8)
+    O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=args.rtol, mg=mg)  # warm-up
+    t = time.perf_counter()
+    for _ in range(steps):
+        r = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=args.rtol, mg=mg)
+    dt = time.perf_counter() - t
+    mg.close()
+    return steps / dt, O.lib().orc_num_threads(), r
+
+
+def run_reference(args):
+    dist, rank, local, ws = dist_init()
+    if rank != 0:
+        return
+    case = make_case(args)
+    val, cores, r = cpu_baseline(case, args, steps=max(1, min(args.steps, 3)))
+    line = {
+        "metric": "pressure projection steps/s (solves/s)", "value": val, "unit": "solves/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": max(1, min(args.steps, 3)), "warmup": 1, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD[args.config], "grid": case.name, "rtol": args.rtol, "mg_levels": case.levels},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{WORKLOAD[args.config]}: full-size steps timed after 1 warm-up"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "divmax": r["divmax"], "iterations": r["info"]["iterations"],
+        "note": "reference build unavailable (PETSc/HYPRE/MPI absent); CPU oracle restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    dist, rank, local, ws = dist_init()
+    from vfs_v3p2_gb300 import capi
+    case = make_case(args)
+    g = case.grid
+    N = g.nvert.size
+    ctx = capi.Context(local)
+    gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    ctx.poisson_lhs(gid)
+    ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
+    ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
+    mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart)
+    fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart)
+
+    def steps(params, K, base_slot):
+        infos, divs = [], []
+        ctx.mark(gid, base_slot)
+        for s in range(K):
+            info, dm = ctx.projection_step(gid, params)
+            ctx.mark(gid, base_slot + 1 + s)
+            infos.append(info)
+            divs.append(dm)
+        total = ctx.elapsed(base_slot, base_slot + K)
+        per = [ctx.elapsed(base_slot + s, base_slot + s + 1) for s in range(K)]
+        return total, per, infos, divs
+
+    # ---- mixed precision, U* resident: the headline ----
+    steps(mixed, max(args.warmup, 3), 0)
+    clk = Clocks(local)
+    barrier(dist)
+    ctx.sync()
+    n0 = capi.launch_count()
+    ctx.probe_begin(capi.PROBE_SMOOTH)
+    total_ms, per_ms, infos, divs = steps(mixed, args.steps, 100)
+    ctx.sync()
+    nl = capi.launch_count() - n0
+    plaunch, pms, pbytes = ctx.probe_end()
+    clocks = clk.stop()
+    barrier(dist)
+    tmax = allmax(dist, total_ms)
+    value = ws * args.steps / (tmax / 1e3)
+    phi_mixed = ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape)
+
+    # ---- plain FP64 on the same grid ----
+    fp64_rate, fp64_iters, fp64_div, mix_vs_fp64_err = None, None, None, None
+    if not args.no_fp64:
+        steps(fp64, 2, 200)
+        K64 = max(3, args.steps // 2)
+        t64, _, inf64, div64 = steps(fp64, K64, 300)
+        fp64_rate = ws * K64 / (allmax(dist, t64) / 1e3)
+        fp64_iters = statistics.mean(i["iterations"] for i in inf64)
+        fp64_div = max(div64)
+        phi64 = ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape)
+        fl = g.nvert < 0.1
+        fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = (False,) * 6
+        a, r = phi_mixed[fl] - phi_mixed[fl].mean(), phi64[fl] - phi64[fl].mean()
+        mix_vs_fp64_err = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+
+    # ---- end to end through the C ABI with page-locked host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        u_host = np.empty_like(case.ucont)
+        p_host = np.zeros(g.nvert.shape)
+        ctx.host_register(u_host)
+        ctx.host_register(p_host)
+        e_ms = []
+        for s in range(2 + args.steps):
+            np.copyto(u_host, case.ucont)
+            ctx.mark(gid, 400)
+            ctx.projection_step_ptr(gid, mixed, u_host.ctypes.data, p_host.ctypes.data)
+            ctx.mark(gid, 401)
+            if s >= 2:
+                e_ms.append(ctx.elapsed(400, 401))
+        ctx.host_unregister(u_host)
+        ctx.host_unregister(p_host)
+        et = allmax(dist, sum(e_ms))
+        e2e = {"value": ws * len(e_ms) / (et / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(u_host.nbytes + p_host.nbytes),
+               "d2h_bytes_per_step": int(u_host.nbytes + p_host.nbytes)}
+
+    peak, peak_kind = measured_peak()
+    achieved = (pbytes / plaunch) / ((pms / plaunch) / 1e3) / 1e9 if plaunch else None
+    traffic = ncu_traffic("k_smooth<float>:" + case.name)
+    roof = {"kernel": "k_smooth<float> (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+            "traffic": traffic, "launches": plaunch, "avg_launch_ms": pms / plaunch if plaunch else None,
+            "alg_bytes_per_launch": pbytes / plaunch if plaunch else None}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cval, cores, _ = cpu_baseline(case, args, steps=2)
+        cpu = {"value": cval, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"2 full-size steps of {case.name} after 1 warm-up (FP64 FGMRES + GMG, OpenMP)"}
+
+    if rank == 0:
+        its = [i["iterations"] for i in infos]
+        line = {
+            "metric": "pressure projection steps/s (solves/s), mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+            "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
+                       "mg_levels": case.levels, "rtol": args.rtol, "nu": args.nu, "restart": args.restart,
+                       "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
+            "e2e": e2e,
+            "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},
+            "iterations": {"mean": statistics.mean(its), "max": max(its)},
+            "divmax": max(divs), "relres_max": max(i["relres"] for i in infos),
+            "fp64": {"value": fp64_rate, "iterations": fp64_iters, "divmax": fp64_div,
+                     "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
+                     "phi_rel_l2_mixed_vs_fp64": mix_vs_fp64_err},
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,198 @@
+/*
+ * vfs_gpu.h -- C ABI of the GB300 pressure-projection step of VFS.
+ *
+ * Drop-in for the reference's pressure path (trunglendsu/VFS_v3p2):
+ *   PoissonLHSNew   poisson.c:976-1691        -> vfs_poisson_lhs
+ *   PoissonRHS      poisson_hypre.c:272-477,
+ *                   poisson.c:1789-1915        -> vfs_poisson_rhs
+ *   PoissonSolver_MG mhv_poisson.c:2121-2359,
+ *   PoissonSolver_Hypre poisson_hypre.c:580-771 -> vfs_poisson_solve
+ *   UpdatePressure  poisson.c:2473-2632       -> vfs_update_pressure
+ *   Projection      poisson.c:2122-2470       -> vfs_projection
+ *   Divergence      main.c:1244-1390          -> vfs_divergence_max
+ *   Flow_Solver pressure section, solvers.c:871-931 -> vfs_projection_step
+ *
+ * Plain C: no PETSc, HYPRE or CUDA types.  Every function returns an int
+ * status (VFS_OK = 0); vfs_last_error() gives the message of the last failure
+ * on a context.  Host buffers are borrowed for the duration of a call.
+ * Fields use the reference's DMDA array layout: extents mx = ni + 2,
+ * my = nj + 2, mz = nk + 2 (one ghost/boundary cell per side), element
+ * (i, j, k) at ((k * my) + j) * mx + i; vector fields (Cmpnts: node
+ * coordinates, Ucont, Ucat) are 3 doubles per element.
+ *
+ * The device state of a grid (metrics, operator, multigrid hierarchy,
+ * Ucont, p, phi, Krylov basis) belongs to the context and stays resident in
+ * HBM between calls.  A context is used by one host thread at a time.
+ */
+#ifndef VFS_GPU_H
+#define VFS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VFS_OK 0
+#define VFS_ERR_ARG 1      /* invalid argument or unsupported grid */
+#define VFS_ERR_CUDA 2     /* CUDA runtime error */
+#define VFS_ERR_NOMEM 3    /* HBM budget exceeded or allocation failure */
+#define VFS_ERR_NOTCONV 4  /* solver stopped at maxit above rtol */
+#define VFS_ERR_STATE 5    /* call order (e.g. solve before the LHS) */
+#define VFS_ERR_NUMERIC 6  /* NaN or Inf in the right-hand side or iterates */
+#define VFS_ERR_BUSY 7     /* serving: no free slot or memory right now */
+
+#define VFS_FP64 0   /* plain: FP64 multigrid inside FP64 FGMRES */
+#define VFS_MIXED 1  /* FP32 multigrid (FP32 coefficients) inside FP64 FGMRES */
+
+/* Fields for vfs_set_field / vfs_get_field. */
+#define VFS_FIELD_UCONT 0  /* 3 doubles per cell (AoS), contravariant flux */
+#define VFS_FIELD_P 1      /* pressure */
+#define VFS_FIELD_PHI 2    /* pressure correction (solution) */
+#define VFS_FIELD_RHS 3    /* Poisson right-hand side */
+#define VFS_FIELD_UCAT 4   /* 3 doubles per cell (AoS), Cartesian velocity */
+#define VFS_FIELD_NVERT 5  /* immersed-boundary mask */
+#define VFS_FIELD_USTAR 6  /* 3 doubles per cell (AoS), resident intermediate flux */
+
+typedef struct vfs_ctx vfs_ctx;
+
+typedef struct {
+  int device;                           /* CUDA device ordinal */
+  unsigned long long hbm_budget_bytes;  /* 0 = no limit; grids beyond it are refused */
+} vfs_config;
+
+typedef struct {
+  int mx, my, mz;                       /* ghosted extents ni+2, nj+2, nk+2 */
+  int i_periodic, j_periodic, k_periodic;
+  int mg_levels;                        /* levels including the finest (>= 1) */
+  int semi_i, semi_j, semi_k;           /* semi-coarsening per axis (-mg_*_semi) */
+  int immersed;                         /* 0: no body, 1: IB flux balance (VolumeFlux) */
+  const double* coor;                   /* host [mz][my][mx][3] node coordinates, nodes 0..n valid */
+  const double* nvert;                  /* host [mz][my][mx] (0 fluid, 1 IB node, >1 solid) */
+} vfs_grid_desc;
+
+typedef struct {
+  int precision;   /* VFS_FP64 or VFS_MIXED */
+  double rtol;     /* stop when ||b - A phi|| <= rtol * ||b|| */
+  int maxit;       /* maximum preconditioner applications */
+  int restart;     /* FGMRES restart length (<= 64) */
+  int nu1, nu2;    /* pre / post y-line smoothing sweeps per level */
+  double omega;    /* line-Jacobi damping */
+  int warm_start;  /* 1: start from the resident phi, 0: from zero */
+} vfs_solve_params;
+
+typedef struct {
+  int iterations;  /* preconditioner applications */
+  int converged;
+  double relres;   /* true ||b - A phi|| / ||b|| at exit */
+  double bnorm;
+  double time_ms;  /* device time of the solve */
+} vfs_solve_info;
+
+/* Context (device, streams, HBM budget). */
+int vfs_create(const vfs_config* cfg, vfs_ctx** out);
+void vfs_destroy(vfs_ctx* ctx);
+const char* vfs_last_error(const vfs_ctx* ctx);
+void vfs_default_params(vfs_solve_params* p);
+
+/* MG_Initial + FormMetrics (init.c:205-905, metrics.c:4-1290): uploads the
+ * node coordinates and nvert, builds the coarse levels (every other node,
+ * init.c:397-449; MyNvertRestriction, poisson.c:2004-2106) and the metrics
+ * of every level on the GPU.  *grid_id receives the handle. */
+int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id);
+int vfs_grid_destroy(vfs_ctx* ctx, int grid);
+/* Device bytes held by a grid (for admission control). */
+int vfs_grid_bytes(vfs_ctx* ctx, int grid, unsigned long long* bytes);
+/* Bytes a grid with this description would hold (nothing is allocated). */
+int vfs_grid_estimate(const vfs_grid_desc* desc, int restart, unsigned long long* bytes);
+
+/* PoissonLHSNew (poisson.c:976-1691): the g tensor and the 19-point
+ * coefficients of every level, plus the coarsest-level dense inverse. */
+int vfs_poisson_lhs(vfs_ctx* ctx, int grid);
+
+/* Field transfer between host and the resident device state. */
+int vfs_set_field(vfs_ctx* ctx, int grid, int field, const double* host);
+int vfs_get_field(vfs_ctx* ctx, int grid, int field, double* host);
+
+/* VolumeFlux (poisson.c:2634-2828 / 2898-3240) on the resident Ucont.
+ * out[0..3] = IB flux and area before, flux and area after the balance. */
+int vfs_volume_flux(vfs_ctx* ctx, int grid, double out[4]);
+
+/* PoissonRHS2_hypre (poisson_hypre.c:342-429) on the resident Ucont, plus
+ * the compatibility fix of PoissonRHS2 (poisson.c:1879-1903) when meanfix.
+ * *sum_out (nullable) receives the sum of b before the fix. */
+int vfs_poisson_rhs(vfs_ctx* ctx, int grid, double dt, double st, double coeff, int meanfix, double* sum_out);
+
+/* PoissonSolver_MG (mhv_poisson.c:2121-2359): FGMRES preconditioned by a
+ * geometric V-cycle, then Remove_Nullspace (poisson_hypre.c:207-270) and
+ * Convert_Phi2_Phi (poisson.c:97-185) on the resident phi. */
+int vfs_poisson_solve(vfs_ctx* ctx, int grid, const vfs_solve_params* p, vfs_solve_info* info);
+
+/* UpdatePressure (poisson.c:2473-2632): p += phi on fluid cells. */
+int vfs_update_pressure(vfs_ctx* ctx, int grid);
+
+/* Projection (poisson.c:2122-2470) on the resident Ucont, then Contra2Cart
+ * (rhs.c:52-190) into the resident Ucat. */
+int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff);
+
+/* Divergence (main.c:1244-1390): max |div U| * aj over the fluid. */
+int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out);
+
+/* The pressure section of Flow_Solver (solvers.c:871-931): VolumeFlux,
+ * PoissonRHS, the solve, UpdatePressure, Projection, Divergence.
+ * ucont_inout (nullable): host U* in, corrected U out; when NULL the
+ * resident U* (VFS_FIELD_USTAR) is the input and the result stays resident.
+ * p_inout (nullable): host pressure in and out.  divmax (nullable). */
+int vfs_projection_step(vfs_ctx* ctx, int grid, double* ucont_inout, double* p_inout, double dt, double st,
+                        double coeff, const vfs_solve_params* p, vfs_solve_info* info, double* divmax);
+
+/* ---- test and introspection hooks (same arithmetic as the hot path) ---- */
+/* metric pack of a level: 43 * N doubles (csi eta zet aj icsi ieta izet iaj
+ * jcsi jeta jzet jaj kcsi keta kzet kaj cent; vectors AoS). */
+int vfs_get_metrics(vfs_ctx* ctx, int grid, int level, double* out);
+/* 19 * N coefficients of a level: which 0 = unscaled FP64 (the outer
+ * operator on the finest level), 1 = aj-scaled FP64, 2 = aj-scaled FP32
+ * (returned as doubles). */
+int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out);
+int vfs_get_level_dims(vfs_ctx* ctx, int grid, int level, int dims[3]);
+int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out);
+/* y = A x with the operator `which` (as vfs_get_coef) of a level. */
+int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, double* y);
+/* One multigrid preconditioner application z = M^{-1} v on the finest level. */
+int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_params* p, const double* v, double* z);
+/* MyRestriction of level `level` (>= 1) to level-1, MyInterpolation of level-1
+ * to `level` (overwrite), in FP64. */
+int vfs_mg_restrict(vfs_ctx* ctx, int grid, int level, const double* x, double* y);
+int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y);
+/* One damped y-line Jacobi sweep on a level (FP64 aj-scaled operator). */
+int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x, double omega);
+
+/* ---- batched solves (many uneven grids in shared launches) ---- */
+/* Runs vfs_projection_step on n grids with resident U*; the launches of
+ * all grids are interleaved on the context's streams. */
+int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, double st, double coeff,
+                              const vfs_solve_params* p, vfs_solve_info* infos, double* divmax);
+
+/* Device synchronisation of all work of a context. */
+int vfs_sync(vfs_ctx* ctx);
+
+/* ---- measurement ---- */
+#define VFS_PROBE_SMOOTH 1   /* full y-line sweeps of the finest multigrid level */
+#define VFS_PROBE_APPLY64 2  /* FP64 outer operator apply (w = A z) */
+/* Record a CUDA event pair around every launch of one kernel (on the stream
+ * it runs on) until vfs_probe_end, which returns the launch count, their
+ * summed device time and their summed algorithmic bytes. */
+int vfs_probe_begin(vfs_ctx* ctx, int kernel);
+int vfs_probe_end(vfs_ctx* ctx, unsigned long long* launches, double* total_ms, double* alg_bytes);
+/* CUDA event `slot` (0..4095) recorded on the stream of a grid; elapsed
+ * device time between two recorded slots. */
+int vfs_mark(vfs_ctx* ctx, int grid, int slot);
+int vfs_elapsed(vfs_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Kernels launched by this library since it was loaded (all contexts). */
+int vfs_launch_count(unsigned long long* out);
+/* Page-lock a host buffer so vfs_projection_step copies it asynchronously. */
+int vfs_host_register(void* ptr, unsigned long long bytes);
+int vfs_host_unregister(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

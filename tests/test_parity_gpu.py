@@ -1,0 +1,221 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Setup kernels and the per-step FP64 kernels follow the reference's
+arithmetic order without FMA contraction, so metrics, g tensor, operator
+coefficients and the projection of a given phi are compared bit for bit.
+Kernels with FMA or tree reductions are compared with the tolerance written
+at each assert.  The solution criterion is the one the pressure path is
+judged by: relative L2 of phi <= 1e-8 after removing the fluid mean
+against a tightly converged oracle solve, and max |div u| at or below the
+divergence the reference's own solver settings leave (poisson_tol = 5e-9,
+poisson_it = 10 iterations, main.c:87,126)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from vfs_v3p2_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def small_cases():
+    return [
+        ("channel", synth.channel_case(16, 12, 16, seed=11, levels=3)),
+        ("sphere", synth.channel_case(32, 16, 16, seed=12, spheres=[(math.pi, 0.0, math.pi / 2, 0.6)], sigma=0.5,
+                                      levels=3)),
+        ("uniform", synth.channel_case(12, 8, 8, seed=13, beta=0.0, skew=0.0, levels=2)),
+        ("ragged", synth.channel_case(20, 6, 12, seed=14, levels=2)),
+    ]
+
+
+CASES = small_cases()
+
+
+@pytest.fixture(scope="module", params=[c[0] for c in CASES])
+def loaded(request, gpu_ctx):
+    name, case = [c for c in CASES if c[0] == request.param][0]
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    gpu_ctx.poisson_lhs(gid)
+    d = O.dims_of(g)
+    mg = O.MG(d, g.coor, g.nvert, case.levels)
+    yield case, gid, d, mg
+    mg.close()
+    gpu_ctx.grid_destroy(gid)
+
+
+def test_metrics_bitexact_all_levels(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    for l in range(case.levels):
+        ref = mg.level_array(l, "M")
+        got = gpu_ctx.metrics(gid, l)
+        assert np.array_equal(got, ref), f"level {l}: max diff {np.abs(got - ref).max()}"
+
+
+def test_nvert_coarsening_exact(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    for l in range(case.levels - 1):
+        ref = mg.level_array(l, "nvert")
+        got = gpu_ctx.level_nvert(gid, l).ravel()
+        assert np.array_equal(got, ref)
+
+
+def test_lhs_coefficients_bitexact(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    for l in range(case.levels):
+        ref = mg.level_array(l, "coef")
+        got = gpu_ctx.coef(gid, l, 0).ravel()
+        assert np.array_equal(got, ref), f"level {l}: {np.abs(got - ref).max()}"
+        refm = mg.level_array(l, "mcoef")
+        assert np.array_equal(gpu_ctx.coef(gid, l, 1).ravel(), refm)
+        assert np.array_equal(gpu_ctx.coef(gid, l, 2).ravel(), refm.astype(np.float32).astype(np.float64))
+
+
+def test_operator_apply(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    rng = np.random.default_rng(5)
+    for l in range(case.levels):
+        ld = mg.level_dims(l)
+        x = rng.normal(size=(ld.mz, ld.my, ld.mx))
+        coef = mg.level_array(l, "coef").reshape((19, ld.mz, ld.my, ld.mx))
+        ref = O.matvec(ld, coef, x)
+        got = gpu_ctx.apply_op(gid, l, 0, x)
+        assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()  # FMA vs separate rounding
+        refm = mg.matvec(l, x)
+        gotm = gpu_ctx.apply_op(gid, l, 1, x)
+        assert np.abs(gotm - refm).max() <= 1e-13 * np.abs(refm).max()
+        got32 = gpu_ctx.apply_op(gid, l, 2, x)
+        assert np.abs(got32 - refm).max() <= 1e-5 * np.abs(refm).max()  # FP32 coefficients and arithmetic
+
+
+def test_transfer_and_smoother(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    rng = np.random.default_rng(6)
+    for l in range(1, case.levels):
+        fd, cd = mg.level_dims(l), mg.level_dims(l - 1)
+        xf = rng.normal(size=(fd.mz, fd.my, fd.mx))
+        ref = mg.restrict(l, xf)
+        got = gpu_ctx.mg_restrict(gid, l, xf)
+        assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
+        xc = rng.normal(size=(cd.mz, cd.my, cd.mx))
+        ref = mg.prolong(l, xc)
+        got = gpu_ctx.mg_prolong(gid, l, xc)
+        assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
+    for l in range(case.levels):
+        ld = mg.level_dims(l)
+        b = rng.normal(size=(ld.mz, ld.my, ld.mx))
+        x = rng.normal(size=(ld.mz, ld.my, ld.mx))
+        nv = mg.level_array(l, "nvert").reshape(b.shape)
+        for a in (b, x):
+            a[nv > 0.1] = 0.0
+            a[0], a[-1], a[:, 0], a[:, -1], a[:, :, 0], a[:, :, -1] = 0, 0, 0, 0, 0, 0
+        ref = x.copy()
+        mg.smooth(l, b, ref, 1, 0.8)
+        got = gpu_ctx.mg_smooth(gid, l, b, x, 0.8)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_rhs_flux_projection_divergence(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    g = case.grid
+    M = O.form_metrics(d, g.coor)
+    u = case.ucont.copy()
+    fa = O.volume_flux(d, case.immersed, u, g.nvert, M)
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, case.ucont)
+    fa_g = gpu_ctx.volume_flux(gid)
+    assert np.allclose(fa_g, fa, rtol=1e-12, atol=1e-15)
+    assert np.abs(gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape) - u).max() <= 1e-14 * np.abs(u).max()
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
+    b, s = O.rhs(d, u, g.nvert)
+    s_g = gpu_ctx.poisson_rhs(gid)
+    bg = gpu_ctx.get_field(gid, capi.FIELD_RHS, b.shape)
+    assert np.abs(bg - b).max() <= 1e-13 * np.abs(b).max()  # mean fix sums in tree order
+    assert abs(s_g - s) <= 1e-12 * np.abs(b).sum()
+    # projection of the same phi is bit-exact
+    rng = np.random.default_rng(8)
+    phi = rng.normal(size=b.shape)
+    O.phi_finish(d, g.nvert, phi)
+    u_ref = u.copy()
+    O.projection(d, M, g.nvert, phi, u_ref)
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
+    gpu_ctx.L.vfs_set_field(gpu_ctx.h, gid, capi.FIELD_PHI, capi.dptr(phi))
+    gpu_ctx.projection(gid)
+    u_got = gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape)
+    assert np.array_equal(u_got, u_ref)
+    ucat_ref = O.contra2cart(d, M, g.nvert, u_ref)
+    ucat = gpu_ctx.get_field(gid, capi.FIELD_UCAT, u.shape)
+    fl = (g.nvert < 0.1)
+    fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
+    assert np.array_equal(ucat[fl], ucat_ref[fl])
+    dv = O.divergence(d, u_ref, O.metric(M, d, "aj"), g.nvert)
+    assert gpu_ctx.divergence_max(gid) == dv
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_full_step_parity(gpu_ctx, loaded, precision):
+    case, gid, d, mg = loaded
+    g = case.grid
+    ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg)
+    params = capi.default_params(precision=precision, rtol=1e-12, maxit=300, restart=30)
+    u = np.ascontiguousarray(case.ucont.copy())
+    p = np.zeros(g.nvert.shape)
+    info, divmax = gpu_ctx.projection_step(gid, params, u, p)
+    assert info["converged"] and info["relres"] < 1e-11
+    phi = gpu_ctx.get_field(gid, capi.FIELD_PHI, p.shape)
+    fl = (g.nvert < 0.1)
+    fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
+    a, r = phi[fl] - phi[fl].mean(), ref["phi"][fl] - ref["phi"][fl].mean()
+    assert np.linalg.norm(a - r) / np.linalg.norm(r) <= 1e-8
+    assert np.abs(p[fl] - ref["p"][fl]).max() <= 1e-8 * np.abs(ref["p"][fl]).max()
+    assert np.abs(u - ref["ucont"]).max() <= 1e-8 * np.abs(ref["ucont"]).max()
+    ref_settings = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=5e-9, maxit=10,
+                                     mg=mg)
+    assert divmax <= ref_settings["divmax"]
+    assert divmax < 1e-8
+
+
+def test_mixed_precision_error_vs_fp64_oracle(gpu_ctx):
+    """Mixed FP32-MG / FP64-FGMRES reaches the FP64 oracle's solution: the
+    FP32 preconditioner only changes search directions."""
+    case = synth.c2_sphere(scale=4)
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, 1)
+    gpu_ctx.poisson_lhs(gid)
+    ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=1, rtol=1e-13, maxit=400)
+    u = np.ascontiguousarray(case.ucont.copy())
+    info, divmax = gpu_ctx.projection_step(gid, capi.default_params(precision="mixed", rtol=1e-12), u, None)
+    phi = gpu_ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape)
+    fl = (g.nvert < 0.1)
+    fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
+    a, r = phi[fl] - phi[fl].mean(), ref["phi"][fl] - ref["phi"][fl].mean()
+    assert np.linalg.norm(a - r) / np.linalg.norm(r) <= 1e-8
+    ref_settings = O.projection_step(g, case.ucont, levels=case.levels, immersed=1, rtol=5e-9, maxit=10)
+    assert divmax <= ref_settings["divmax"] and divmax < 1e-8
+    gpu_ctx.grid_destroy(gid)
+
+
+def test_errors_are_reported(gpu_ctx):
+    case = CASES[0][1]
+    g = case.grid
+    with pytest.raises(capi.VfsError) as e:
+        gpu_ctx.grid_create(g.coor[:, :, :-1].copy(), g.nvert[:, :, :-1].copy(), 3, 0)  # odd i extent
+    assert e.value.code == capi.VFS_ERR_ARG
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, 2, 0)
+    with pytest.raises(capi.VfsError) as e:
+        gpu_ctx.poisson_solve(gid, capi.default_params())
+    assert e.value.code == capi.VFS_ERR_STATE
+    gpu_ctx.poisson_lhs(gid)
+    bad = case.ucont.copy()
+    bad[3, 3, 3, 0] = np.nan
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, bad)
+    with pytest.raises(capi.VfsError) as e:
+        gpu_ctx.poisson_rhs(gid)
+    assert e.value.code == capi.VFS_ERR_NUMERIC
+    gpu_ctx.grid_destroy(gid)
+    small = capi.Context(0, hbm_budget_bytes=1 << 20)
+    with pytest.raises(capi.VfsError) as e:
+        small.grid_create(g.coor, g.nvert, 3, 0)
+    assert e.value.code == capi.VFS_ERR_NOMEM
+    small.close()

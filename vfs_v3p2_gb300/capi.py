@@ -1,0 +1,375 @@
+"""ctypes binding of the C ABI in include/vfs_gpu.h.
+
+This is the reference-side binding a Python caller uses; a C or C++ caller
+links libvfs_gb300.so and includes vfs_gpu.h directly.  There is no CPU
+fallback: if the CUDA library cannot be built or loaded, every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+VFS_OK = 0
+VFS_ERR_ARG = 1
+VFS_ERR_CUDA = 2
+VFS_ERR_NOMEM = 3
+VFS_ERR_NOTCONV = 4
+VFS_ERR_STATE = 5
+VFS_ERR_NUMERIC = 6
+VFS_ERR_BUSY = 7
+
+VFS_FP64 = 0
+VFS_MIXED = 1
+
+FIELD_UCONT = 0
+FIELD_P = 1
+FIELD_PHI = 2
+FIELD_RHS = 3
+FIELD_UCAT = 4
+FIELD_NVERT = 5
+FIELD_USTAR = 6
+
+ERRNAMES = {1: "VFS_ERR_ARG", 2: "VFS_ERR_CUDA", 3: "VFS_ERR_NOMEM", 4: "VFS_ERR_NOTCONV", 5: "VFS_ERR_STATE",
+            6: "VFS_ERR_NUMERIC", 7: "VFS_ERR_BUSY"}
+
+
+class VfsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_ulonglong)]
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("mx", ctypes.c_int), ("my", ctypes.c_int), ("mz", ctypes.c_int),
+                ("i_periodic", ctypes.c_int), ("j_periodic", ctypes.c_int), ("k_periodic", ctypes.c_int),
+                ("mg_levels", ctypes.c_int), ("semi_i", ctypes.c_int), ("semi_j", ctypes.c_int),
+                ("semi_k", ctypes.c_int), ("immersed", ctypes.c_int),
+                ("coor", ctypes.POINTER(ctypes.c_double)), ("nvert", ctypes.POINTER(ctypes.c_double))]
+
+
+class SolveParams(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
+                ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
+                ("omega", ctypes.c_double), ("warm_start", ctypes.c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("relres", ctypes.c_double),
+                ("bnorm", ctypes.c_double), ("time_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return dict(iterations=self.iterations, converged=bool(self.converged), relres=self.relres,
+                    bnorm=self.bnorm, time_ms=self.time_ms)
+
+
+# Every symbol include/vfs_gpu.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+SIGNATURES = {
+    "vfs_create": ([ctypes.POINTER(Config), ctypes.POINTER(_P)], _I),
+    "vfs_destroy": ([_P], None),
+    "vfs_last_error": ([_P], ctypes.c_char_p),
+    "vfs_default_params": ([ctypes.POINTER(SolveParams)], None),
+    "vfs_grid_create": ([_P, ctypes.POINTER(GridDesc), _IP], _I),
+    "vfs_grid_destroy": ([_P, _I], _I),
+    "vfs_grid_bytes": ([_P, _I, ctypes.POINTER(ctypes.c_ulonglong)], _I),
+    "vfs_grid_estimate": ([ctypes.POINTER(GridDesc), _I, ctypes.POINTER(ctypes.c_ulonglong)], _I),
+    "vfs_poisson_lhs": ([_P, _I], _I),
+    "vfs_set_field": ([_P, _I, _I, _DP], _I),
+    "vfs_get_field": ([_P, _I, _I, _DP], _I),
+    "vfs_volume_flux": ([_P, _I, _DP], _I),
+    "vfs_poisson_rhs": ([_P, _I, _D, _D, _D, _I, _DP], _I),
+    "vfs_poisson_solve": ([_P, _I, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo)], _I),
+    "vfs_update_pressure": ([_P, _I], _I),
+    "vfs_projection": ([_P, _I, _D, _D, _D], _I),
+    "vfs_divergence_max": ([_P, _I, _DP], _I),
+    "vfs_projection_step": ([_P, _I, _DP, _DP, _D, _D, _D, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo),
+                             _DP], _I),
+    "vfs_get_metrics": ([_P, _I, _I, _DP], _I),
+    "vfs_get_coef": ([_P, _I, _I, _I, _DP], _I),
+    "vfs_get_level_dims": ([_P, _I, _I, _IP], _I),
+    "vfs_get_level_nvert": ([_P, _I, _I, _DP], _I),
+    "vfs_apply_op": ([_P, _I, _I, _I, _DP, _DP], _I),
+    "vfs_apply_precond": ([_P, _I, _I, ctypes.POINTER(SolveParams), _DP, _DP], _I),
+    "vfs_mg_restrict": ([_P, _I, _I, _DP, _DP], _I),
+    "vfs_mg_prolong": ([_P, _I, _I, _DP, _DP], _I),
+    "vfs_mg_smooth": ([_P, _I, _I, _DP, _DP, _D], _I),
+    "vfs_projection_step_batch": ([_P, _I, _IP, _D, _D, _D, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo),
+                                   _DP], _I),
+    "vfs_sync": ([_P], _I),
+    "vfs_probe_begin": ([_P, _I], _I),
+    "vfs_probe_end": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _DP, _DP], _I),
+    "vfs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], _I),
+    "vfs_mark": ([_P, _I, _I], _I),
+    "vfs_elapsed": ([_P, _I, _I, _DP], _I),
+    "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
+    "vfs_host_unregister": ([_P], _I),
+}
+
+PROBE_SMOOTH = 1
+PROBE_APPLY64 = 2
+
+
+def launch_count() -> int:
+    n = ctypes.c_ulonglong()
+    load().vfs_launch_count(ctypes.byref(n))
+    return n.value
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libvfs_gb300.so (building it first when missing or stale)."""
+    global _lib
+    if _lib is None:
+        if build_if_missing:
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError(f"CUDA library {_build.LIB} is missing; run vfs_v3p2_gb300/build.py")
+        L = ctypes.CDLL(_build.LIB)
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def dptr(a: np.ndarray):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("arrays passed to the C ABI must be C-contiguous float64")
+    return a.ctypes.data_as(_DP)
+
+
+def default_params(**kw) -> SolveParams:
+    p = SolveParams()
+    load().vfs_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = {"fp64": VFS_FP64, "mixed": VFS_MIXED}[v]
+        setattr(p, k, v)
+    return p
+
+
+class Context:
+    """One vfs_ctx (a device and its resident grids)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.L = load()
+        cfg = Config(device, hbm_budget_bytes)
+        h = _P()
+        rc = self.L.vfs_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc:
+            raise VfsError(rc, "vfs_create failed (no usable CUDA device?)")
+        self.h = h
+
+    def check(self, rc):
+        if rc:
+            raise VfsError(rc, self.L.vfs_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.vfs_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- grids --
+    def grid_create(self, coor: np.ndarray, nvert: np.ndarray, levels: int, immersed: int = 0,
+                    periodic=(1, 0, 1), semi=(0, 0, 0)) -> int:
+        coor = np.ascontiguousarray(coor, dtype=np.float64)
+        nvert = np.ascontiguousarray(nvert, dtype=np.float64)
+        mz, my, mx = nvert.shape
+        if coor.shape != (mz, my, mx, 3):
+            raise ValueError("coor must be [mz, my, mx, 3]")
+        d = GridDesc(mx, my, mz, periodic[0], periodic[1], periodic[2], levels, semi[0], semi[1], semi[2], immersed,
+                     dptr(coor), dptr(nvert))
+        gid = ctypes.c_int()
+        self.check(self.L.vfs_grid_create(self.h, ctypes.byref(d), ctypes.byref(gid)))
+        return gid.value
+
+    def grid_destroy(self, g: int):
+        self.check(self.L.vfs_grid_destroy(self.h, g))
+
+    def grid_bytes(self, g: int) -> int:
+        b = ctypes.c_ulonglong()
+        self.check(self.L.vfs_grid_bytes(self.h, g, ctypes.byref(b)))
+        return b.value
+
+    def level_dims(self, g: int, level: int):
+        d = (ctypes.c_int * 3)()
+        self.check(self.L.vfs_get_level_dims(self.h, g, level, d))
+        return tuple(d)
+
+    def poisson_lhs(self, g: int):
+        self.check(self.L.vfs_poisson_lhs(self.h, g))
+
+    def set_field(self, g: int, field: int, a: np.ndarray):
+        self.check(self.L.vfs_set_field(self.h, g, field, dptr(np.ascontiguousarray(a, dtype=np.float64))))
+
+    def get_field(self, g: int, field: int, shape) -> np.ndarray:
+        out = np.zeros(shape)
+        self.check(self.L.vfs_get_field(self.h, g, field, dptr(out)))
+        return out
+
+    def volume_flux(self, g: int):
+        out = np.zeros(4)
+        self.check(self.L.vfs_volume_flux(self.h, g, dptr(out)))
+        return out
+
+    def poisson_rhs(self, g: int, dt=0.04, st=1.0, coeff=1.0, meanfix=True) -> float:
+        s = ctypes.c_double()
+        self.check(self.L.vfs_poisson_rhs(self.h, g, dt, st, coeff, int(meanfix), ctypes.byref(s)))
+        return s.value
+
+    def poisson_solve(self, g: int, params: SolveParams, allow_notconv=False):
+        info = SolveInfo()
+        rc = self.L.vfs_poisson_solve(self.h, g, ctypes.byref(params), ctypes.byref(info))
+        if rc and not (allow_notconv and rc == VFS_ERR_NOTCONV):
+            self.check(rc)
+        return info.as_dict()
+
+    def update_pressure(self, g: int):
+        self.check(self.L.vfs_update_pressure(self.h, g))
+
+    def projection(self, g: int, dt=0.04, st=1.0, coeff=1.0):
+        self.check(self.L.vfs_projection(self.h, g, dt, st, coeff))
+
+    def divergence_max(self, g: int) -> float:
+        v = ctypes.c_double()
+        self.check(self.L.vfs_divergence_max(self.h, g, ctypes.byref(v)))
+        return v.value
+
+    def projection_step(self, g: int, params: SolveParams, ucont: np.ndarray = None, p: np.ndarray = None, dt=0.04,
+                        st=1.0, coeff=1.0):
+        info = SolveInfo()
+        dm = ctypes.c_double()
+        self.check(self.L.vfs_projection_step(self.h, g, dptr(ucont), dptr(p), dt, st, coeff, ctypes.byref(params),
+                                              ctypes.byref(info), ctypes.byref(dm)))
+        return info.as_dict(), dm.value
+
+    def projection_step_ptr(self, g: int, params: SolveParams, ucont_ptr: int, p_ptr: int, dt=0.04, st=1.0,
+                            coeff=1.0):
+        """Same as projection_step with raw host addresses (e.g. pinned buffers)."""
+        info = SolveInfo()
+        dm = ctypes.c_double()
+        self.check(self.L.vfs_projection_step(self.h, g, ctypes.cast(ucont_ptr, _DP) if ucont_ptr else None,
+                                              ctypes.cast(p_ptr, _DP) if p_ptr else None, dt, st, coeff,
+                                              ctypes.byref(params), ctypes.byref(info), ctypes.byref(dm)))
+        return info.as_dict(), dm.value
+
+    def projection_step_batch(self, grids, params: SolveParams, dt=0.04, st=1.0, coeff=1.0):
+        n = len(grids)
+        ids = (ctypes.c_int * n)(*grids)
+        infos = (SolveInfo * n)()
+        dm = np.zeros(n)
+        self.check(self.L.vfs_projection_step_batch(self.h, n, ids, dt, st, coeff, ctypes.byref(params), infos,
+                                                    dptr(dm)))
+        return [i.as_dict() for i in infos], dm
+
+    def sync(self):
+        self.check(self.L.vfs_sync(self.h))
+
+    def mark(self, g: int, slot: int):
+        self.check(self.L.vfs_mark(self.h, g, slot))
+
+    def elapsed(self, a: int, b: int) -> float:
+        ms = ctypes.c_double()
+        self.check(self.L.vfs_elapsed(self.h, a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def probe_begin(self, kernel: int):
+        self.check(self.L.vfs_probe_begin(self.h, kernel))
+
+    def probe_end(self):
+        n = ctypes.c_ulonglong()
+        ms = ctypes.c_double()
+        by = ctypes.c_double()
+        self.check(self.L.vfs_probe_end(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(by)))
+        return n.value, ms.value, by.value
+
+    def host_register(self, a: np.ndarray):
+        rc = self.L.vfs_host_register(a.ctypes.data_as(_P), a.nbytes)
+        if rc:
+            raise VfsError(rc, "cudaHostRegister failed")
+
+    def host_unregister(self, a: np.ndarray):
+        self.L.vfs_host_unregister(a.ctypes.data_as(_P))
+
+    # -- hooks --
+    def metrics(self, g: int, level: int) -> np.ndarray:
+        mx, my, mz = self.level_dims(g, level)
+        out = np.zeros(43 * mx * my * mz)
+        self.check(self.L.vfs_get_metrics(self.h, g, level, dptr(out)))
+        return out
+
+    def coef(self, g: int, level: int, which: int = 0) -> np.ndarray:
+        mx, my, mz = self.level_dims(g, level)
+        out = np.zeros(19 * mx * my * mz)
+        self.check(self.L.vfs_get_coef(self.h, g, level, which, dptr(out)))
+        return out.reshape((19, mz, my, mx))
+
+    def level_nvert(self, g: int, level: int) -> np.ndarray:
+        mx, my, mz = self.level_dims(g, level)
+        out = np.zeros((mz, my, mx))
+        self.check(self.L.vfs_get_level_nvert(self.h, g, level, dptr(out)))
+        return out
+
+    def apply_op(self, g: int, level: int, which: int, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self.check(self.L.vfs_apply_op(self.h, g, level, which, dptr(x), dptr(y)))
+        return y
+
+    def apply_precond(self, g: int, precision: int, params: SolveParams, v: np.ndarray) -> np.ndarray:
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        z = np.zeros_like(v)
+        self.check(self.L.vfs_apply_precond(self.h, g, precision, ctypes.byref(params), dptr(v), dptr(z)))
+        return z
+
+    def mg_restrict(self, g: int, level: int, x: np.ndarray) -> np.ndarray:
+        mx, my, mz = self.level_dims(g, level - 1)
+        y = np.zeros((mz, my, mx))
+        self.check(self.L.vfs_mg_restrict(self.h, g, level, dptr(np.ascontiguousarray(x, dtype=np.float64)), dptr(y)))
+        return y
+
+    def mg_prolong(self, g: int, level: int, x: np.ndarray) -> np.ndarray:
+        mx, my, mz = self.level_dims(g, level)
+        y = np.zeros((mz, my, mx))
+        self.check(self.L.vfs_mg_prolong(self.h, g, level, dptr(np.ascontiguousarray(x, dtype=np.float64)), dptr(y)))
+        return y
+
+    def mg_smooth(self, g: int, level: int, b: np.ndarray, x: np.ndarray, omega: float) -> np.ndarray:
+        x = np.array(x, dtype=np.float64, copy=True, order="C")
+        self.check(self.L.vfs_mg_smooth(self.h, g, level, dptr(np.ascontiguousarray(b, dtype=np.float64)), dptr(x),
+                                        omega))
+        return x

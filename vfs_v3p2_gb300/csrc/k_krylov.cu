@@ -1,0 +1,271 @@
+// Flexible GMRES(m) in FP64 with all scalars on the device.
+//
+// The Krylov basis V (m+1 vectors) is FP64; the preconditioned directions Z
+// are in the multigrid precision T.  Gram-Schmidt is classical with one
+// re-orthogonalisation pass (CGS2), each pass a deterministic multi-dot
+// (fixed block partials summed in index order by one block) followed by one
+// fused update sweep.  The Hessenberg column, Givens rotations and the
+// residual estimate live in a KrylovState in device memory and are updated
+// by a single-block kernel, so the host enqueues iterations without reading
+// anything back; every kernel returns immediately once st->done is set.
+#include "vfs_common.cuh"
+#include "vfs_proj.h"
+
+namespace vfs {
+
+constexpr int KB = 256;
+
+int krylov_nblocks(size_t n) {
+  size_t b = (n + KB * 4 - 1) / (KB * 4);
+  if (b > 152 * 4) b = 152 * 4;
+  return (int)(b ? b : 1);
+}
+
+__device__ __forceinline__ bool is_done(const KrylovState* st) { return *(volatile const int*)&st->done; }
+
+// ||v||^2 partials; then finish: is_b ? bnorm : beta (+ g[0], done check).
+__global__ void __launch_bounds__(KB) k_sq_partials(const KrylovState* st, const double* __restrict__ v, size_t n,
+                                                     double* parts, int check_done) {
+  if (check_done && is_done(st)) return;
+  __shared__ double sh[32];
+  double s = 0.;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    double a = v[t];
+    s = fma(a, a, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+__global__ void k_norm_finish(KrylovState* st, const double* __restrict__ parts, int nparts, int is_b) {
+  if (!is_b && is_done(st)) return;
+  __shared__ double sh[32];
+  double s = 0.;
+  for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[p];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) {
+    double nrm = sqrt(s);
+    if (is_b) {
+      st->bnorm = nrm;
+      st->done = (nrm == 0.) ? 1 : 0;
+      st->it = 0;
+      st->j = 0;
+    } else {
+      st->beta = nrm;
+      st->resid = nrm;
+      for (int q = 0; q <= st->m; q++) st->g[q] = 0.;
+      st->g[0] = nrm;
+      for (int q = 0; q < (st->m + 1) * st->m; q++) st->H[q] = 0.;
+      st->j = 0;
+      st->inv_hn = nrm > 0. ? 1. / nrm : 0.;
+      if (nrm <= st->rtol * st->bnorm) st->done = 1;
+    }
+  }
+}
+
+int launch_norm_init(KrylovState* st, const double* r, size_t n, double* parts, int is_b, cudaStream_t s) {
+  const int nb = krylov_nblocks(n);
+  k_sq_partials<<<nb, KB, 0, s>>>(st, r, n, parts, !is_b); ++g_launches;
+  k_norm_finish<<<1, KB, 0, s>>>(st, parts, nb, is_b); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// v0 = r * (1 / beta)
+__global__ void k_scale_vec(const KrylovState* st, const double* __restrict__ r, double* __restrict__ v, size_t n) {
+  if (is_done(st)) return;
+  const double f = st->inv_hn;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) v[t] = r[t] * f;
+}
+int launch_vec_scale_first(KrylovState* st, const double* r, double* v0, size_t n, cudaStream_t s) {
+  k_scale_vec<<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, r, v0, n); ++g_launches;
+  return (int)cudaGetLastError();
+}
+int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStream_t s) {
+  k_scale_vec<<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, n); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Multi-dot partials: parts[b * ld + q] = sum over the block's cells of V_q . w
+// for q < nv, chunks of 4 columns per sweep (w is re-read from L2).
+__global__ void __launch_bounds__(KB) k_multidot(const KrylovState* st, const double* __restrict__ V, int nv,
+                                                 const double* __restrict__ w, size_t n, double* parts, int ld) {
+  if (is_done(st)) return;
+  __shared__ double sh[32];
+  for (int q0 = 0; q0 < nv; q0 += 4) {
+    double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
+    const int nq = min(4, nv - q0);
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+      const double wv = w[t];
+      a0 = fma(V[(size_t)q0 * n + t], wv, a0);
+      if (nq > 1) a1 = fma(V[(size_t)(q0 + 1) * n + t], wv, a1);
+      if (nq > 2) a2 = fma(V[(size_t)(q0 + 2) * n + t], wv, a2);
+      if (nq > 3) a3 = fma(V[(size_t)(q0 + 3) * n + t], wv, a3);
+    }
+    a0 = block_sum(a0, sh);
+    if (nq > 1) a1 = block_sum(a1, sh);
+    if (nq > 2) a2 = block_sum(a2, sh);
+    if (nq > 3) a3 = block_sum(a3, sh);
+    if (threadIdx.x == 0) {
+      parts[(size_t)blockIdx.x * ld + q0] = a0;
+      if (nq > 1) parts[(size_t)blockIdx.x * ld + q0 + 1] = a1;
+      if (nq > 2) parts[(size_t)blockIdx.x * ld + q0 + 2] = a2;
+      if (nq > 3) parts[(size_t)blockIdx.x * ld + q0 + 3] = a3;
+    }
+  }
+}
+
+// Sum the multi-dot partials into st->h (and accumulate the column in hacc).
+__global__ void k_multidot_finish(KrylovState* st, const double* __restrict__ parts, int nparts, int nv, int ld, int pass) {
+  if (is_done(st)) return;
+  __shared__ double sh[32];
+  for (int q = 0; q < nv; q++) {
+    double s = 0.;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[(size_t)p * ld + q];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) {
+      st->h[q] = s;
+      st->hacc[q] = (pass == 1) ? s : st->hacc[q] + s;
+    }
+    __syncthreads();
+  }
+}
+
+int launch_multidot(KrylovState* st, const double* V, int nv, const double* w, size_t n, double* parts, int pass,
+                    cudaStream_t s) {
+  const int nb = krylov_nblocks(n);
+  const int ld = 72;
+  k_multidot<<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches;
+  k_multidot_finish<<<1, KB, 0, s>>>(st, parts, nb, nv, ld, pass); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// w -= sum_q h[q] V_q, with the partials of ||w||^2 after the update.
+__global__ void __launch_bounds__(KB) k_gs_update(const KrylovState* st, const double* __restrict__ V, int nv,
+                                                  double* __restrict__ w, size_t n, double* parts) {
+  if (is_done(st)) return;
+  __shared__ double sh[32];
+  __shared__ double hs[72];
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) hs[q] = st->h[q];
+  __syncthreads();
+  double s = 0.;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    double a = w[t];
+    for (int q = 0; q < nv; q++) a = fma(-hs[q], V[(size_t)q * n + t], a);
+    w[t] = a;
+    s = fma(a, a, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, int pass,
+                     cudaStream_t s) {
+  (void)pass;
+  k_gs_update<<<krylov_nblocks(n), KB, 0, s>>>(st, V, nv, w, n, parts); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Close Arnoldi column j: ||w||, Hessenberg column, Givens rotation, residual
+// estimate |g[j+1]|, convergence test, 1 / h[j+1][j] for the next basis vector.
+__global__ void k_arnoldi_finish(KrylovState* st, const double* __restrict__ parts, int nparts) {
+  if (is_done(st)) return;
+  __shared__ double sh[32];
+  double s = 0.;
+  for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[p];
+  s = block_sum(s, sh);
+  if (threadIdx.x != 0) return;
+  const int m = st->m, j = st->j;
+  const double hn = sqrt(s);
+  double* Hc = st->H + (size_t)j * (m + 1);
+  for (int q = 0; q <= j; q++) Hc[q] = st->hacc[q];
+  Hc[j + 1] = hn;
+  for (int q = 0; q < j; q++) {
+    const double a = Hc[q], b = Hc[q + 1];
+    Hc[q] = st->cs[q] * a + st->sn[q] * b;
+    Hc[q + 1] = -st->sn[q] * a + st->cs[q] * b;
+  }
+  const double a = Hc[j], b = Hc[j + 1];
+  const double den = sqrt(a * a + b * b);
+  const double c = den > 0. ? a / den : 1., sn = den > 0. ? b / den : 0.;
+  st->cs[j] = c;
+  st->sn[j] = sn;
+  Hc[j] = den;
+  Hc[j + 1] = 0.;
+  st->g[j + 1] = -sn * st->g[j];
+  st->g[j] = c * st->g[j];
+  st->resid = fabs(st->g[j + 1]);
+  st->hn = hn;
+  st->inv_hn = hn > 0. ? 1. / hn : 0.;
+  st->j = j + 1;
+  st->it += 1;
+  if (st->resid <= st->rtol * st->bnorm || hn == 0. || !(st->resid == st->resid)) st->done = 1;
+}
+int launch_arnoldi_finish(KrylovState* st, int nparts, const double* parts, cudaStream_t s) {
+  k_arnoldi_finish<<<1, KB, 0, s>>>(st, parts, nparts); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// y = R^{-1} g over the st->j closed columns (runs whether or not done).
+__global__ void k_lsq(KrylovState* st) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = st->m, J = st->j;
+  for (int q = J - 1; q >= 0; q--) {
+    double s = st->g[q];
+    for (int p = q + 1; p < J; p++) s -= st->H[(size_t)p * (m + 1) + q] * st->y[p];
+    st->y[q] = s / st->H[(size_t)q * (m + 1) + q];
+  }
+}
+int launch_lsq_update(KrylovState* st, cudaStream_t s) {
+  k_lsq<<<1, 32, 0, s>>>(st); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// x += sum_q y_q Z_q over the closed columns.
+template <typename T>
+__global__ void __launch_bounds__(KB) k_x_update(const KrylovState* st, const T* __restrict__ Z, size_t n, double* x) {
+  __shared__ double ys[72];
+  const int J = st->j;
+  for (int q = threadIdx.x; q < J; q += blockDim.x) ys[q] = st->y[q];
+  __syncthreads();
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    double a = x[t];
+    for (int q = 0; q < J; q++) a = fma(ys[q], (double)Z[(size_t)q * n + t], a);
+    x[t] = a;
+  }
+}
+template <typename T>
+int launch_x_update(KrylovState* st, const T* Z, size_t n, double* x, cudaStream_t s) {
+  k_x_update<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, Z, n, x); ++g_launches;
+  return (int)cudaGetLastError();
+}
+template int launch_x_update<float>(KrylovState*, const float*, size_t, double*, cudaStream_t);
+template int launch_x_update<double>(KrylovState*, const double*, size_t, double*, cudaStream_t);
+
+// Mark the closed columns as applied (a later x update adds nothing).
+__global__ void k_restart_reset(KrylovState* st) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) st->j = 0;
+}
+int launch_restart_reset(KrylovState* st, cudaStream_t s) {
+  k_restart_reset<<<1, 32, 0, s>>>(st); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// out = ||v||_2 (no Krylov state involved).
+__global__ void k_sqrt_sum(const double* __restrict__ parts, int nparts, double* out) {
+  __shared__ double sh[32];
+  double s = 0.;
+  for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[p];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = sqrt(s);
+}
+int launch_norm2(const double* v, size_t n, double* parts, double* out, cudaStream_t s) {
+  const int nb = krylov_nblocks(n);
+  k_sq_partials<<<nb, KB, 0, s>>>(nullptr, v, n, parts, 0); ++g_launches;
+  k_sqrt_sum<<<1, KB, 0, s>>>(parts, nb, out); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s) {
+  return (int)cudaMemcpyAsync(hst, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+}
+
+}  // namespace vfs

@@ -1,0 +1,365 @@
+// Hot-path stencil kernels: the FP64 outer operator apply / residual and the
+// multigrid preconditioner (y-line smoother, residual + restriction,
+// prolongation + correction, coarsest-level dense solve), templated on the
+// working precision (float for the mixed solver, double for the plain FP64
+// solver).
+//
+// All stencil kernels walk the interior with a (32 x 8) thread tile in (i, j)
+// and march a chunk of k planes per block: a warp reads 32 consecutive i of
+// every coefficient row (coalesced), the x neighbours of the 19-point stencil
+// come back through L1/L2.  Slots that are zero on the whole level (mask bit
+// clear) are skipped with a warp-uniform branch, so a grid whose metric has
+// no i-j or j-k cross terms streams 11 coefficient arrays instead of 19.
+#include "vfs_common.cuh"
+#include "vfs_kernels.h"
+
+namespace vfs {
+
+constexpr int TX = 32, TY = 8, KCHUNK = 4;
+
+__host__ __forceinline__ dim3 tile_grid(const Dims& d) {
+  const int ni = d.mx - 2, nj = d.my - 2, nk = d.mz - 2;
+  return dim3((ni + TX - 1) / TX, (nj + TY - 1) / TY, (nk + KCHUNK - 1) / KCHUNK);
+}
+
+#define TILE_LOOP(d)                                                       \
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;                         \
+  const int j = 1 + blockIdx.y * TY + threadIdx.y;                         \
+  const bool _in = (i <= (d).mx - 2) && (j <= (d).my - 2);                 \
+  const int _k0 = 1 + blockIdx.z * KCHUNK;                                 \
+  const int _k1 = min(_k0 + KCHUNK, (d).mz - 1);                           \
+  for (int k = _k0; k < _k1; k++)
+
+// sum_m coef[m] * x[nbr(m)] for interior cell (i, j, k), accumulated in A.
+template <typename TC, typename TX_, typename TA>
+__device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef, unsigned mask, const TX_* __restrict__ x,
+                                      int i, int j, int k) {
+  const size_t N = ncell(d);
+  const size_t c = cidx(d, i, j, k);
+  const int im = wrapi(i - 1, d.mx, d.ip), ip1 = wrapi(i + 1, d.mx, d.ip);
+  const int jm = wrapi(j - 1, d.my, d.jp), jp1 = wrapi(j + 1, d.my, d.jp);
+  const int km = wrapi(k - 1, d.mz, d.kp), kp1 = wrapi(k + 1, d.mz, d.kp);
+  const int II[3] = {im, i, ip1}, JJ[3] = {jm, j, jp1}, KK[3] = {km, k, kp1};
+  TA s = TA(0);
+#pragma unroll
+  for (int m = 0; m < 19; m++) {
+    if (mask & (1u << m)) {
+      const size_t n = cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]);
+      s = fma((TA)__ldg(coef + (size_t)m * N + c), (TA)__ldg(x + n), s);
+    }
+  }
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 outer operator: y = A x, or y = b - A x.
+// ---------------------------------------------------------------------------
+template <typename TXin>
+__global__ void __launch_bounds__(TX* TY) k_apply64(OpView<double> A, const TXin* __restrict__ x, const double* __restrict__ b,
+                                                    double* __restrict__ y) {
+  if (skipped(A.skip)) return;
+  TILE_LOOP(A.d) {
+    if (!_in) continue;
+    const size_t c = cidx(A.d, i, j, k);
+    double s = stencil<double, TXin, double>(A.d, A.coef, A.mask, x, i, j, k);
+    y[c] = b ? b[c] - s : s;
+  }
+}
+
+int launch_apply64(const OpView<double>& A, const double* x, const double* b, double* y, cudaStream_t s) {
+  k_apply64<double><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  return (int)cudaGetLastError();
+}
+int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, double* y, cudaStream_t s) {
+  k_apply64<float><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TX* TY) k_apply_mg(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+                                                     T* __restrict__ y) {
+  if (skipped(A.skip)) return;
+  TILE_LOOP(A.d) {
+    if (!_in) continue;
+    const size_t c = cidx(A.d, i, j, k);
+    T s = stencil<T, T, T>(A.d, A.coef, A.mask, x, i, j, k);
+    y[c] = b ? b[c] - s : s;
+  }
+}
+template <typename T>
+int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s) {
+  k_apply_mg<T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Damped y-line Jacobi sweep.  One block owns a tile of TW consecutive
+// i-columns x all j of one k plane.  Phase 1 (all threads, coalesced over i):
+// the residual r = b - A x and the tridiagonal (SP, CP, NP) entries of every
+// cell of the tile go to shared memory.  Phase 2 (one thread per column):
+// Thomas elimination in shared memory.  Phase 3: xo = xi + omega * delta.
+// Couplings across a j-periodic seam and to non-fluid cells stay in the
+// residual (off-line); non-fluid cells are identity rows with delta = 0.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict__ xi, const T* __restrict__ b,
+                                                T* __restrict__ xo, T omega, int TW) {
+  if (skipped(A.skip)) return;
+  extern __shared__ unsigned char smraw[];
+  const Dims d = A.d;
+  const int nj = d.my - 2;
+  T* sr = (T*)smraw;
+  T* sa = sr + TW * nj;
+  T* sd = sa + TW * nj;
+  T* sc = sd + TW * nj;
+  const size_t N = ncell(d);
+  const int i0 = 1 + blockIdx.x * TW;
+  const int k = 1 + blockIdx.y;
+  const int nt = TW * nj;
+  for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
+    const int il = idx % TW, jl = idx / TW;
+    const int i = i0 + il, j = 1 + jl;
+    T r = T(0), a = T(0), dd = T(1), cc = T(0);
+    if (i <= d.mx - 2) {
+      const size_t c = cidx(d, i, j, k);
+      const T cp = A.coef[c];
+      if (cp != T(0)) {
+        T ax = xi ? stencil<T, T, T>(d, A.coef, A.mask, xi, i, j, k) : T(0);
+        r = b[c] - ax;
+        dd = cp;
+        a = (j > 1) ? A.coef[(size_t)SP * N + c] : T(0);
+        cc = (j < d.my - 2) ? A.coef[(size_t)NP * N + c] : T(0);
+      }
+    }
+    sr[idx] = r;
+    sa[idx] = a;
+    sd[idx] = dd;
+    sc[idx] = cc;
+  }
+  __syncthreads();
+  if (threadIdx.x < TW) {
+    const int il = threadIdx.x;
+    T cprev = T(0), dprev = T(0);
+    for (int jl = 0; jl < nj; jl++) {
+      const int q = jl * TW + il;
+      const T a = sa[q];
+      const T inv = T(1) / (sd[q] - a * cprev);
+      cprev = sc[q] * inv;
+      dprev = (sr[q] - a * dprev) * inv;
+      sc[q] = cprev;
+      sr[q] = dprev;
+    }
+    T xn = T(0);
+    for (int jl = nj - 1; jl >= 0; jl--) {
+      const int q = jl * TW + il;
+      xn = sr[q] - sc[q] * xn;
+      sr[q] = xn;
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
+    const int il = idx % TW, jl = idx / TW;
+    const int i = i0 + il, j = 1 + jl;
+    if (i > d.mx - 2) continue;
+    const size_t c = cidx(d, i, j, k);
+    const T x0 = xi ? xi[c] : T(0);
+    xo[c] = x0 + omega * sr[idx];
+  }
+}
+
+template <typename T>
+static int smooth_tw(int nj) {
+  int tw = 32;
+  while (tw > 4 && (size_t)4 * tw * nj * sizeof(T) > 64 * 1024) tw >>= 1;
+  return tw;
+}
+
+template <typename T>
+int launch_smooth(const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_smooth<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
+  const int tw = smooth_tw<T>(nj);
+  const size_t sm = (size_t)4 * tw * nj * sizeof(T);
+  dim3 g((ni + tw - 1) / tw, nk);
+  k_smooth<T><<<g, 256, sm, s>>>(A, xi, b, xo, omega, tw); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Residual + restriction (MyRestriction, poisson.c:364-471), one thread per
+// coarse interior cell: bc = 0.125 * sum over the 8 children of
+// (b - A x) * max(0, 1 - nvert_f), 0 on solid coarse cells; xc = 0.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+                                                        const double* __restrict__ nvf, Dims c, const double* __restrict__ nvc,
+                                                        int si, int sj, int sk, T* __restrict__ bc, T* __restrict__ xc) {
+  if (skipped(A.skip)) return;
+  const int ia = si ? 0 : 1, ja = sj ? 0 : 1, ka = sk ? 0 : 1;
+  TILE_LOOP(c) {
+    if (!_in) continue;
+    const size_t q = cidx(c, i, j, k);
+    T acc = T(0);
+    if (!(nvc[q] > 0.1)) {
+      const int ih = si ? i : 2 * i, jh = sj ? j : 2 * j, kh = sk ? k : 2 * k;
+      const int oi[8] = {0, ia, 0, 0, ia, 0, ia, ia}, oj[8] = {0, 0, ja, 0, ja, ja, 0, ja},
+                ok[8] = {0, 0, 0, ka, 0, ka, ka, ka};
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int fi = ih - oi[t], fj = jh - oj[t], fk = kh - ok[t];
+        const size_t fc = cidx(A.d, fi, fj, fk);
+        const double w = fmax(0., 1. - nvf[fc]);
+        T r = T(0);
+        if (w != 0.) {
+          T ax = x ? stencil<T, T, T>(A.d, A.coef, A.mask, x, fi, fj, fk) : T(0);
+          r = (b[fc] - ax) * (T)w;
+        }
+        acc += r;
+      }
+      acc *= T(0.125);
+    }
+    bc[q] = acc;
+    xc[q] = T(0);
+  }
+}
+
+template <typename T>
+int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
+                             const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
+  k_resrestrict<T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+__global__ void k_restrict_plain(Dims f, const T* __restrict__ x, const double* __restrict__ nvf, Dims c,
+                                 const double* __restrict__ nvc, int si, int sj, int sk, T* __restrict__ out) {
+  const int ia = si ? 0 : 1, ja = sj ? 0 : 1, ka = sk ? 0 : 1;
+  TILE_LOOP(c) {
+    if (!_in) continue;
+    const size_t q = cidx(c, i, j, k);
+    const int ih = si ? i : 2 * i, jh = sj ? j : 2 * j, kh = sk ? k : 2 * k;
+    const int oi[8] = {0, ia, 0, 0, ia, 0, ia, ia}, oj[8] = {0, 0, ja, 0, ja, ja, 0, ja}, ok[8] = {0, 0, 0, ka, 0, ka, ka, ka};
+    T acc = T(0);
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      const size_t fc = cidx(f, ih - oi[t], jh - oj[t], kh - ok[t]);
+      acc += x[fc] * (T)fmax(0., 1. - nvf[fc]);
+    }
+    acc *= T(0.125);
+    out[q] = (nvc[q] > 0.1) ? T(0) : acc;
+  }
+}
+template <typename T>
+int launch_restrict(const Dims& f, const T* x, const double* nvf, const Dims& c, const double* nvc, int si, int sj, int sk,
+                    T* out, cudaStream_t s) {
+  k_restrict_plain<T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(f, x, nvf, c, nvc, si, sj, sk, out); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Prolongation + correction (MyInterpolation, poisson.c:526-669), one thread
+// per fine interior cell, offsets from the precomputed code.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(TX* TY) k_prolong(Dims f, const uint8_t* __restrict__ code, Dims c, const T* __restrict__ xc,
+                                                    T* __restrict__ xf, int add, int si, int sj, int sk,
+                                                    const int* skip) {
+  if (skipped(skip)) return;
+  TILE_LOOP(f) {
+    if (!_in) continue;
+    const size_t q = cidx(f, i, j, k);
+    const uint8_t cd = code[q];
+    T v = T(0);
+    if (!(cd & 0x80)) {
+      const int ia = (cd & 3) - 1, ja = ((cd >> 2) & 3) - 1, ka = ((cd >> 4) & 3) - 1;
+      const int ic = si ? i : (i + 1) / 2, jc = sj ? j : (j + 1) / 2, kc = sk ? k : (k + 1) / 2;
+#define X(a, b, cc) xc[cidx(c, a, b, cc)]
+      v = (X(ic, jc, kc) * T(9) + X(ic, jc + ja, kc) * T(3) + X(ic + ia, jc, kc) * T(3) + X(ic + ia, jc + ja, kc)) * (T(3) / T(64)) +
+          (X(ic, jc, kc + ka) * T(9) + X(ic, jc + ja, kc + ka) * T(3) + X(ic + ia, jc, kc + ka) * T(3) +
+           X(ic + ia, jc + ja, kc + ka)) / T(64);
+#undef X
+    }
+    xf[q] = add ? xf[q] + v : v;
+  }
+}
+template <typename T>
+int launch_prolong(const Dims& f, const uint8_t* code, const Dims& c, const T* xc, T* xf, int add, const int* skip,
+                   cudaStream_t s) {
+  // semi-coarsening flags are implied by equal extents
+  const int si = (c.mx == f.mx), sj = (c.my == f.my), sk = (c.mz == f.mz);
+  k_prolong<T><<<tile_grid(f), dim3(TX, TY), 0, s>>>(f, code, c, xc, xf, add, si, sj, sk, skip); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Coarsest level: x = Binv b over the packed interior (dense, one warp per row).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarse_gemv(Dims d, const T* __restrict__ Binv, int n, const T* __restrict__ b,
+                                                     T* __restrict__ x, const int* skip) {
+  if (skipped(skip)) return;
+  extern __shared__ unsigned char smraw[];
+  T* sb = (T*)smraw;
+  const int ni = d.mx - 2, nj = d.my - 2;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const int i = 1 + r % ni, j = 1 + (r / ni) % nj, k = 1 + r / (ni * nj);
+    sb[r] = b[cidx(d, i, j, k)];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * 8 + warp;
+  if (row >= n) return;
+  const T* Br = Binv + (size_t)row * n;
+  T s = T(0);
+  for (int col = lane; col < n; col += 32) s = fma(Br[col], sb[col], s);
+  s = warp_sum(s);
+  if (lane == 0) {
+    const int i = 1 + row % ni, j = 1 + (row / ni) % nj, k = 1 + row / (ni * nj);
+    x[cidx(d, i, j, k)] = s;
+  }
+}
+template <typename T>
+int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const int* skip, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_coarse_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_coarse_gemv<T><<<(n + 7) / 8, 256, (size_t)n * sizeof(T), s>>>(d, Binv, n, b, x, skip); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TX* TY) k_scale_in(Dims d, const double* __restrict__ aj, const double* __restrict__ v,
+                                                     T* __restrict__ out, const int* skip) {
+  if (skipped(skip)) return;
+  TILE_LOOP(d) {
+    if (!_in) continue;
+    const size_t c = cidx(d, i, j, k);
+    out[c] = (T)(aj[c] * v[c]);
+  }
+}
+template <typename T>
+int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s) {
+  k_scale_in<T><<<tile_grid(d), dim3(TX, TY), 0, s>>>(d, aj, v, out, skip); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+#define INST(T)                                                                                                        \
+  template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, T*, T, cudaStream_t);                           \
+  template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const double*, const Dims&,           \
+                                           const double*, int, int, int, T*, T*, cudaStream_t);                       \
+  template int launch_restrict<T>(const Dims&, const T*, const double*, const Dims&, const double*, int, int, int, T*, \
+                                  cudaStream_t);                                                                      \
+  template int launch_prolong<T>(const Dims&, const uint8_t*, const Dims&, const T*, T*, int, const int*, cudaStream_t); \
+  template int launch_coarse_gemv<T>(const Dims&, const T*, int, const T*, T*, const int*, cudaStream_t);             \
+  template int launch_scale_in<T>(const Dims&, const double*, const double*, T*, const int*, cudaStream_t);
+INST(float)
+INST(double)
+
+}  // namespace vfs

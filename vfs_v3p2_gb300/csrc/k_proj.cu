@@ -1,0 +1,511 @@
+// Per-step FP64 kernels around the solve: the divergence right-hand side and
+// its compatibility fix, the immersed-boundary flux balance, null-space
+// removal, the phi / pressure ghost fills, the contravariant velocity
+// correction (Projection), Contra2Cart and the divergence check.
+//
+// Compiled with --fmad=false like k_setup.cu: each kernel performs the
+// reference's multiplies and adds in the reference's order, so for equal
+// inputs the outputs are bit-identical (reductions excepted, which sum in a
+// fixed tree order instead of the reference's loop order).
+#include "vfs_common.cuh"
+#include "vfs_kernels.h"
+#include "vfs_proj.h"
+
+namespace vfs {
+
+constexpr int RB = 256;  // reduction block size
+
+#define GRID_LOOP(d)                                                                          \
+  for (size_t _t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; _t < ncell(d);              \
+       _t += (size_t)gridDim.x * blockDim.x)
+#define DECOMP(d, i, j, k)               \
+  int i = (int)(_t % (d).mx);            \
+  int j = (int)((_t / (d).mx) % (d).my); \
+  int k = (int)(_t / ((size_t)(d).mx * (d).my))
+
+static inline int nblk(size_t n, int bs = 256) {
+  size_t b = (n + bs - 1) / bs;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)(b ? b : 1);
+}
+
+// Sum per-block partials [nparts][q] in index order (one block).
+__global__ void k_finish_sums(const double* __restrict__ parts, int nparts, int nq, double* out) {
+  __shared__ double sh[32];
+  for (int q = 0; q < nq; q++) {
+    double s = 0.;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[(size_t)p * nq + q];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[q] = s;
+    __syncthreads();
+  }
+}
+__global__ void k_finish_max(const double* __restrict__ parts, int nparts, double* out) {
+  __shared__ double sh[32];
+  double s = 0.;
+  for (int p = threadIdx.x; p < nparts; p += blockDim.x) s = fmax(s, parts[p]);
+  s = block_max(s, sh);
+  if (threadIdx.x == 0) *out = s;
+}
+
+// ---- AoS (reference Cmpnts) <-> SoA device layout ----
+__global__ void k_aos2soa(size_t n, const double* __restrict__ a, double* x, double* y, double* z) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    x[t] = a[3 * t];
+    y[t] = a[3 * t + 1];
+    z[t] = a[3 * t + 2];
+  }
+}
+__global__ void k_soa2aos(size_t n, const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                          double* a) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    a[3 * t] = x[t];
+    a[3 * t + 1] = y[t];
+    a[3 * t + 2] = z[t];
+  }
+}
+int launch_aos2soa(size_t n, const double* aos, double* x, double* y, double* z, cudaStream_t s) {
+  k_aos2soa<<<nblk(n), 256, 0, s>>>(n, aos, x, y, z); ++g_launches;
+  return (int)cudaGetLastError();
+}
+int launch_soa2aos(size_t n, const double* x, const double* y, const double* z, double* aos, cudaStream_t s) {
+  k_soa2aos<<<nblk(n), 256, 0, s>>>(n, x, y, z, aos); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// PoissonRHS2_hypre (poisson_hypre.c:342-429): b = div(U*) * st * coeff / dt
+// on fluid cells, periodic wrap of the minus faces; partial sums of b and of
+// the fluid count for the compatibility fix of PoissonRHS2 (poisson.c:1879-1903).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RB) k_rhs(Dims d, Ucont u, const double* __restrict__ nvert, double dt, double st,
+                                            double coeff, double* b, double* parts) {
+  __shared__ double sh[32];
+  double lsum = 0., lcnt = 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    double val = 0.;
+    if (interior(d, i, j, k) && !(nvert[_t] >= 0.1)) {
+      val -= u.x[_t];
+      if (i == 1 && d.ip) val += u.x[cidx(d, d.mx - 2, j, k)];
+      else val += u.x[cidx(d, i - 1, j, k)];
+      val -= u.y[_t];
+      if (j == 1 && d.jp) val += u.y[cidx(d, i, d.my - 2, k)];
+      else val += u.y[cidx(d, i, j - 1, k)];
+      val -= u.z[_t];
+      if (k == 1 && d.kp) val += u.z[cidx(d, i, j, d.mz - 2)];
+      else val += u.z[cidx(d, i, j, k - 1)];
+      val *= -1.0 / dt * st * coeff;
+      lsum += val;
+      lcnt += 1.;
+    }
+    b[_t] = val;
+  }
+  lsum = block_sum(lsum, sh);
+  lcnt = block_sum(lcnt, sh);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = lsum;
+    parts[2 * blockIdx.x + 1] = lcnt;
+  }
+}
+// b += -sum / count on fluid interior cells (sc = {sum, count}).
+__global__ void k_meanfix(Dims d, const double* __restrict__ nvert, const double* __restrict__ sc, double* b) {
+  const double v = (sc[1] > 0.) ? -sc[0] / sc[1] : 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (interior(d, i, j, k) && nvert[_t] < 0.1) b[_t] += v;
+  }
+}
+int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, double st, double coeff, int meanfix,
+               double* b, double* parts, double* sc, cudaStream_t s) {
+  const int nb = nblk(ncell(d), RB);
+  k_rhs<<<nb, RB, 0, s>>>(d, u, nvert, dt, st, coeff, b, parts); ++g_launches;
+  k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, sc); ++g_launches;
+  if (meanfix) {
+    k_meanfix<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, sc, b);
+    ++g_launches;
+  }
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// IB flux balance.  mode 1: VolumeFlux(flg = 0), poisson.c:2898-3240
+// (immersed == 1).  mode 0: VolumeFlux(lUcor), poisson.c:2634-2828 with
+// immersed == 0, which zeroes every fluid / non-fluid face.
+// phase 0: (mode 1) zero faces with |U| <= 1e-10 and sum flux, area;
+// phase 1: apply the correction flux / area; phase 2: sums again.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nrm3(const double* v, size_t c) {
+  return sqrt(v[3 * c] * v[3 * c] + v[3 * c + 1] * v[3 * c + 1] + v[3 * c + 2] * v[3 * c + 2]);
+}
+
+__global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont u, const double* __restrict__ nv,
+                                              const double* __restrict__ csi, const double* __restrict__ eta,
+                                              const double* __restrict__ zet, const double* __restrict__ fa, double* parts) {
+  __shared__ double sh[32];
+  const double eps = 1.e-10, ibmval = 1.1;
+  double flux = 0., area = 0.;
+  double corr = 0.;
+  if (phase == 1) corr = (fa[1] > 1.e-15) ? fa[0] / fa[1] : 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k)) continue;
+    const size_t c = _t;
+    const size_t ce = cidx(d, i + 1, j, k), cn = cidx(d, i, j + 1, k), ct = cidx(d, i, j, k + 1);
+    double* uf[3] = {u.x, u.y, u.z};
+    const double* mt[3] = {csi, eta, zet};
+    const size_t nb[3] = {ce, cn, ct};
+    const bool lim1[3] = {i < d.mx - 2, j < d.my - 2, k < d.mz - 2};
+    const bool lim0[3] = {i <= d.mx - 2, j <= d.my - 2, k <= d.mz - 2};
+    for (int f = 0; f < 3; f++) {
+      double* uu = uf[f];
+      if (mode == 1) {
+        const bool plus = nv[c] < 0.1 && nv[nb[f]] > 0.1 && nv[nb[f]] < ibmval && lim1[f];
+        const bool minus = nv[c] > 0.1 && nv[c] < ibmval && nv[nb[f]] < 0.1 && lim1[f];
+        if (!(plus || minus)) continue;
+        if (phase == 0) {
+          if (fabs(uu[c]) > eps) {
+            flux += plus ? uu[c] : -uu[c];
+            area += nrm3(mt[f], c);
+          } else uu[c] = 0.;
+        } else if (phase == 1) {
+          if (fabs(uu[c]) > eps) {
+            if (plus) uu[c] -= nrm3(mt[f], c) * corr;
+            else uu[c] += nrm3(mt[f], c) * corr;
+          }
+        } else {
+          flux += plus ? uu[c] : -uu[c];
+          area += nrm3(mt[f], c);
+        }
+      } else {
+        const bool plus = nv[c] < VFS_THR && nv[nb[f]] > VFS_THR && lim0[f];
+        const bool minus = nv[c] > VFS_THR && nv[nb[f]] < VFS_THR && lim0[f];
+        if (!(plus || minus)) continue;
+        if (phase == 1) {
+          uu[c] = 0.;
+        } else {
+          flux += plus ? uu[c] : -uu[c];
+          area += nrm3(mt[f], c);
+        }
+      }
+    }
+  }
+  flux = block_sum(flux, sh);
+  area = block_sum(area, sh);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = flux;
+    parts[2 * blockIdx.x + 1] = area;
+  }
+}
+int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nvert, const double* M, double* parts,
+                       double* fa4, cudaStream_t s) {
+  const size_t N = ncell(d);
+  const int nb = nblk(N, RB);
+  const double *csi = M + N * MP_CSI, *eta = M + N * MP_ETA, *zet = M + N * MP_ZET;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 0, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
+  k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4); ++g_launches;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 1, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 2, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
+  k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4 + 2); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Remove_Nullspace (poisson_hypre.c:207-270): subtract the fluid mean of phi.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RB) k_fluid_sum(Dims d, const double* __restrict__ nvert, const double* __restrict__ x,
+                                                  double* parts) {
+  __shared__ double sh[32];
+  double s = 0., n = 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (interior(d, i, j, k) && nvert[_t] < 0.1) {
+      s += x[_t];
+      n += 1.;
+    }
+  }
+  s = block_sum(s, sh);
+  n = block_sum(n, sh);
+  if (threadIdx.x == 0) {
+    parts[2 * blockIdx.x] = s;
+    parts[2 * blockIdx.x + 1] = n;
+  }
+}
+__global__ void k_sub_mean(Dims d, const double* __restrict__ nvert, const double* __restrict__ sc, double* x) {
+  const double v = (sc[1] > 0.) ? -sc[0] / sc[1] : 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (interior(d, i, j, k) && nvert[_t] < 0.1) x[_t] += v;
+  }
+}
+int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s) {
+  const int nb = nblk(ncell(d), RB);
+  k_fluid_sum<<<nb, RB, 0, s>>>(d, nvert, x, parts); ++g_launches;
+  k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, sc); ++g_launches;
+  k_sub_mean<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, sc, x); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Convert_Phi2_Phi (poisson.c:97-185): zero on boundary and non-fluid cells.
+__global__ void k_phi_zero(Dims d, const double* __restrict__ nvert, double* phi) {
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k) || (int)nvert[_t] > VFS_THR) phi[_t] = 0.;
+  }
+}
+// Periodic ghost fill of a scalar (poisson.c:146-181, 2580-2616).
+__global__ void k_scalar_ghosts(Dims d, double* a) {
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    int ai = wrapi(i, d.mx, d.ip), bj = wrapi(j, d.my, d.jp), ck = wrapi(k, d.mz, d.kp);
+    if (ai != i || bj != j || ck != k) a[_t] = a[cidx(d, ai, bj, ck)];
+  }
+}
+int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStream_t s) {
+  k_phi_zero<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, phi); ++g_launches;
+  k_scalar_ghosts<<<nblk(ncell(d)), 256, 0, s>>>(d, phi); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// UpdatePressure (poisson.c:2522-2548, non-PRIMITIVE branch, + ghost fill).
+__global__ void k_update_p(Dims d, const double* __restrict__ nvert, const double* __restrict__ phi, double* p) {
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (interior(d, i, j, k) && nvert[_t] < 0.1) p[_t] += phi[_t];
+  }
+}
+int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s) {
+  k_update_p<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, phi, p); ++g_launches;
+  k_scalar_ghosts<<<nblk(ncell(d)), 256, 0, s>>>(d, p); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Projection (poisson.c:2202-2397): U^xi -= (dpdc g11 + dpde g12 + dpdz g13)
+// dt st / coeff at i faces (likewise j, k), with the LHS's one-sided /
+// centred / zero regimes for the cross derivatives; faces touching nvert are
+// left alone.  pd holds the nine metric dot products of each face family
+// (icsi.icsi, ieta.icsi, izet.icsi, jcsi.jeta, jeta.jeta, jzet.jeta,
+// kcsi.kzet, keta.kzet, kzet.kzet) and M the face Jacobians iaj, jaj, kaj,
+// multiplied in the reference's order: (dpdc * dot) * iaj.
+// ---------------------------------------------------------------------------
+__global__ void k_projection(Dims d, const double* __restrict__ pd, const double* __restrict__ iaj,
+                             const double* __restrict__ jaj, const double* __restrict__ kaj, const double* __restrict__ nvert,
+                             const double* __restrict__ phi, double dt, double st, double coeff, Ucont u) {
+  const size_t N = ncell(d);
+  const int mx = d.mx, my = d.my, mz = d.mz, ip = d.ip, jp = d.jp, kp = d.kp;
+  const double THR = VFS_THR;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    const size_t c = _t;
+#define NV(ii, jj, kk) nvert[cidx(d, ii, jj, kk)]
+#define PH(ii, jj, kk) phi[cidx(d, ii, jj, kk)]
+    const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+    double dpdc, dpde, dpdz;
+    if (j > 0 && j < my - 1 && k > 0 && k < mz - 1)
+      if ((i > 0 && i < mx - 2) || (ip && i == mx - 2)) {
+        dpdc = PH(i + 1, j, k) - PH(i, j, k);
+        if (i == mx - 2 && ip) dpdc = PH(1, j, k) - PH(i, j, k);
+        dpde = 0.;
+        dpdz = 0.;
+        if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > THR) {
+          if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < THR && (j != 1))
+            dpde = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.5;
+        } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > THR) {
+          if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < THR)
+            dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+        } else {
+          dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.25;
+        }
+        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > THR) {
+          if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < THR && (k != 1))
+            dpdz = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.5;
+        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > THR) {
+          if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < THR)
+            dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+        } else {
+          dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.25;
+        }
+        if ((NV(i, j, k) + NV(i + 1, j, k)) < THR) {
+          const double a = iaj[c];
+          u.x[c] -= (dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt * st / coeff / r1;
+        }
+      }
+    if (i > 0 && i < mx - 1 && k > 0 && k < mz - 1)
+      if ((j > 0 && j < my - 2) || (jp && j == my - 2)) {
+        dpdc = 0.;
+        dpdz = 0.;
+        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > THR) {
+          if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < THR && (i != 1))
+            dpdc = (PH(i, j, k) + PH(i, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.5;
+        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > THR) {
+          if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < THR)
+            dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+        } else {
+          dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
+        }
+        if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
+        else dpde = PH(i, j + 1, k) - PH(i, j, k);
+        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > THR) {
+          if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < THR && (k != 1))
+            dpdz = (PH(i, j, k) + PH(i, j + 1, k) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.5;
+        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > THR) {
+          if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < THR)
+            dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+        } else {
+          dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.25;
+        }
+        if ((NV(i, j, k) + NV(i, j + 1, k)) < THR) {
+          const double a = jaj[c];
+          u.y[c] -= (dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt * st / coeff / r2;
+        }
+      }
+    if (i > 0 && i < mx - 1 && j > 0 && j < my - 1)
+      if ((k > 0 && k < mz - 2) || (kp && k == mz - 2)) {
+        dpdc = 0.;
+        dpde = 0.;
+        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > THR) {
+          if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < THR && (i != 1))
+            dpdc = (PH(i, j, k) + PH(i, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.5;
+        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > THR) {
+          if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < THR)
+            dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+        } else {
+          dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.25;
+        }
+        if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > THR) {
+          if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < THR && (j != 1))
+            dpde = (PH(i, j, k) + PH(i, j, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.5;
+        } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > THR) {
+          if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < THR)
+            dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+        } else {
+          dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
+        }
+        if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
+        else dpdz = PH(i, j, k + 1) - PH(i, j, k);
+        if ((NV(i, j, k) + NV(i, j, k + 1)) < THR) {
+          const double a = kaj[c];
+          u.z[c] -= (dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt * st / coeff / r3;
+        }
+      }
+#undef PH
+#undef NV
+  }
+}
+
+// periodic ghost sync of the flagged component (poisson.c:2398-2437)
+__global__ void k_ucont_ghosts(Dims d, Ucont u) {
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    int a = wrapi(i, d.mx, d.ip), b = wrapi(j, d.my, d.jp), cc = wrapi(k, d.mz, d.kp);
+    if (a == i && b == j && cc == k) continue;
+    size_t s = cidx(d, a, b, cc);
+    if (a != i) u.x[_t] = u.x[s];
+    if (b != j) u.y[_t] = u.y[s];
+    if (cc != k) u.z[_t] = u.z[s];
+  }
+}
+
+// The nine metric dot products of the projection (same expressions as the
+// reference's Projection, poisson.c:2262-2360, without the Jacobian).
+__global__ void k_proj_dots(Dims d, const double* __restrict__ M, double* pd) {
+  const size_t N = ncell(d);
+  GRID_LOOP(d) {
+    const size_t c = _t;
+    const double* A = M + N * MP_ICSI + 3 * c;
+    const double* B = M + N * MP_IETA + 3 * c;
+    const double* E = M + N * MP_IZET + 3 * c;
+    pd[0 * N + c] = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+    pd[1 * N + c] = B[0] * A[0] + B[1] * A[1] + B[2] * A[2];
+    pd[2 * N + c] = E[0] * A[0] + E[1] * A[1] + E[2] * A[2];
+    A = M + N * MP_JCSI + 3 * c;
+    B = M + N * MP_JETA + 3 * c;
+    E = M + N * MP_JZET + 3 * c;
+    pd[3 * N + c] = A[0] * B[0] + A[1] * B[1] + A[2] * B[2];
+    pd[4 * N + c] = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    pd[5 * N + c] = E[0] * B[0] + E[1] * B[1] + E[2] * B[2];
+    A = M + N * MP_KCSI + 3 * c;
+    B = M + N * MP_KETA + 3 * c;
+    E = M + N * MP_KZET + 3 * c;
+    pd[6 * N + c] = A[0] * E[0] + A[1] * E[1] + A[2] * E[2];
+    pd[7 * N + c] = B[0] * E[0] + B[1] * E[1] + B[2] * E[2];
+    pd[8 * N + c] = E[0] * E[0] + E[1] * E[1] + E[2] * E[2];
+  }
+}
+int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s) {
+  k_proj_dots<<<nblk(ncell(d)), 256, 0, s>>>(d, M, pd); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const double* phi, double dt,
+                      double st, double coeff, const Ucont& u, cudaStream_t s) {
+  const size_t N = ncell(d);
+  k_projection<<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, phi, dt, st, coeff, u); ++g_launches;
+  k_ucont_ghosts<<<nblk(N), 256, 0, s>>>(d, u); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Contra2Cart (rhs.c:144-183): Cartesian velocity at fluid cells.
+__global__ void k_contra2cart(Dims d, const double* __restrict__ M, const double* __restrict__ nvert, Ucont u, double* ucat) {
+  const size_t N = ncell(d);
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k) || !(nvert[_t] < 0.1)) continue;
+    const size_t c = _t;
+    const double* A = M + N * MP_CSI + 3 * c;
+    const double* B = M + N * MP_ETA + 3 * c;
+    const double* E = M + N * MP_ZET + 3 * c;
+    const double q0 = 0.5 * (u.x[cidx(d, i - 1, j, k)] + u.x[c]);
+    const double q1 = 0.5 * (u.y[cidx(d, i, j - 1, k)] + u.y[c]);
+    const double q2 = 0.5 * (u.z[cidx(d, i, j, k - 1)] + u.z[c]);
+    const double det = A[0] * (B[1] * E[2] - B[2] * E[1]) - A[1] * (B[0] * E[2] - B[2] * E[0]) + A[2] * (B[0] * E[1] - B[1] * E[0]);
+    const double det0 = q0 * (B[1] * E[2] - B[2] * E[1]) - q1 * (A[1] * E[2] - A[2] * E[1]) + q2 * (A[1] * B[2] - A[2] * B[1]);
+    const double det1 = -q0 * (B[0] * E[2] - B[2] * E[0]) + q1 * (A[0] * E[2] - A[2] * E[0]) - q2 * (A[0] * B[2] - A[2] * B[0]);
+    const double det2 = q0 * (B[0] * E[1] - B[1] * E[0]) - q1 * (A[0] * E[1] - A[1] * E[0]) + q2 * (A[0] * B[1] - A[1] * B[0]);
+    ucat[3 * c] = det0 / det;
+    ucat[3 * c + 1] = det1 / det;
+    ucat[3 * c + 2] = det2 / det;
+  }
+}
+int launch_contra2cart(const Dims& d, const double* M, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s) {
+  k_contra2cart<<<nblk(ncell(d)), 256, 0, s>>>(d, M, nvert, u, ucat); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Divergence (main.c:1279-1349): max over cells of |div U| * aj, 0 where the
+// cell or a face neighbour carries nvert.
+__global__ void __launch_bounds__(RB) k_divergence(Dims d, Ucont u, const double* __restrict__ aj,
+                                                   const double* __restrict__ nvert, double* parts) {
+  __shared__ double sh[32];
+  double mxv = 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k)) continue;
+    const size_t c = _t;
+    double v = fabs((u.x[c] - u.x[cidx(d, i - 1, j, k)] + u.y[c] - u.y[cidx(d, i, j - 1, k)] + u.z[c] -
+                     u.z[cidx(d, i, j, k - 1)]) * aj[c]);
+    if (nvert[c] + nvert[cidx(d, i, j, k + 1)] + nvert[cidx(d, i, j, k - 1)] + nvert[cidx(d, i, j + 1, k)] +
+            nvert[cidx(d, i, j - 1, k)] + nvert[cidx(d, i + 1, j, k)] + nvert[cidx(d, i - 1, j, k)] > 0.1)
+      v = 0.;
+    mxv = fmax(mxv, v);
+  }
+  mxv = block_max(mxv, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = mxv;
+}
+int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
+                      cudaStream_t s) {
+  const int nb = nblk(ncell(d), RB);
+  k_divergence<<<nb, RB, 0, s>>>(d, u, aj, nvert, parts); ++g_launches;
+  k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_finish_sums(const double* parts, int nparts, int nq, double* out, cudaStream_t s) {
+  k_finish_sums<<<1, 256, 0, s>>>(parts, nparts, nq, out); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int partial_blocks(const Dims& d) { return nblk(ncell(d), RB); }
+
+}  // namespace vfs

@@ -1,0 +1,131 @@
+// Shared definitions of the GB300 pressure-projection kernels.
+//
+// Layout.  Every field uses the reference's PETSc DMDA array layout
+// (variables.h:305-383): extents mx = ni + 2, my = nj + 2, mz = nk + 2 with one
+// ghost/boundary cell per side, cell (i, j, k) at ((k * my) + j) * mx + i, i
+// fastest.  Scalars are one array; the contravariant flux Ucont is kept on the
+// device as three SoA arrays (x, y, z components) so that a stencil reads only
+// the component it needs; host transfers convert from/to the reference's AoS
+// Cmpnts layout.  The 19-point operator is stored as 19 SoA coefficient
+// arrays [slot][cell] in the slot order of poisson.c:956-974.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#define VFS_THR 0.1  // poisson_threshold, poisson.c:16
+
+namespace vfs {
+
+// Number of kernels this library has launched (all contexts).
+extern std::atomic<unsigned long long> g_launches;
+
+enum Slot { CP = 0, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW, NSLOT };
+
+struct Dims {
+  int mx, my, mz;  // ghosted extents
+  int ip, jp, kp;  // i/j/k periodic (index 0 mirrors m-2, m-1 mirrors 1)
+};
+
+__host__ __device__ __forceinline__ size_t cidx(const Dims& d, int i, int j, int k) {
+  return ((size_t)k * d.my + j) * d.mx + i;
+}
+__host__ __device__ __forceinline__ size_t ncell(const Dims& d) { return (size_t)d.mx * d.my * d.mz; }
+__host__ __device__ __forceinline__ int wrapi(int i, int m, int per) {
+  return per ? (i == 0 ? m - 2 : (i == m - 1 ? 1 : i)) : i;
+}
+__host__ __device__ __forceinline__ bool interior(const Dims& d, int i, int j, int k) {
+  return i > 0 && j > 0 && k > 0 && i < d.mx - 1 && j < d.my - 1 && k < d.mz - 1;
+}
+
+__host__ __device__ __forceinline__ int slot_di(int m) {
+  const int t[19] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, 1, -1, -1};
+  return t[m];
+}
+__host__ __device__ __forceinline__ int slot_dj(int m) {
+  const int t[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, 1, -1, -1, 0, 0, 0, 0};
+  return t[m];
+}
+__host__ __device__ __forceinline__ int slot_dk(int m) {
+  const int t[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+  return t[m];
+}
+
+// Wrapped neighbour offsets of one interior cell: nb[m] = cell index of slot m.
+struct Nbr {
+  size_t c[19];
+};
+__device__ __forceinline__ void neighbours(const Dims& d, int i, int j, int k, Nbr& nb) {
+  const int im = wrapi(i - 1, d.mx, d.ip), ip1 = wrapi(i + 1, d.mx, d.ip);
+  const int jm = wrapi(j - 1, d.my, d.jp), jp1 = wrapi(j + 1, d.my, d.jp);
+  const int km = wrapi(k - 1, d.mz, d.kp), kp1 = wrapi(k + 1, d.mz, d.kp);
+  const int II[3] = {im, i, ip1}, JJ[3] = {jm, j, jp1}, KK[3] = {km, k, kp1};
+#pragma unroll
+  for (int m = 0; m < 19; m++) nb.c[m] = cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]);
+}
+
+// One multigrid level (or the outer operator) as seen by a kernel.
+template <typename T>
+struct OpView {
+  Dims d;
+  const T* coef;     // [19][N]
+  unsigned mask;     // bit m set if slot m is nonzero somewhere on this level
+  const int* skip;   // device flag (nullable): kernels return at once when *skip != 0
+};
+
+__device__ __forceinline__ bool skipped(const int* f) { return f && *(volatile const int*)f; }
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions: every block writes one partial; a single block
+// sums the partials in index order.  Same launch shape => same bits.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_down_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+// Block sum of v (blockDim.x a multiple of 32, <= 1024); result valid in thread 0.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* sh /* >= 32 */) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ T block_max(T v, T* sh) {
+  v = warp_max(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+  if (w == 0) v = warp_max(v);
+  __syncthreads();
+  return v;
+}
+
+}  // namespace vfs
+
+#define VFS_CUDA_OK(expr)                      \
+  do {                                         \
+    cudaError_t _e = (expr);                   \
+    if (_e != cudaSuccess) return (int)_e;     \
+  } while (0)

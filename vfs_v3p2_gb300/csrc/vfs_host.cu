@@ -1,0 +1,1262 @@
+// Host runtime of the GB300 pressure-projection step: the C ABI of
+// include/vfs_gpu.h, grid and multigrid-hierarchy setup, the V-cycle, the
+// FP64 flexible GMRES driver and the whole projection step.
+//
+// The reference runs the same sequence on the CPU through PETSc and HYPRE
+// (solvers.c:871-931, poisson_hypre.c:580-771, mhv_poisson.c:2121-2359).
+// Here every array lives in HBM, every loop is a kernel, and the Krylov
+// scalars stay on the device: the host only enqueues launches and reads one
+// status word per iteration, one iteration behind, so the GPU never waits for
+// the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "vfs_common.cuh"
+#include "vfs_gpu.h"
+#include "vfs_kernels.h"
+#include "vfs_proj.h"
+
+using namespace vfs;
+
+std::atomic<unsigned long long> vfs::g_launches{0};
+
+namespace {
+
+// CUDA-event probe around every launch of one kernel of the finest level
+// (timed on the stream the kernel runs on), with its algorithmic bytes.
+struct Probe {
+  int kind = 0;  // VFS_PROBE_*
+  std::vector<cudaEvent_t> ev;
+  int used = 0;
+  double bytes = 0.;
+  unsigned long long launches = 0;
+  bool begin(cudaStream_t s) {
+    if (used + 2 > (int)ev.size()) return false;
+    cudaEventRecord(ev[used], s);
+    return true;
+  }
+  void end(cudaStream_t s, double b) {
+    cudaEventRecord(ev[used + 1], s);
+    used += 2;
+    bytes += b;
+    launches++;
+  }
+};
+Probe g_probe;
+
+constexpr int MAXLEV = 12;
+constexpr int MAXRESTART = 64;
+constexpr int DENSE_MAX = 8192;  // largest coarsest level solved by a dense inverse
+
+struct Level {
+  Dims d{};
+  size_t N = 0;
+  double* coor = nullptr;
+  double* nvert = nullptr;
+  double* M = nullptr;
+  double* coef = nullptr;
+  double* mcoef = nullptr;
+  float* mcoef32 = nullptr;
+  unsigned mask = 0;
+  uint8_t* pcode = nullptr;
+  float* x32[2] = {nullptr, nullptr};
+  float* b32 = nullptr;
+  double* x64[2] = {nullptr, nullptr};
+  double* b64 = nullptr;
+  double* Binv = nullptr;
+  float* Binv32 = nullptr;
+  int nco = 0;
+};
+
+struct Grid {
+  Dims d{};
+  int L = 1, si = 0, sj = 0, sk = 0, immersed = 0;
+  Level lev[MAXLEV];
+  double* pd = nullptr;
+  double* u = nullptr;      // SoA Ucont: x | y | z
+  double* ustar = nullptr;  // SoA resident U*
+  double* p = nullptr;
+  double* phi = nullptr;
+  double* b = nullptr;
+  double* ucat = nullptr;   // AoS
+  double* aos = nullptr;    // AoS staging
+  int m = 0;
+  double* V = nullptr;
+  double* w = nullptr;
+  float* Z32 = nullptr;
+  double* Z64 = nullptr;
+  KrylovState* st = nullptr;
+  double* starr = nullptr;
+  double* parts = nullptr;
+  double* scal = nullptr;   // small device scalars (sums, divmax)
+  int* hstat = nullptr;     // pinned
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  bool lhs = false;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  Ucont U() const { size_t N = ncell(d); return Ucont{u, u + N, u + 2 * N}; }
+};
+
+}  // namespace
+
+struct vfs_ctx {
+  int device = 0;
+  std::vector<cudaEvent_t> marks;  // vfs_mark slots
+  size_t budget = 0, used = 0;
+  std::map<int, Grid*> grids;
+  int next_id = 1;
+  std::string err;
+};
+
+namespace {
+
+int fail(vfs_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+int cuda_fail(vfs_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, VFS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(expr)                                             \
+  do {                                                       \
+    cudaError_t _e = (cudaError_t)(expr);                    \
+    if (_e != cudaSuccess) return cuda_fail(ctx, _e, #expr); \
+  } while (0)
+
+template <typename T>
+int galloc(vfs_ctx* ctx, Grid& g, T** out, size_t count) {
+  const size_t bytes = count * sizeof(T);
+  if (ctx->budget && ctx->used + bytes > ctx->budget)
+    return fail(ctx, VFS_ERR_NOMEM, "HBM budget exceeded (" + std::to_string(ctx->used + bytes) + " > " +
+                                        std::to_string(ctx->budget) + " bytes)");
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, VFS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  e = cudaMemset(p, 0, bytes ? bytes : 16);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemset");
+  g.allocs.push_back(p);
+  g.bytes += bytes;
+  ctx->used += bytes;
+  *out = (T*)p;
+  return VFS_OK;
+}
+#define GA(ptr, count)                                  \
+  do {                                                  \
+    int _r = galloc(ctx, g, &(ptr), (size_t)(count));   \
+    if (_r) return _r;                                  \
+  } while (0)
+
+void grid_free(vfs_ctx* ctx, Grid* g) {
+  if (g->s) cudaStreamSynchronize(g->s);
+  for (void* p : g->allocs) cudaFree(p);
+  if (ctx) ctx->used -= std::min(ctx->used, g->bytes);
+  if (g->hstat) cudaFreeHost(g->hstat);
+  for (auto& e : g->ev) if (e) cudaEventDestroy(e);
+  if (g->t0) cudaEventDestroy(g->t0);
+  if (g->t1) cudaEventDestroy(g->t1);
+  if (g->s) cudaStreamDestroy(g->s);
+  delete g;
+}
+
+Grid* get_grid(vfs_ctx* ctx, int id) {
+  auto it = ctx->grids.find(id);
+  return it == ctx->grids.end() ? nullptr : it->second;
+}
+
+int coarse_n(int n) { return n / 2; }
+
+template <typename T> T* mcoef_of(Level& L);
+template <> float* mcoef_of<float>(Level& L) { return L.mcoef32; }
+template <> double* mcoef_of<double>(Level& L) { return L.mcoef; }
+template <typename T> T** xbuf(Level& L);
+template <> float** xbuf<float>(Level& L) { return L.x32; }
+template <> double** xbuf<double>(Level& L) { return L.x64; }
+template <typename T> T*& bbuf(Level& L);
+template <> float*& bbuf<float>(Level& L) { return L.b32; }
+template <> double*& bbuf<double>(Level& L) { return L.b64; }
+template <typename T> T* binv(Level& L);
+template <> float* binv<float>(Level& L) { return L.Binv32; }
+template <> double* binv<double>(Level& L) { return L.Binv; }
+
+template <typename T>
+OpView<T> mgview(Level& L, const int* skip) {
+  return OpView<T>{L.d, mcoef_of<T>(L), L.mask, skip};
+}
+
+template <typename T>
+int ensure_mg(vfs_ctx* ctx, Grid& g) {
+  for (int l = 0; l < g.L; l++) {
+    Level& L = g.lev[l];
+    T** x = xbuf<T>(L);
+    if (!x[0]) {
+      GA(x[0], L.N);
+      GA(x[1], L.N);
+      GA(bbuf<T>(L), L.N);
+    }
+  }
+  return VFS_OK;
+}
+
+int ensure_krylov(vfs_ctx* ctx, Grid& g, int m, int prec) {
+  const size_t N = ncell(g.d);
+  if (g.m < m) {
+    if (g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow after the first solve of a grid");
+    GA(g.V, (size_t)(m + 1) * N);
+    GA(g.w, N);
+    g.m = m;
+    GA(g.starr, (size_t)(m + 1) * m + 6 * (m + 2));
+  }
+  if (prec == VFS_MIXED && !g.Z32) GA(g.Z32, (size_t)g.m * N);
+  if (prec == VFS_FP64 && !g.Z64) GA(g.Z64, (size_t)g.m * N);
+  return VFS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle from a zero initial guess on level l: approximately solves
+// A_l x = b; xa / xb are the level's ping-pong buffers; returns the buffer
+// that holds the result.
+// ---------------------------------------------------------------------------
+struct MGCfg {
+  int nu1, nu2, ncoarse;
+  double omega, omega_c;
+};
+
+int popcount(unsigned m) {
+  int c = 0;
+  for (; m; m &= m - 1) c++;
+  return c;
+}
+size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.mz - 2); }
+
+// A full smoothing sweep (x != 0) streams the active coefficient slots, x,
+// b and writes x: (slots + 3) words per interior cell.
+template <typename T>
+void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
+  const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
+  launch_smooth<T>(A, xi, b, xo, omega, s);
+  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 3));
+}
+
+template <typename T>
+T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, cudaStream_t s) {
+  Level& L = g.lev[l];
+  OpView<T> A = mgview<T>(L, skip);
+  if (l == 0) {
+    if (binv<T>(L)) {
+      launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, xa, skip, s);
+      return xa;
+    }
+    T* cur = nullptr;
+    T* bufs[2] = {xa, xb};
+    for (int q = 0; q < c.ncoarse; q++) {
+      T* o = bufs[q & 1];
+      launch_smooth<T>(A, cur, b, o, (T)c.omega_c, s);
+      cur = o;
+    }
+    return cur ? cur : xa;
+  }
+  T* bufs[2] = {xa, xb};
+  int q = 0;
+  T* cur = nullptr;
+  for (; q < c.nu1; q++) {
+    T* o = bufs[q & 1];
+    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, s);
+    cur = o;
+  }
+  Level& C = g.lev[l - 1];
+  T** xc = xbuf<T>(C);
+  launch_residual_restrict<T>(A, cur, b, L.nvert, C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s);
+  T* ec = vcycle<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, skip, s);
+  if (!cur) {
+    cur = bufs[q & 1];
+    q++;
+    launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 0, skip, s);
+  } else {
+    launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s);
+  }
+  for (int r = 0; r < c.nu2; r++, q++) {
+    T* o = bufs[q & 1];
+    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, s);
+    cur = o;
+  }
+  return cur;
+}
+
+MGCfg mgcfg(const vfs_solve_params& p) {
+  MGCfg c;
+  c.nu1 = p.nu1;
+  c.nu2 = p.nu2;
+  c.ncoarse = 32;
+  c.omega = p.omega;
+  c.omega_c = p.omega;
+  return c;
+}
+
+// z = M^{-1} v on the finest level (v FP64, z in T), optional skip flag.
+template <typename T>
+int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T* z, T* tmp, const int* skip,
+            cudaStream_t s) {
+  Level& F = g.lev[g.L - 1];
+  const double* aj = F.M + F.N * MP_AJ;
+  T* bf = bbuf<T>(F);
+  launch_scale_in<T>(F.d, aj, v, bf, skip, s);
+  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p), skip, s);
+  if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  return VFS_OK;
+}
+
+int apply_outer(Grid& g, const double* x, const double* b, double* y, const int* skip, cudaStream_t s) {
+  Level& F = g.lev[g.L - 1];
+  OpView<double> A{F.d, F.coef, F.mask, skip};
+  return launch_apply64(A, x, b, y, s);
+}
+int apply_outer(Grid& g, const float* x, const double* b, double* y, const int* skip, cudaStream_t s) {
+  Level& F = g.lev[g.L - 1];
+  OpView<double> A{F.d, F.coef, F.mask, skip};
+  return launch_apply64_xf(A, x, b, y, s);
+}
+
+// ---------------------------------------------------------------------------
+// Flexible GMRES(m), FP64 outer, preconditioned by one V-cycle in T.
+// ---------------------------------------------------------------------------
+struct Fgmres {
+  // issue-side bookkeeping of one solve, so that several grids can be
+  // interleaved (batched) by the same driver
+  Grid* g;
+  const vfs_solve_params* p;
+  int it = 0, j = 0;
+  bool observed = false, finished = false;
+};
+
+template <typename T>
+T* zbase(Grid& g);
+template <>
+float* zbase<float>(Grid& g) { return g.Z32; }
+template <>
+double* zbase<double>(Grid& g) { return g.Z64; }
+
+template <typename T>
+int fg_start(vfs_ctx* ctx, Fgmres& f) {
+  Grid& g = *f.g;
+  const vfs_solve_params& p = *f.p;
+  const size_t N = ncell(g.d);
+  cudaStream_t s = g.s;
+  KrylovState h{};
+  h.m = p.restart;
+  h.rtol = p.rtol;
+  double* a = g.starr;
+  h.H = a; a += (size_t)(p.restart + 1) * p.restart;
+  h.cs = a; a += p.restart + 2;
+  h.sn = a; a += p.restart + 2;
+  h.g = a; a += p.restart + 2;
+  h.y = a; a += p.restart + 2;
+  h.h = a; a += p.restart + 2;
+  h.hacc = a;
+  if (!g.st) {
+    int r = galloc(ctx, g, (unsigned char**)&g.st, sizeof(KrylovState));
+    if (r) return r;
+  }
+  CK(cudaMemcpyAsync(g.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  if (!p.warm_start) CK(cudaMemsetAsync(g.phi, 0, N * sizeof(double), s));
+  launch_norm_init(g.st, g.b, N, g.parts, 1, s);
+  apply_outer(g, g.phi, g.b, g.V, &g.st->done, s);
+  launch_norm_init(g.st, g.V, N, g.parts, 0, s);
+  launch_vec_scale_first(g.st, g.V, g.V, N, s);
+  f.it = 0;
+  f.j = 0;
+  f.observed = f.finished = false;
+  return VFS_OK;
+}
+
+// Issue one Arnoldi iteration (and the cycle end / restart when due); check
+// the status of the previous iteration.  Sets f.finished when done.
+template <typename T>
+int fg_step(vfs_ctx* ctx, Fgmres& f) {
+  Grid& g = *f.g;
+  const vfs_solve_params& p = *f.p;
+  const size_t N = ncell(g.d);
+  cudaStream_t s = g.s;
+  const int* skip = &g.st->done;
+  const int nb = krylov_nblocks(N);
+  T* Z = zbase<T>(g);
+  T* zj = Z + (size_t)f.j * N;
+  double* vj = g.V + (size_t)f.j * N;
+  Level& F = g.lev[g.L - 1];
+  int r = precond<T>(ctx, g, p, vj, zj, xbuf<T>(F)[1], skip, s);
+  if (r) return r;
+  {
+    const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
+    apply_outer(g, zj, nullptr, g.w, skip, s);
+    if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + sizeof(T) + 8.0));
+  }
+  launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s);
+  launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s);
+  launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s);
+  launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s);
+  launch_arnoldi_finish(g.st, nb, g.parts, s);
+  launch_vnext(g.st, g.w, g.V + (size_t)(f.j + 1) * N, N, s);
+  f.it++;
+  f.j++;
+  launch_status_copy(g.st, &g.hstat[f.it & 1], s);
+  CK(cudaEventRecord(g.ev[f.it & 1], s));
+  if (f.it >= 2) {
+    CK(cudaEventSynchronize(g.ev[(f.it - 1) & 1]));
+    if (g.hstat[(f.it - 1) & 1]) f.observed = true;
+  }
+  if (f.observed || f.it >= p.maxit || f.j == f.p->restart) {
+    launch_lsq_update(g.st, s);
+    launch_x_update<T>(g.st, Z, N, g.phi, s);
+    launch_restart_reset(g.st, s);
+    if (f.observed || f.it >= p.maxit) {
+      f.finished = true;
+      return VFS_OK;
+    }
+    apply_outer(g, g.phi, g.b, g.V, skip, s);
+    launch_norm_init(g.st, g.V, N, g.parts, 0, s);
+    launch_vec_scale_first(g.st, g.V, g.V, N, s);
+    f.j = 0;
+  }
+  return VFS_OK;
+}
+
+// Close a solve: true residual, null-space removal, phi finish, info.
+int fg_finish(vfs_ctx* ctx, Fgmres& f, vfs_solve_info* info) {
+  Grid& g = *f.g;
+  const size_t N = ncell(g.d);
+  cudaStream_t s = g.s;
+  Level& F = g.lev[g.L - 1];
+  apply_outer(g, g.phi, g.b, g.w, nullptr, s);  // w = b - A phi
+  launch_norm2(g.w, N, g.parts, g.scal + 16, s);
+  launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s);
+  launch_phi_finish(F.d, F.nvert, g.phi, s);
+  CK(cudaEventRecord(g.t1, s));
+  KrylovState h{};
+  double rn = 0.;
+  CK(cudaMemcpyAsync(&h, g.st, sizeof(h), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rn, g.scal + 16, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (info) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g.t0, g.t1);
+    info->iterations = h.it;
+    info->converged = (h.done && h.resid <= h.rtol * h.bnorm) || h.bnorm == 0.;
+    info->bnorm = h.bnorm;
+    info->relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
+    info->time_ms = ms;
+  }
+  if (!(h.bnorm == h.bnorm) || !(h.resid == h.resid) || !(rn == rn)) return fail(ctx, VFS_ERR_NUMERIC, "NaN in the solve");
+  return VFS_OK;
+}
+
+template <typename T>
+int solve_one(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, vfs_solve_info* info) {
+  int r = ensure_mg<T>(ctx, g);
+  if (r) return r;
+  r = ensure_krylov(ctx, g, p.restart, sizeof(T) == 4 ? VFS_MIXED : VFS_FP64);
+  if (r) return r;
+  CK(cudaEventRecord(g.t0, g.s));
+  Fgmres f{&g, &p};
+  r = fg_start<T>(ctx, f);
+  if (r) return r;
+  while (!f.finished) {
+    r = fg_step<T>(ctx, f);
+    if (r) return r;
+  }
+  return fg_finish(ctx, f, info);
+}
+
+int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
+  if (!p) return fail(ctx, VFS_ERR_ARG, "null solve params");
+  if (p->restart < 1 || p->restart > MAXRESTART) return fail(ctx, VFS_ERR_ARG, "restart must be in [1, 64]");
+  if (p->maxit < 1) return fail(ctx, VFS_ERR_ARG, "maxit must be >= 1");
+  if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 + p->nu2 < 1) return fail(ctx, VFS_ERR_ARG, "need at least one smoothing sweep");
+  if (!(p->rtol > 0.)) return fail(ctx, VFS_ERR_ARG, "rtol must be > 0");
+  if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
+  return VFS_OK;
+}
+
+int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* info) {
+  int r = check_params(ctx, p);
+  if (r) return r;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the solve");
+  if (g.m && p->restart > g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow after the first solve");
+  r = (p->precision == VFS_MIXED) ? solve_one<float>(ctx, g, *p, info) : solve_one<double>(ctx, g, *p, info);
+  return r;
+}
+
+size_t level_bytes(const Dims& d, bool finest) {
+  const size_t N = ncell(d);
+  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19) * 8 + N * 19 * 4 + N;  // coor nvert M coef mcoef mcoef32 pcode
+  b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
+  if (finest) b += N * 8 * (9 + 3 + 3 + 3 + 3 + 3);                    // pd u ustar p phi b ucat aos
+  return b;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void vfs_default_params(vfs_solve_params* p) {
+  if (!p) return;
+  p->precision = VFS_MIXED;
+  p->rtol = 1e-9;
+  p->maxit = 200;
+  p->restart = 30;
+  p->nu1 = 2;
+  p->nu2 = 2;
+  p->omega = 0.8;
+  p->warm_start = 0;
+}
+
+int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
+  if (!out) return VFS_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return VFS_ERR_CUDA;
+  }
+  vfs_ctx* ctx = new vfs_ctx();
+  ctx->device = cfg ? cfg->device : 0;
+  ctx->budget = cfg ? (size_t)cfg->hbm_budget_bytes : 0;
+  if (ctx->device < 0 || ctx->device >= ndev) {
+    delete ctx;
+    return VFS_ERR_ARG;
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) {
+    delete ctx;
+    return VFS_ERR_CUDA;
+  }
+  *out = ctx;
+  return VFS_OK;
+}
+
+void vfs_destroy(vfs_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  for (auto& e : ctx->marks) cudaEventDestroy(e);
+  for (auto& kv : ctx->grids) grid_free(ctx, kv.second);
+  ctx->grids.clear();
+  delete ctx;
+}
+
+const char* vfs_last_error(const vfs_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int vfs_grid_estimate(const vfs_grid_desc* desc, int restart, unsigned long long* bytes) {
+  if (!desc || !bytes) return VFS_ERR_ARG;
+  Dims d{desc->mx, desc->my, desc->mz, desc->i_periodic, desc->j_periodic, desc->k_periodic};
+  size_t b = level_bytes(d, true);
+  Dims c = d;
+  for (int l = 1; l < desc->mg_levels; l++) {
+    if (!desc->semi_i) c.mx = (c.mx - 2) / 2 + 2;
+    if (!desc->semi_j) c.my = (c.my - 2) / 2 + 2;
+    if (!desc->semi_k) c.mz = (c.mz - 2) / 2 + 2;
+    b += level_bytes(c, false);
+  }
+  const size_t N = ncell(d);
+  b += N * 8 * (size_t)(restart + 2) + N * 4 * (size_t)restart + N * 8 * (size_t)restart;
+  *bytes = b;
+  return VFS_OK;
+}
+
+int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
+  if (!ctx) return VFS_ERR_ARG;
+  if (!desc || !grid_id || !desc->coor || !desc->nvert) return fail(ctx, VFS_ERR_ARG, "null grid description");
+  CK(cudaSetDevice(ctx->device));
+  const int L = desc->mg_levels;
+  if (L < 1 || L > MAXLEV) return fail(ctx, VFS_ERR_ARG, "mg_levels must be in [1, 12]");
+  Dims d{desc->mx, desc->my, desc->mz, desc->i_periodic ? 1 : 0, desc->j_periodic ? 1 : 0, desc->k_periodic ? 1 : 0};
+  const int sem[3] = {desc->semi_i, desc->semi_j, desc->semi_k};
+  const int ext[3] = {d.mx - 2, d.my - 2, d.mz - 2};
+  const int per[3] = {d.ip, d.jp, d.kp};
+  for (int a = 0; a < 3; a++) {
+    int n = ext[a];
+    if (n < 2) return fail(ctx, VFS_ERR_ARG, "every axis needs at least 2 interior cells");
+    for (int l = 1; l < L; l++) {
+      if (sem[a]) continue;
+      if (n % 2) return fail(ctx, VFS_ERR_ARG, "a coarsened axis has an odd cell count at some level");
+      n = coarse_n(n);
+    }
+    if (per[a] && n < 3) return fail(ctx, VFS_ERR_ARG, "a periodic axis needs at least 3 cells on the coarsest level");
+    if (n < 2) return fail(ctx, VFS_ERR_ARG, "too many multigrid levels for this grid");
+  }
+  if (ext[1] > 3000) return fail(ctx, VFS_ERR_ARG, "the y-line smoother supports at most 3000 cells in j");
+  Grid* gp = new Grid();
+  Grid& g = *gp;
+  g.d = d;
+  g.L = L;
+  g.si = desc->semi_i ? 1 : 0;
+  g.sj = desc->semi_j ? 1 : 0;
+  g.sk = desc->semi_k ? 1 : 0;
+  g.immersed = desc->immersed;
+  auto bail = [&](int r) {
+    grid_free(ctx, gp);
+    return r;
+  };
+  if (cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(ctx, cudaGetLastError(), "stream"));
+  cudaEventCreateWithFlags(&g.ev[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&g.ev[1], cudaEventDisableTiming);
+  cudaEventCreate(&g.t0);
+  cudaEventCreate(&g.t1);
+  if (cudaMallocHost(&g.hstat, 4 * sizeof(int)) != cudaSuccess) return bail(cuda_fail(ctx, cudaGetLastError(), "pinned"));
+  // level extents, finest = L-1
+  g.lev[L - 1].d = d;
+  for (int l = L - 2; l >= 0; l--) {
+    Dims c = g.lev[l + 1].d;
+    if (!g.si) c.mx = coarse_n(c.mx - 2) + 2;
+    if (!g.sj) c.my = coarse_n(c.my - 2) + 2;
+    if (!g.sk) c.mz = coarse_n(c.mz - 2) + 2;
+    g.lev[l].d = c;
+  }
+  int r;
+  double* tmp = nullptr;
+  for (int l = 0; l < L; l++) {
+    Level& Lv = g.lev[l];
+    Lv.N = ncell(Lv.d);
+#define GAB(ptr, cnt)                                           \
+  do {                                                          \
+    r = galloc(ctx, g, &(ptr), (size_t)(cnt));                  \
+    if (r) return bail(r);                                      \
+  } while (0)
+    GAB(Lv.coor, 3 * Lv.N);
+    GAB(Lv.nvert, Lv.N);
+    GAB(Lv.M, MP_TOTAL * Lv.N);
+    GAB(Lv.coef, 19 * Lv.N);
+    GAB(Lv.mcoef, 19 * Lv.N);
+    GAB(Lv.mcoef32, 19 * Lv.N);
+    if (l > 0) GAB(Lv.pcode, Lv.N);
+  }
+  const size_t N = ncell(d);
+  GAB(tmp, 9 * N);
+  GAB(g.pd, 9 * N);
+  GAB(g.u, 3 * N);
+  GAB(g.ustar, 3 * N);
+  GAB(g.p, N);
+  GAB(g.phi, N);
+  GAB(g.b, N);
+  GAB(g.ucat, 3 * N);
+  GAB(g.aos, 3 * N);
+  GAB(g.parts, (size_t)krylov_nblocks(N) * 72 + 4096);
+  GAB(g.scal, 64);
+  Level& F = g.lev[L - 1];
+  if (cudaMemcpyAsync(F.coor, desc->coor, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess ||
+      cudaMemcpyAsync(F.nvert, desc->nvert, N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess)
+    return bail(cuda_fail(ctx, cudaGetLastError(), "upload"));
+  for (int l = L - 2; l >= 0; l--)
+    launch_coarsen(g.lev[l + 1].d, g.lev[l].d, g.si, g.sj, g.sk, g.lev[l + 1].coor, g.lev[l + 1].nvert, g.lev[l].coor,
+                   g.lev[l].nvert, g.s);
+  for (int l = 0; l < L; l++) launch_form_metrics(g.lev[l].d, g.lev[l].coor, g.lev[l].M, tmp, g.s);
+  cudaError_t e = cudaStreamSynchronize(g.s);
+  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "grid setup"));
+  const int id = ctx->next_id++;
+  ctx->grids[id] = gp;
+  *grid_id = id;
+  return VFS_OK;
+}
+
+int vfs_grid_destroy(vfs_ctx* ctx, int grid) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  grid_free(ctx, g);
+  ctx->grids.erase(grid);
+  return VFS_OK;
+}
+
+int vfs_grid_bytes(vfs_ctx* ctx, int grid, unsigned long long* bytes) {
+  if (!ctx || !bytes) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  *bytes = g->bytes;
+  return VFS_OK;
+}
+
+int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  CK(cudaSetDevice(ctx->device));
+  const size_t N = ncell(g.d);
+  double* gt = nullptr;
+  unsigned* dmask = nullptr;
+  CK(cudaMalloc(&gt, 9 * N * sizeof(double)));
+  CK(cudaMalloc(&dmask, sizeof(unsigned)));
+  for (int l = 0; l < g.L; l++) {
+    Level& Lv = g.lev[l];
+    launch_gtensor(Lv.d, Lv.M, gt, g.s);
+    launch_assemble(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.coef, Lv.mcoef, Lv.mcoef32, dmask, g.s);
+    CK(cudaMemcpyAsync(&Lv.mask, dmask, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
+    if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
+  }
+  Level& F = g.lev[g.L - 1];
+  launch_proj_dots(F.d, F.M, g.pd, g.s);
+  CK(cudaStreamSynchronize(g.s));
+  cudaFree(gt);
+  cudaFree(dmask);
+  // coarsest level: dense inverse of A + sigma e e^T when small enough
+  Level& C = g.lev[0];
+  const int n = (C.d.mx - 2) * (C.d.my - 2) * (C.d.mz - 2);
+  if (n <= DENSE_MAX && !C.Binv) {
+    std::vector<double> cp(C.N);
+    CK(cudaMemcpy(cp.data(), C.mcoef, C.N * sizeof(double), cudaMemcpyDeviceToHost));
+    double sabs = 0.;
+    long nf = 0;
+    for (size_t c = 0; c < C.N; c++)
+      if (cp[c] != 0.) {
+        sabs += std::fabs(cp[c]);
+        nf++;
+      }
+    if (nf > 0) {
+      const double sigma = -(sabs / nf) / (double)nf;
+      double *W = nullptr, *fac = nullptr, *pval = nullptr;
+      int* piv = nullptr;
+      CK(cudaMalloc(&W, (size_t)n * 2 * n * sizeof(double)));
+      CK(cudaMalloc(&fac, (size_t)n * sizeof(double)));
+      CK(cudaMalloc(&pval, sizeof(double)));
+      CK(cudaMalloc(&piv, sizeof(int)));
+      int r = galloc(ctx, g, &C.Binv, (size_t)n * n);
+      if (!r) r = galloc(ctx, g, &C.Binv32, (size_t)n * n);
+      if (r) {
+        cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv);
+        return r;
+      }
+      launch_dense_inverse(C.d, C.mcoef, sigma, W, fac, piv, pval, C.Binv, C.Binv32, n, g.s);
+      cudaError_t e = cudaStreamSynchronize(g.s);
+      cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "coarse inverse");
+      C.nco = n;
+    }
+  }
+  g.lhs = true;
+  return VFS_OK;
+}
+
+int vfs_set_field(vfs_ctx* ctx, int grid, int field, const double* host) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || !host) return fail(ctx, VFS_ERR_ARG, "no such grid or null buffer");
+  Grid& g = *gp;
+  const size_t N = ncell(g.d);
+  switch (field) {
+    case VFS_FIELD_UCONT:
+    case VFS_FIELD_USTAR: {
+      double* dst = field == VFS_FIELD_UCONT ? g.u : g.ustar;
+      CK(cudaMemcpyAsync(g.aos, host, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+      launch_aos2soa(N, g.aos, dst, dst + N, dst + 2 * N, g.s);
+      break;
+    }
+    case VFS_FIELD_P: CK(cudaMemcpyAsync(g.p, host, N * sizeof(double), cudaMemcpyHostToDevice, g.s)); break;
+    case VFS_FIELD_PHI: CK(cudaMemcpyAsync(g.phi, host, N * sizeof(double), cudaMemcpyHostToDevice, g.s)); break;
+    case VFS_FIELD_RHS: CK(cudaMemcpyAsync(g.b, host, N * sizeof(double), cudaMemcpyHostToDevice, g.s)); break;
+    default: return fail(ctx, VFS_ERR_ARG, "field cannot be set");
+  }
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+int vfs_get_field(vfs_ctx* ctx, int grid, int field, double* host) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || !host) return fail(ctx, VFS_ERR_ARG, "no such grid or null buffer");
+  Grid& g = *gp;
+  const size_t N = ncell(g.d);
+  switch (field) {
+    case VFS_FIELD_UCONT:
+    case VFS_FIELD_USTAR: {
+      double* src = field == VFS_FIELD_UCONT ? g.u : g.ustar;
+      launch_soa2aos(N, src, src + N, src + 2 * N, g.aos, g.s);
+      CK(cudaMemcpyAsync(host, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+      break;
+    }
+    case VFS_FIELD_P: CK(cudaMemcpyAsync(host, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.s)); break;
+    case VFS_FIELD_PHI: CK(cudaMemcpyAsync(host, g.phi, N * sizeof(double), cudaMemcpyDeviceToHost, g.s)); break;
+    case VFS_FIELD_RHS: CK(cudaMemcpyAsync(host, g.b, N * sizeof(double), cudaMemcpyDeviceToHost, g.s)); break;
+    case VFS_FIELD_UCAT: CK(cudaMemcpyAsync(host, g.ucat, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.s)); break;
+    case VFS_FIELD_NVERT:
+      CK(cudaMemcpyAsync(host, g.lev[g.L - 1].nvert, N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+      break;
+    default: return fail(ctx, VFS_ERR_ARG, "unknown field");
+  }
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+int vfs_volume_flux(vfs_ctx* ctx, int grid, double out[4]) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  Level& F = g.lev[g.L - 1];
+  launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s);
+  if (out) CK(cudaMemcpyAsync(out, g.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+int vfs_poisson_rhs(vfs_ctx* ctx, int grid, double dt, double st, double coeff, int meanfix, double* sum_out) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
+  Grid& g = *gp;
+  Level& F = g.lev[g.L - 1];
+  launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, meanfix, g.b, g.parts, g.scal + 4, g.s);
+  double sc[2];
+  CK(cudaMemcpyAsync(sc, g.scal + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  CK(cudaStreamSynchronize(g.s));
+  if (sum_out) *sum_out = sc[0];
+  if (!(sc[0] == sc[0])) return fail(ctx, VFS_ERR_NUMERIC, "NaN in the right-hand side");
+  return VFS_OK;
+}
+
+int vfs_poisson_solve(vfs_ctx* ctx, int grid, const vfs_solve_params* p, vfs_solve_info* info) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  vfs_solve_info tmp{};
+  int r = do_solve(ctx, *gp, p, info ? info : &tmp);
+  if (r) return r;
+  const vfs_solve_info& i = info ? *info : tmp;
+  if (!i.converged) return fail(ctx, VFS_ERR_NOTCONV, "FGMRES stopped at maxit above rtol");
+  return VFS_OK;
+}
+
+int vfs_update_pressure(vfs_ctx* ctx, int grid) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  Level& F = g.lev[g.L - 1];
+  launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s);
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection");
+  Level& F = g.lev[g.L - 1];
+  launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s);
+  launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s);
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out) {
+  if (!ctx || !out) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  Level& F = g.lev[g.L - 1];
+  launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s);
+  CK(cudaMemcpyAsync(out, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Everything of one projection step after the inputs are resident, up to the
+// solve start (flux balance, RHS).
+void step_pre(Grid& g, double dt, double st, double coeff) {
+  Level& F = g.lev[g.L - 1];
+  launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s);
+  launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s);
+}
+// After the solve: pressure, projection, Contra2Cart, divergence.
+void step_post(Grid& g, double dt, double st, double coeff) {
+  Level& F = g.lev[g.L - 1];
+  launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s);
+  launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s);
+  launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s);
+  launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vfs_projection_step(vfs_ctx* ctx, int grid, double* ucont_inout, double* p_inout, double dt, double st,
+                        double coeff, const vfs_solve_params* p, vfs_solve_info* info, double* divmax) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  int r = check_params(ctx, p);
+  if (r) return r;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection step");
+  if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
+  const size_t N = ncell(g.d);
+  if (ucont_inout) {
+    CK(cudaMemcpyAsync(g.aos, ucont_inout, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+    launch_aos2soa(N, g.aos, g.u, g.u + N, g.u + 2 * N, g.s);
+  } else {
+    CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
+  }
+  if (p_inout) CK(cudaMemcpyAsync(g.p, p_inout, N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+  step_pre(g, dt, st, coeff);
+  vfs_solve_info tmp{};
+  r = do_solve(ctx, g, p, info ? info : &tmp);
+  if (r) return r;
+  step_post(g, dt, st, coeff);
+  if (ucont_inout) {
+    launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, g.s);
+    CK(cudaMemcpyAsync(ucont_inout, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  }
+  if (p_inout) CK(cudaMemcpyAsync(p_inout, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  double dm = 0.;
+  CK(cudaMemcpyAsync(&dm, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
+  CK(cudaStreamSynchronize(g.s));
+  if (divmax) *divmax = dm;
+  const vfs_solve_info& i = info ? *info : tmp;
+  if (!i.converged) return fail(ctx, VFS_ERR_NOTCONV, "FGMRES stopped at maxit above rtol");
+  return VFS_OK;
+}
+
+int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, double st, double coeff,
+                              const vfs_solve_params* p, vfs_solve_info* infos, double* divmax) {
+  if (!ctx || n < 0 || (n && !grids)) return VFS_ERR_ARG;
+  int r = check_params(ctx, p);
+  if (r) return r;
+  std::vector<Grid*> gs(n);
+  for (int q = 0; q < n; q++) {
+    gs[q] = get_grid(ctx, grids[q]);
+    if (!gs[q]) return fail(ctx, VFS_ERR_ARG, "no such grid in the batch");
+    if (!gs[q]->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the batch");
+    if (gs[q]->m && p->restart > gs[q]->m) return fail(ctx, VFS_ERR_ARG, "restart cannot grow");
+  }
+  const bool mixed = p->precision == VFS_MIXED;
+  std::vector<Fgmres> fs(n);
+  for (int q = 0; q < n; q++) {
+    Grid& g = *gs[q];
+    r = mixed ? ensure_mg<float>(ctx, g) : ensure_mg<double>(ctx, g);
+    if (!r) r = ensure_krylov(ctx, g, p->restart, p->precision);
+    if (r) return r;
+    const size_t N = ncell(g.d);
+    CK(cudaEventRecord(g.t0, g.s));
+    CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
+    step_pre(g, dt, st, coeff);
+    fs[q] = Fgmres{&g, p};
+    r = mixed ? fg_start<float>(ctx, fs[q]) : fg_start<double>(ctx, fs[q]);
+    if (r) return r;
+  }
+  // interleave the iterations of all grids, each on its own stream
+  int live = n;
+  while (live > 0) {
+    live = 0;
+    for (int q = 0; q < n; q++) {
+      if (fs[q].finished) continue;
+      r = mixed ? fg_step<float>(ctx, fs[q]) : fg_step<double>(ctx, fs[q]);
+      if (r) return r;
+      if (!fs[q].finished) live++;
+    }
+  }
+  int rc = VFS_OK;
+  for (int q = 0; q < n; q++) {
+    vfs_solve_info tmp{};
+    r = fg_finish(ctx, fs[q], infos ? &infos[q] : &tmp);
+    if (r) return r;
+    step_post(*gs[q], dt, st, coeff);
+  }
+  for (int q = 0; q < n; q++) {
+    Grid& g = *gs[q];
+    double dm = 0.;
+    CK(cudaMemcpyAsync(&dm, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
+    CK(cudaStreamSynchronize(g.s));
+    if (divmax) divmax[q] = dm;
+    if (infos && !infos[q].converged) rc = VFS_ERR_NOTCONV;
+  }
+  if (rc) fail(ctx, rc, "a solve of the batch stopped at maxit above rtol");
+  return rc;
+}
+
+int vfs_probe_begin(vfs_ctx* ctx, int kernel) {
+  if (!ctx) return VFS_ERR_ARG;
+  if (kernel != VFS_PROBE_SMOOTH && kernel != VFS_PROBE_APPLY64) return fail(ctx, VFS_ERR_ARG, "unknown probe kernel");
+  CK(cudaSetDevice(ctx->device));
+  if (g_probe.ev.empty()) {
+    g_probe.ev.resize(2 * 8192);
+    for (auto& e : g_probe.ev) CK(cudaEventCreate(&e));
+  }
+  g_probe.kind = kernel;
+  g_probe.used = 0;
+  g_probe.bytes = 0.;
+  g_probe.launches = 0;
+  return VFS_OK;
+}
+
+int vfs_probe_end(vfs_ctx* ctx, unsigned long long* launches, double* total_ms, double* alg_bytes) {
+  if (!ctx) return VFS_ERR_ARG;
+  CK(cudaDeviceSynchronize());
+  double ms = 0.;
+  for (int q = 0; q + 1 < g_probe.used; q += 2) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, g_probe.ev[q], g_probe.ev[q + 1]));
+    ms += t;
+  }
+  if (launches) *launches = g_probe.launches;
+  if (total_ms) *total_ms = ms;
+  if (alg_bytes) *alg_bytes = g_probe.bytes;
+  g_probe.kind = 0;
+  return VFS_OK;
+}
+
+int vfs_launch_count(unsigned long long* out) {
+  if (!out) return VFS_ERR_ARG;
+  *out = g_launches.load();
+  return VFS_OK;
+}
+
+int vfs_host_register(void* ptr, unsigned long long bytes) {
+  if (!ptr || !bytes) return VFS_ERR_ARG;
+  return cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault) == cudaSuccess ? VFS_OK : VFS_ERR_CUDA;
+}
+
+int vfs_host_unregister(void* ptr) {
+  if (!ptr) return VFS_ERR_ARG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? VFS_OK : VFS_ERR_CUDA;
+}
+
+int vfs_mark(vfs_ctx* ctx, int grid, int slot) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || slot < 0 || slot >= 4096) return fail(ctx, VFS_ERR_ARG, "no such grid or slot out of [0, 4096)");
+  if (ctx->marks.empty()) {
+    ctx->marks.resize(4096);
+    for (auto& e : ctx->marks) CK(cudaEventCreate(&e));
+  }
+  CK(cudaEventRecord(ctx->marks[slot], g->s));
+  return VFS_OK;
+}
+
+int vfs_elapsed(vfs_ctx* ctx, int slot_a, int slot_b, double* ms) {
+  if (!ctx || !ms || ctx->marks.empty() || slot_a < 0 || slot_b < 0 || slot_a >= 4096 || slot_b >= 4096)
+    return fail(ctx, VFS_ERR_ARG, "bad timer slots");
+  CK(cudaEventSynchronize(ctx->marks[slot_b]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->marks[slot_a], ctx->marks[slot_b]));
+  *ms = t;
+  return VFS_OK;
+}
+
+int vfs_sync(vfs_ctx* ctx) {
+  if (!ctx) return VFS_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaDeviceSynchronize());
+  return VFS_OK;
+}
+
+// ---- test hooks ----
+int vfs_get_level_dims(vfs_ctx* ctx, int grid, int level, int dims[3]) {
+  if (!ctx || !dims) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  dims[0] = g->lev[level].d.mx;
+  dims[1] = g->lev[level].d.my;
+  dims[2] = g->lev[level].d.mz;
+  return VFS_OK;
+}
+
+int vfs_get_metrics(vfs_ctx* ctx, int grid, int level, double* out) {
+  if (!ctx || !out) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Level& L = g->lev[level];
+  CK(cudaMemcpy(out, L.M, MP_TOTAL * L.N * sizeof(double), cudaMemcpyDeviceToHost));
+  return VFS_OK;
+}
+
+int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out) {
+  if (!ctx || !out) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Level& L = g->lev[level];
+  CK(cudaMemcpy(out, L.nvert, L.N * sizeof(double), cudaMemcpyDeviceToHost));
+  return VFS_OK;
+}
+
+int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out) {
+  if (!ctx || !out) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (!g->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  Level& L = g->lev[level];
+  if (which == 0) CK(cudaMemcpy(out, L.coef, 19 * L.N * sizeof(double), cudaMemcpyDeviceToHost));
+  else if (which == 1) CK(cudaMemcpy(out, L.mcoef, 19 * L.N * sizeof(double), cudaMemcpyDeviceToHost));
+  else if (which == 2) {
+    std::vector<float> f(19 * L.N);
+    CK(cudaMemcpy(f.data(), L.mcoef32, 19 * L.N * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < f.size(); q++) out[q] = f[q];
+  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1 or 2");
+  return VFS_OK;
+}
+
+int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, double* y) {
+  if (!ctx || !x || !y) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || level < 0 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  Level& L = g.lev[level];
+  const size_t N = L.N;
+  if (which == 0 || which == 1) {
+    double *dx, *dy;
+    CK(cudaMalloc(&dx, N * 8));
+    CK(cudaMalloc(&dy, N * 8));
+    CK(cudaMemcpy(dx, x, N * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dy, 0, N * 8));
+    if (which == 0) {
+      OpView<double> A{L.d, L.coef, L.mask, nullptr};
+      launch_apply64(A, dx, nullptr, dy, 0);
+    } else {
+      OpView<double> A{L.d, L.mcoef, L.mask, nullptr};
+      launch_apply_mg<double>(A, dx, nullptr, dy, 0);
+    }
+    cudaError_t e = cudaMemcpy(y, dy, N * 8, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
+  } else if (which == 2) {
+    std::vector<float> hx(N), hy(N);
+    for (size_t q = 0; q < N; q++) hx[q] = (float)x[q];
+    float *dx, *dy;
+    CK(cudaMalloc(&dx, N * 4));
+    CK(cudaMalloc(&dy, N * 4));
+    CK(cudaMemcpy(dx, hx.data(), N * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dy, 0, N * 4));
+    OpView<float> A{L.d, L.mcoef32, L.mask, nullptr};
+    launch_apply_mg<float>(A, dx, nullptr, dy, 0);
+    cudaError_t e = cudaMemcpy(hy.data(), dy, N * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
+    for (size_t q = 0; q < N; q++) y[q] = hy[q];
+  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1 or 2");
+  return VFS_OK;
+}
+
+int vfs_mg_restrict(vfs_ctx* ctx, int grid, int level, const double* x, double* y) {
+  if (!ctx || !x || !y) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || level < 1 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Grid& g = *gp;
+  Level &F = g.lev[level], &C = g.lev[level - 1];
+  double *dx, *dy;
+  CK(cudaMalloc(&dx, F.N * 8));
+  CK(cudaMalloc(&dy, C.N * 8));
+  CK(cudaMemcpy(dx, x, F.N * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dy, 0, C.N * 8));
+  launch_restrict<double>(F.d, dx, F.nvert, C.d, C.nvert, g.si, g.sj, g.sk, dy, 0);
+  cudaError_t e = cudaMemcpy(y, dy, C.N * 8, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "restrict");
+  return VFS_OK;
+}
+
+int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y) {
+  if (!ctx || !x || !y) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || level < 1 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  Level &F = g.lev[level], &C = g.lev[level - 1];
+  double *dx, *dy;
+  CK(cudaMalloc(&dx, C.N * 8));
+  CK(cudaMalloc(&dy, F.N * 8));
+  CK(cudaMemcpy(dx, x, C.N * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dy, 0, F.N * 8));
+  launch_prolong<double>(F.d, F.pcode, C.d, dx, dy, 0, nullptr, 0);
+  cudaError_t e = cudaMemcpy(y, dy, F.N * 8, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "prolong");
+  return VFS_OK;
+}
+
+int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x, double omega) {
+  if (!ctx || !x || !b) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp || level < 0 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  Level& L = g.lev[level];
+  double *db, *dx, *dy;
+  CK(cudaMalloc(&db, L.N * 8));
+  CK(cudaMalloc(&dx, L.N * 8));
+  CK(cudaMalloc(&dy, L.N * 8));
+  CK(cudaMemcpy(db, b, L.N * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dx, x, L.N * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemset(dy, 0, L.N * 8));
+  OpView<double> A{L.d, L.mcoef, L.mask, nullptr};
+  launch_smooth<double>(A, dx, db, dy, omega, 0);
+  cudaError_t e = cudaMemcpy(x, dy, L.N * 8, cudaMemcpyDeviceToHost);
+  cudaFree(db);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "smooth");
+  return VFS_OK;
+}
+
+int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_params* p, const double* v, double* z) {
+  if (!ctx || !v || !z || !p) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  const size_t N = ncell(g.d);
+  Level& F = g.lev[g.L - 1];
+  double* dv;
+  CK(cudaMalloc(&dv, N * 8));
+  CK(cudaMemcpy(dv, v, N * 8, cudaMemcpyHostToDevice));
+  int r;
+  if (precision == VFS_MIXED) {
+    r = ensure_mg<float>(ctx, g);
+    float* dz = nullptr;
+    if (!r && cudaMalloc(&dz, N * 4) != cudaSuccess) r = VFS_ERR_NOMEM;
+    if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s);
+    if (!r) {
+      std::vector<float> hz(N);
+      cudaStreamSynchronize(g.s);
+      cudaMemcpy(hz.data(), dz, N * 4, cudaMemcpyDeviceToHost);
+      for (size_t q = 0; q < N; q++) z[q] = hz[q];
+    }
+    cudaFree(dz);
+  } else {
+    r = ensure_mg<double>(ctx, g);
+    double* dz = nullptr;
+    if (!r && cudaMalloc(&dz, N * 8) != cudaSuccess) r = VFS_ERR_NOMEM;
+    if (!r) r = precond<double>(ctx, g, *p, dv, dz, F.x64[1], nullptr, g.s);
+    if (!r) {
+      cudaStreamSynchronize(g.s);
+      cudaMemcpy(z, dz, N * 8, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dz);
+  }
+  cudaFree(dv);
+  return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// Kernel launchers shared between the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vfs_common.cuh"
+
+namespace vfs {
+
+// Metric pack offsets in units of N doubles (same order as the CPU oracle):
+// csi eta zet (AoS, 3 each) aj | icsi ieta izet iaj | jcsi jeta jzet jaj |
+// kcsi keta kzet kaj | cent.
+enum {
+  MP_CSI = 0, MP_ETA = 3, MP_ZET = 6, MP_AJ = 9,
+  MP_ICSI = 10, MP_IETA = 13, MP_IZET = 16, MP_IAJ = 19,
+  MP_JCSI = 20, MP_JETA = 23, MP_JZET = 26, MP_JAJ = 29,
+  MP_KCSI = 30, MP_KETA = 33, MP_KZET = 36, MP_KAJ = 39,
+  MP_CENT = 40, MP_TOTAL = 43
+};
+
+// ---- setup (k_setup.cu) ----
+int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tmp, cudaStream_t s);
+int launch_gtensor(const Dims& d, const double* M, double* g, cudaStream_t s);
+int launch_assemble(const Dims& d, const double* g, const double* nvert, const double* aj, double* coef, double* mcoef,
+                    float* mcoef32, unsigned* mask, cudaStream_t s);
+int launch_coarsen(const Dims& f, const Dims& c, int si, int sj, int sk, const double* coor_f, const double* nv_f,
+                   double* coor_c, double* nv_c, cudaStream_t s);
+int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nv_f, const double* nv_c,
+                         uint8_t* code, cudaStream_t s);
+int launch_dense_inverse(const Dims& d, const double* mcoef, double sigma, double* W, double* fac, int* piv, double* pval,
+                         double* Binv, float* Binv32, int n, cudaStream_t s);
+
+// ---- stencils and multigrid (k_mg.cu) ----
+// y = A x (FP64 accumulate; x FP64 or FP32); r = b - A x when b != nullptr.
+int launch_apply64(const OpView<double>& A, const double* x, const double* b, double* y, cudaStream_t s);
+int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, double* y, cudaStream_t s);
+// multigrid operator apply in precision T (testing hook / residual)
+template <typename T>
+int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s);
+// one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0
+template <typename T>
+int launch_smooth(const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
+// fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc
+template <typename T>
+int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
+                             const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s);
+// plain restriction of a fine vector (testing hook)
+template <typename T>
+int launch_restrict(const Dims& f, const T* x, const double* nvf, const Dims& c, const double* nvc, int si, int sj, int sk,
+                    T* out, cudaStream_t s);
+// xf += P xc (MyInterpolation) using the prolongation codes of the fine level; add == 0 overwrites
+template <typename T>
+int launch_prolong(const Dims& f, const uint8_t* code, const Dims& c, const T* xc, T* xf, int add, const int* skip,
+                   cudaStream_t s);
+// x = Binv b over the packed interior of the coarsest level
+template <typename T>
+int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const int* skip, cudaStream_t s);
+// fine-level preconditioner input: out = T(aj * v)
+template <typename T>
+int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s);
+
+}  // namespace vfs

@@ -1,0 +1,71 @@
+// Launchers of the per-step FP64 kernels (k_proj.cu) and the Krylov kernels
+// (k_krylov.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vfs_common.cuh"
+
+namespace vfs {
+
+// Contravariant flux Ucont as three component arrays (SoA) on the device.
+struct Ucont {
+  double *x, *y, *z;
+};
+
+int partial_blocks(const Dims& d);
+int launch_finish_sums(const double* parts, int nparts, int nq, double* out, cudaStream_t s);
+int launch_aos2soa(size_t n, const double* aos, double* x, double* y, double* z, cudaStream_t s);
+int launch_soa2aos(size_t n, const double* x, const double* y, const double* z, double* aos, cudaStream_t s);
+int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, double st, double coeff, int meanfix,
+               double* b, double* parts, double* sc, cudaStream_t s);
+int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nvert, const double* M, double* parts,
+                       double* fa4, cudaStream_t s);
+int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s);
+int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStream_t s);
+int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s);
+int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s);
+int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const double* phi, double dt,
+                      double st, double coeff, const Ucont& u, cudaStream_t s);
+int launch_contra2cart(const Dims& d, const double* M, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
+int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
+                      cudaStream_t s);
+
+// ---- FGMRES device state (k_krylov.cu) ----
+// One flexible GMRES(m) solve keeps all of its scalars on the device so an
+// iteration is a fixed sequence of launches with no host round trip; every
+// kernel returns at once when the solve has converged.
+struct KrylovState {
+  int m;          // restart length
+  int j;          // current Arnoldi column
+  int done;       // 1 once converged (or broken down)
+  int it;         // preconditioner applications so far
+  int reorth;     // 1 if the second Gram-Schmidt pass is needed this column
+  double rtol, bnorm, beta, resid;
+  double hn, inv_hn;
+  double* H;      // (m+1) x m, column-major: H[j*(m+1) + i]
+  double* cs;     // m
+  double* sn;     // m
+  double* g;      // m+1
+  double* y;      // m
+  double* h;      // m+1 dots of the current pass
+  double* hacc;   // m+1 accumulated dots of the column
+};
+
+// parts must hold nblocks * (m + 2) doubles.
+int krylov_nblocks(size_t n);
+int launch_norm_init(KrylovState* st, const double* r, size_t n, double* parts, int is_b, cudaStream_t s);
+int launch_vec_scale_first(KrylovState* st, const double* r, double* v0, size_t n, cudaStream_t s);
+int launch_multidot(KrylovState* st, const double* V, int nv, const double* w, size_t n, double* parts, int pass,
+                    cudaStream_t s);
+int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, int pass, cudaStream_t s);
+int launch_arnoldi_finish(KrylovState* st, int nparts, const double* parts, cudaStream_t s);
+int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStream_t s);
+int launch_lsq_update(KrylovState* st, cudaStream_t s);
+template <typename T>
+int launch_x_update(KrylovState* st, const T* Z, size_t n, double* x, cudaStream_t s);
+int launch_restart_reset(KrylovState* st, cudaStream_t s);
+int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s);
+int launch_norm2(const double* v, size_t n, double* parts, double* out, cudaStream_t s);
+
+}  // namespace vfs
