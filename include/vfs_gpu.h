@@ -71,18 +71,26 @@ typedef struct {
 
 typedef struct {
   int precision;   /* VFS_FP64 or VFS_MIXED */
-  double rtol;     /* stop when ||b - A phi|| <= rtol * ||b|| */
+  double rtol;     /* relative tolerance on the aj-scaled residual (see div_tol) */
   int maxit;       /* maximum preconditioner applications */
   int restart;     /* FGMRES restart length (<= 64) */
   int nu1, nu2;    /* pre / post y-line smoothing sweeps per level */
   double omega;    /* line-Jacobi damping */
   int warm_start;  /* 1: start from the resident phi, 0: from zero */
+  double div_tol;  /* > 0: also require max |div u| <= div_tol after the projection */
 } vfs_solve_params;
+/* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
+ * form the reference's multigrid path assembles (poisson == -1 scales every
+ * row by aj, poisson.c:1560, with the RHS scaled alike).  Its residual r_s =
+ * aj (b - A phi) is, cell by cell, the divergence the projection leaves
+ * divided by dt st / coeff, so the solve stops when ||r_s|| <= rtol ||aj b||
+ * and, when div_tol > 0, dt st / coeff * ||r_s|| <= div_tol, which bounds
+ * max |div u| by div_tol. */
 
 typedef struct {
   int iterations;  /* preconditioner applications */
   int converged;
-  double relres;   /* true ||b - A phi|| / ||b|| at exit */
+  double relres;   /* true ||aj (b - A phi)|| / ||aj b|| at exit */
   double bnorm;
   double time_ms;  /* device time of the solve */
 } vfs_solve_info;

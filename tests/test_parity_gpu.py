@@ -125,7 +125,7 @@ def test_rhs_flux_projection_divergence(gpu_ctx, loaded):
     fa = O.volume_flux(d, case.immersed, u, g.nvert, M)
     gpu_ctx.set_field(gid, capi.FIELD_UCONT, case.ucont)
     fa_g = gpu_ctx.volume_flux(gid)
-    assert np.allclose(fa_g, fa, rtol=1e-12, atol=1e-15)
+    assert np.allclose(fa_g, fa, rtol=1e-12, atol=1e-13 * abs(fa[0]))  # flux after the balance is rounding residue
     assert np.abs(gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape) - u).max() <= 1e-14 * np.abs(u).max()
     gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
     b, s = O.rhs(d, u, g.nvert)

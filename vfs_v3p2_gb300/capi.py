@@ -59,7 +59,7 @@ class GridDesc(ctypes.Structure):
 class SolveParams(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
-                ("omega", ctypes.c_double), ("warm_start", ctypes.c_int)]
+                ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):

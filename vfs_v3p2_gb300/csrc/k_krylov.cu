@@ -22,6 +22,9 @@ int krylov_nblocks(size_t n) {
 }
 
 __device__ __forceinline__ bool is_done(const KrylovState* st) { return *(volatile const int*)&st->done; }
+__device__ __forceinline__ bool met(const KrylovState* st, double r) {
+  return r <= st->rtol * st->bnorm && (st->atol <= 0. || r <= st->atol);
+}
 
 // ||v||^2 partials; then finish: is_b ? bnorm : beta (+ g[0], done check).
 __global__ void __launch_bounds__(KB) k_sq_partials(const KrylovState* st, const double* __restrict__ v, size_t n,
@@ -58,7 +61,7 @@ __global__ void k_norm_finish(KrylovState* st, const double* __restrict__ parts,
       for (int q = 0; q < (st->m + 1) * st->m; q++) st->H[q] = 0.;
       st->j = 0;
       st->inv_hn = nrm > 0. ? 1. / nrm : 0.;
-      if (nrm <= st->rtol * st->bnorm) st->done = 1;
+      if (met(st, nrm)) st->done = 1;
     }
   }
 }
@@ -197,7 +200,7 @@ __global__ void k_arnoldi_finish(KrylovState* st, const double* __restrict__ par
   st->inv_hn = hn > 0. ? 1. / hn : 0.;
   st->j = j + 1;
   st->it += 1;
-  if (st->resid <= st->rtol * st->bnorm || hn == 0. || !(st->resid == st->resid)) st->done = 1;
+  if (met(st, st->resid) || hn == 0. || !(st->resid == st->resid)) st->done = 1;
 }
 int launch_arnoldi_finish(KrylovState* st, int nparts, const double* parts, cudaStream_t s) {
   k_arnoldi_finish<<<1, KB, 0, s>>>(st, parts, nparts); ++g_launches;

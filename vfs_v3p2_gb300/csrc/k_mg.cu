@@ -93,66 +93,66 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 }
 
 // ---------------------------------------------------------------------------
-// Damped y-line Jacobi sweep.  One block owns a tile of TW consecutive
-// i-columns x all j of one k plane.  Phase 1 (all threads, coalesced over i):
-// the residual r = b - A x and the tridiagonal (SP, CP, NP) entries of every
-// cell of the tile go to shared memory.  Phase 2 (one thread per column):
-// Thomas elimination in shared memory.  Phase 3: xo = xi + omega * delta.
-// Couplings across a j-periodic seam and to non-fluid cells stay in the
-// residual (off-line); non-fluid cells are identity rows with delta = 0.
+// Damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi), T the
+// tridiagonal j-coupling (SP, CP, NP) of each (i, k) column.  T is constant
+// per level, so its Thomas factors c'_j and 1/m_j are precomputed at setup
+// (k_line_factors) and the per-column recurrences are one FMA (forward) and
+// one FMA (backward) deep.  One block owns TW consecutive i-columns x all j
+// of one k plane: phase 1 (all threads, coalesced over i) forms the residual
+// and stages it with the factors in shared memory, phase 2 (one thread per
+// column) runs the two substitutions, phase 3 writes xo.  Couplings across a
+// j-periodic seam and to non-fluid cells stay in the residual; non-fluid
+// cells have delta = 0.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict__ xi, const T* __restrict__ b,
-                                                T* __restrict__ xo, T omega, int TW) {
+__global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi,
+                                                const T* __restrict__ b, T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
   extern __shared__ unsigned char smraw[];
   const Dims d = A.d;
   const int nj = d.my - 2;
   T* sr = (T*)smraw;
   T* sa = sr + TW * nj;
-  T* sd = sa + TW * nj;
-  T* sc = sd + TW * nj;
+  T* sl = sa + TW * nj;  // c'_j
+  T* si = sl + TW * nj;  // 1 / m_j
   const size_t N = ncell(d);
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
+#pragma unroll 2
   for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
     const int il = idx % TW, jl = idx / TW;
     const int i = i0 + il, j = 1 + jl;
-    T r = T(0), a = T(0), dd = T(1), cc = T(0);
+    T r = T(0), a = T(0), lc = T(0), li = T(1);
     if (i <= d.mx - 2) {
       const size_t c = cidx(d, i, j, k);
-      const T cp = A.coef[c];
+      const T cp = __ldg(A.coef + c);
       if (cp != T(0)) {
-        T ax = xi ? stencil<T, T, T>(d, A.coef, A.mask, xi, i, j, k) : T(0);
-        r = b[c] - ax;
-        dd = cp;
-        a = (j > 1) ? A.coef[(size_t)SP * N + c] : T(0);
-        cc = (j < d.my - 2) ? A.coef[(size_t)NP * N + c] : T(0);
+        const T ax = xi ? stencil<T, T, T>(d, A.coef, A.mask, xi, i, j, k) : T(0);
+        r = __ldg(b + c) - ax;
+        a = (j > 1) ? __ldg(A.coef + (size_t)SP * N + c) : T(0);
+        lc = __ldg(lf + c);
+        li = __ldg(lf + N + c);
       }
     }
     sr[idx] = r;
     sa[idx] = a;
-    sd[idx] = dd;
-    sc[idx] = cc;
+    sl[idx] = lc;
+    si[idx] = li;
   }
   __syncthreads();
   if (threadIdx.x < TW) {
     const int il = threadIdx.x;
-    T cprev = T(0), dprev = T(0);
+    T dprev = T(0);
     for (int jl = 0; jl < nj; jl++) {
       const int q = jl * TW + il;
-      const T a = sa[q];
-      const T inv = T(1) / (sd[q] - a * cprev);
-      cprev = sc[q] * inv;
-      dprev = (sr[q] - a * dprev) * inv;
-      sc[q] = cprev;
+      dprev = (sr[q] - sa[q] * dprev) * si[q];
       sr[q] = dprev;
     }
     T xn = T(0);
     for (int jl = nj - 1; jl >= 0; jl--) {
       const int q = jl * TW + il;
-      xn = sr[q] - sc[q] * xn;
+      xn = sr[q] - sl[q] * xn;
       sr[q] = xn;
     }
   }
@@ -168,24 +168,56 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
 }
 
 template <typename T>
-static int smooth_tw(int nj) {
-  int tw = 32;
-  while (tw > 4 && (size_t)4 * tw * nj * sizeof(T) > 64 * 1024) tw >>= 1;
+static int smooth_tw(int ni, int nj) {
+  int tw = 16;
+  while (tw > 4 && (size_t)4 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
+  while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   return tw;
 }
 
 template <typename T>
-int launch_smooth(const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
+int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_smooth<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
-  const int tw = smooth_tw<T>(nj);
+  const int tw = smooth_tw<T>(ni, nj);
   const size_t sm = (size_t)4 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
-  k_smooth<T><<<g, 256, sm, s>>>(A, xi, b, xo, omega, tw); ++g_launches;
+  k_smooth<T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Thomas factors of the y-line tridiagonal (SP, CP, NP) of every column, in
+// FP64 from the aj-scaled FP64 operator: lf[c] = c'_j, lf[N + c] = 1/m_j, as
+// T.  Non-fluid cells are identity rows; j-periodic seam couplings stay off.
+template <typename T>
+__global__ void k_line_factors(Dims d, const double* __restrict__ mcoef, T* __restrict__ lf) {
+  const size_t N = ncell(d);
+  const int ni = d.mx - 2, nk = d.mz - 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ni * nk; t += gridDim.x * blockDim.x) {
+    const int i = 1 + t % ni, k = 1 + t / ni;
+    double cprev = 0.;
+    for (int j = 1; j < d.my - 1; j++) {
+      const size_t c = cidx(d, i, j, k);
+      double a = (j > 1) ? mcoef[(size_t)SP * N + c] : 0.;
+      double bb = mcoef[c];
+      double cc = (j < d.my - 2) ? mcoef[(size_t)NP * N + c] : 0.;
+      if (bb == 0.) { a = 0.; bb = 1.; cc = 0.; }
+      const double m = bb - a * cprev;
+      const double inv = 1. / m;
+      cprev = cc * inv;
+      lf[c] = (T)cprev;
+      lf[N + c] = (T)inv;
+    }
+  }
+}
+template <typename T>
+int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s) {
+  const int n = (d.mx - 2) * (d.mz - 2);
+  k_line_factors<T><<<(n + 127) / 128, 128, 0, s>>>(d, mcoef, lf); ++g_launches;
   return (int)cudaGetLastError();
 }
 
@@ -340,7 +372,7 @@ __global__ void __launch_bounds__(TX* TY) k_scale_in(Dims d, const double* __res
   TILE_LOOP(d) {
     if (!_in) continue;
     const size_t c = cidx(d, i, j, k);
-    out[c] = (T)(aj[c] * v[c]);
+    out[c] = (T)(aj ? aj[c] * v[c] : v[c]);
   }
 }
 template <typename T>
@@ -351,7 +383,8 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
 
 #define INST(T)                                                                                                        \
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
-  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, T*, T, cudaStream_t);                           \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t);                 \
+  template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
   template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const double*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \
   template int launch_restrict<T>(const Dims&, const T*, const double*, const Dims&, const double*, int, int, int, T*, \

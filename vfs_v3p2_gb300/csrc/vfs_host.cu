@@ -14,6 +14,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -52,6 +53,23 @@ struct Probe {
 };
 Probe g_probe;
 
+// VFS_DEBUG_SYNC=1: synchronise after every launch stage of the solve and
+// report the first stage that leaves a CUDA error (a self-check for faults).
+const bool g_debug = [] {
+  const char* e = getenv("VFS_DEBUG_SYNC");
+  return e && e[0] == '1';
+}();
+int g_debug_err = 0;
+void dbg(const char* stage, int level, int rc, cudaStream_t s) {
+  if (!g_debug || g_debug_err) return;
+  cudaError_t e = rc ? (cudaError_t)rc : cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_debug_err = (int)e;
+    fprintf(stderr, "VFS_DEBUG_SYNC: %s (level %d) -> %s\n", stage, level, cudaGetErrorString(e));
+  }
+}
+
 constexpr int MAXLEV = 12;
 constexpr int MAXRESTART = 64;
 constexpr int DENSE_MAX = 8192;  // largest coarsest level solved by a dense inverse
@@ -65,6 +83,8 @@ struct Level {
   double* coef = nullptr;
   double* mcoef = nullptr;
   float* mcoef32 = nullptr;
+  float* lf32 = nullptr;   // y-line Thomas factors [c' | 1/m]
+  double* lf64 = nullptr;
   unsigned mask = 0;
   uint8_t* pcode = nullptr;
   float* x32[2] = {nullptr, nullptr};
@@ -86,6 +106,8 @@ struct Grid {
   double* p = nullptr;
   double* phi = nullptr;
   double* b = nullptr;
+  double* bs = nullptr;     // aj-scaled right-hand side of the outer solve
+  double dt = 0.04, st_ = 1.0, coeff = 1.0;  // of the last right-hand side
   double* ucat = nullptr;   // AoS
   double* aos = nullptr;    // AoS staging
   int m = 0;
@@ -145,8 +167,11 @@ int galloc(vfs_ctx* ctx, Grid& g, T** out, size_t count) {
     cudaGetLastError();
     return fail(ctx, VFS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
-  e = cudaMemset(p, 0, bytes ? bytes : 16);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemset");
+  // Zero on the grid's own stream: a plain cudaMemset runs on the legacy
+  // default stream, which does not order against the grid's non-blocking
+  // stream, and could land after later writes (e.g. the Krylov state copy).
+  e = cudaMemsetAsync(p, 0, bytes ? bytes : 16, g.s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemsetAsync");
   g.allocs.push_back(p);
   g.bytes += bytes;
   ctx->used += bytes;
@@ -187,6 +212,9 @@ template <> double** xbuf<double>(Level& L) { return L.x64; }
 template <typename T> T*& bbuf(Level& L);
 template <> float*& bbuf<float>(Level& L) { return L.b32; }
 template <> double*& bbuf<double>(Level& L) { return L.b64; }
+template <typename T> T* lf_of(Level& L);
+template <> float* lf_of<float>(Level& L) { return L.lf32; }
+template <> double* lf_of<double>(Level& L) { return L.lf64; }
 template <typename T> T* binv(Level& L);
 template <> float* binv<float>(Level& L) { return L.Binv32; }
 template <> double* binv<double>(Level& L) { return L.Binv; }
@@ -246,8 +274,9 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 template <typename T>
 void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
-  launch_smooth<T>(A, xi, b, xo, omega, s);
+  int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s);
   if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 3));
+  dbg("smooth", l, rc, s);
 }
 
 template <typename T>
@@ -256,14 +285,14 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   OpView<T> A = mgview<T>(L, skip);
   if (l == 0) {
     if (binv<T>(L)) {
-      launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, xa, skip, s);
+      dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, xa, skip, s), s);
       return xa;
     }
     T* cur = nullptr;
     T* bufs[2] = {xa, xb};
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      launch_smooth<T>(A, cur, b, o, (T)c.omega_c, s);
+      launch_smooth<T>(A, lf_of<T>(L), cur, b, o, (T)c.omega_c, s);
       cur = o;
     }
     return cur ? cur : xa;
@@ -278,14 +307,14 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   Level& C = g.lev[l - 1];
   T** xc = xbuf<T>(C);
-  launch_residual_restrict<T>(A, cur, b, L.nvert, C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s);
+  dbg("residual_restrict", l, launch_residual_restrict<T>(A, cur, b, L.nvert, C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s), s);
   T* ec = vcycle<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, skip, s);
   if (!cur) {
     cur = bufs[q & 1];
     q++;
-    launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 0, skip, s);
+    dbg("prolong", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 0, skip, s), s);
   } else {
-    launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s);
+    dbg("prolong_add", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s), s);
   }
   for (int r = 0; r < c.nu2; r++, q++) {
     T* o = bufs[q & 1];
@@ -310,22 +339,23 @@ template <typename T>
 int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T* z, T* tmp, const int* skip,
             cudaStream_t s) {
   Level& F = g.lev[g.L - 1];
-  const double* aj = F.M + F.N * MP_AJ;
   T* bf = bbuf<T>(F);
-  launch_scale_in<T>(F.d, aj, v, bf, skip, s);
+  dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s), s);
   T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p), skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
 }
 
+// The outer operator is the aj-scaled FP64 operator (the multigrid path's
+// form of the same system).
 int apply_outer(Grid& g, const double* x, const double* b, double* y, const int* skip, cudaStream_t s) {
   Level& F = g.lev[g.L - 1];
-  OpView<double> A{F.d, F.coef, F.mask, skip};
+  OpView<double> A{F.d, F.mcoef, F.mask, skip};
   return launch_apply64(A, x, b, y, s);
 }
 int apply_outer(Grid& g, const float* x, const double* b, double* y, const int* skip, cudaStream_t s) {
   Level& F = g.lev[g.L - 1];
-  OpView<double> A{F.d, F.coef, F.mask, skip};
+  OpView<double> A{F.d, F.mcoef, F.mask, skip};
   return launch_apply64_xf(A, x, b, y, s);
 }
 
@@ -357,6 +387,7 @@ int fg_start(vfs_ctx* ctx, Fgmres& f) {
   KrylovState h{};
   h.m = p.restart;
   h.rtol = p.rtol;
+  h.atol = p.div_tol > 0. ? p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
   double* a = g.starr;
   h.H = a; a += (size_t)(p.restart + 1) * p.restart;
   h.cs = a; a += p.restart + 2;
@@ -371,10 +402,12 @@ int fg_start(vfs_ctx* ctx, Fgmres& f) {
   }
   CK(cudaMemcpyAsync(g.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   if (!p.warm_start) CK(cudaMemsetAsync(g.phi, 0, N * sizeof(double), s));
-  launch_norm_init(g.st, g.b, N, g.parts, 1, s);
-  apply_outer(g, g.phi, g.b, g.V, &g.st->done, s);
-  launch_norm_init(g.st, g.V, N, g.parts, 0, s);
-  launch_vec_scale_first(g.st, g.V, g.V, N, s);
+  Level& F = g.lev[g.L - 1];
+  dbg("scale_rhs", 0, launch_scale_in<double>(F.d, F.M + F.N * MP_AJ, g.b, g.bs, nullptr, s), s);
+  dbg("bnorm", 0, launch_norm_init(g.st, g.bs, N, g.parts, 1, s), s);
+  dbg("residual0", 0, apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s), s);
+  dbg("beta", 0, launch_norm_init(g.st, g.V, N, g.parts, 0, s), s);
+  dbg("v0", 0, launch_vec_scale_first(g.st, g.V, g.V, N, s), s);
   f.it = 0;
   f.j = 0;
   f.observed = f.finished = false;
@@ -399,15 +432,17 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
   if (r) return r;
   {
     const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
+    dbg("precond_done", g.L - 1, 0, s);
     apply_outer(g, zj, nullptr, g.w, skip, s);
     if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + sizeof(T) + 8.0));
   }
-  launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s);
-  launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s);
-  launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s);
-  launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s);
-  launch_arnoldi_finish(g.st, nb, g.parts, s);
-  launch_vnext(g.st, g.w, g.V + (size_t)(f.j + 1) * N, N, s);
+  dbg("apply64", g.L - 1, 0, s);
+  dbg("multidot1", 0, launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s), s);
+  dbg("gs_update1", 0, launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s), s);
+  dbg("multidot2", 0, launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s), s);
+  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s), s);
+  dbg("arnoldi", 0, launch_arnoldi_finish(g.st, nb, g.parts, s), s);
+  dbg("vnext", 0, launch_vnext(g.st, g.w, g.V + (size_t)(f.j + 1) * N, N, s), s);
   f.it++;
   f.j++;
   launch_status_copy(g.st, &g.hstat[f.it & 1], s);
@@ -417,14 +452,14 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
     if (g.hstat[(f.it - 1) & 1]) f.observed = true;
   }
   if (f.observed || f.it >= p.maxit || f.j == f.p->restart) {
-    launch_lsq_update(g.st, s);
-    launch_x_update<T>(g.st, Z, N, g.phi, s);
-    launch_restart_reset(g.st, s);
+    dbg("lsq", 0, launch_lsq_update(g.st, s), s);
+    dbg("x_update", 0, launch_x_update<T>(g.st, Z, N, g.phi, s), s);
+    dbg("restart_reset", 0, launch_restart_reset(g.st, s), s);
     if (f.observed || f.it >= p.maxit) {
       f.finished = true;
       return VFS_OK;
     }
-    apply_outer(g, g.phi, g.b, g.V, skip, s);
+    apply_outer(g, g.phi, g.bs, g.V, skip, s);
     launch_norm_init(g.st, g.V, N, g.parts, 0, s);
     launch_vec_scale_first(g.st, g.V, g.V, N, s);
     f.j = 0;
@@ -438,10 +473,10 @@ int fg_finish(vfs_ctx* ctx, Fgmres& f, vfs_solve_info* info) {
   const size_t N = ncell(g.d);
   cudaStream_t s = g.s;
   Level& F = g.lev[g.L - 1];
-  apply_outer(g, g.phi, g.b, g.w, nullptr, s);  // w = b - A phi
-  launch_norm2(g.w, N, g.parts, g.scal + 16, s);
-  launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s);
-  launch_phi_finish(F.d, F.nvert, g.phi, s);
+  dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
+  dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
+  dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s), s);
+  dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
   CK(cudaEventRecord(g.t1, s));
   KrylovState h{};
   double rn = 0.;
@@ -452,7 +487,7 @@ int fg_finish(vfs_ctx* ctx, Fgmres& f, vfs_solve_info* info) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, g.t0, g.t1);
     info->iterations = h.it;
-    info->converged = (h.done && h.resid <= h.rtol * h.bnorm) || h.bnorm == 0.;
+    info->converged = (h.done && h.resid <= h.rtol * h.bnorm && (h.atol <= 0. || h.resid <= h.atol)) || h.bnorm == 0.;
     info->bnorm = h.bnorm;
     info->relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
     info->time_ms = ms;
@@ -484,6 +519,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->maxit < 1) return fail(ctx, VFS_ERR_ARG, "maxit must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 + p->nu2 < 1) return fail(ctx, VFS_ERR_ARG, "need at least one smoothing sweep");
   if (!(p->rtol > 0.)) return fail(ctx, VFS_ERR_ARG, "rtol must be > 0");
+  if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   return VFS_OK;
 }
@@ -499,7 +535,7 @@ int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* i
 
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
-  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19) * 8 + N * 19 * 4 + N;  // coor nvert M coef mcoef mcoef32 pcode
+  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 2) * 8 + N * (19 + 2) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 3 + 3 + 3 + 3 + 3);                    // pd u ustar p phi b ucat aos
   return b;
@@ -522,6 +558,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->nu2 = 2;
   p->omega = 0.8;
   p->warm_start = 0;
+  p->div_tol = 0.;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -640,6 +677,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.coef, 19 * Lv.N);
     GAB(Lv.mcoef, 19 * Lv.N);
     GAB(Lv.mcoef32, 19 * Lv.N);
+    GAB(Lv.lf32, 2 * Lv.N);
+    GAB(Lv.lf64, 2 * Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
   }
   const size_t N = ncell(d);
@@ -650,6 +689,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   GAB(g.p, N);
   GAB(g.phi, N);
   GAB(g.b, N);
+  GAB(g.bs, N);
   GAB(g.ucat, 3 * N);
   GAB(g.aos, 3 * N);
   GAB(g.parts, (size_t)krylov_nblocks(N) * 72 + 4096);
@@ -704,6 +744,8 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     launch_assemble(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.coef, Lv.mcoef, Lv.mcoef32, dmask, g.s);
     CK(cudaMemcpyAsync(&Lv.mask, dmask, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
+    launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
+    launch_line_factors<double>(Lv.d, Lv.mcoef, Lv.lf64, g.s);
   }
   Level& F = g.lev[g.L - 1];
   launch_proj_dots(F.d, F.M, g.pd, g.s);
@@ -817,6 +859,9 @@ int vfs_poisson_rhs(vfs_ctx* ctx, int grid, double dt, double st, double coeff, 
   if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
+  g.dt = dt;
+  g.st_ = st;
+  g.coeff = coeff;
   launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, meanfix, g.b, g.parts, g.scal + 4, g.s);
   double sc[2];
   CK(cudaMemcpyAsync(sc, g.scal + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
@@ -882,16 +927,19 @@ namespace {
 // solve start (flux balance, RHS).
 void step_pre(Grid& g, double dt, double st, double coeff) {
   Level& F = g.lev[g.L - 1];
-  launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s);
-  launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s);
+  g.dt = dt;
+  g.st_ = st;
+  g.coeff = coeff;
+  dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s), g.s);
+  dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s), g.s);
 }
 // After the solve: pressure, projection, Contra2Cart, divergence.
 void step_post(Grid& g, double dt, double st, double coeff) {
   Level& F = g.lev[g.L - 1];
-  launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s);
-  launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s);
-  launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s);
-  launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s);
+  dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
+  dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s), g.s);
+  dbg("contra2cart", 0, launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s), g.s);
+  dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s), g.s);
 }
 
 }  // namespace
@@ -1211,7 +1259,7 @@ int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x,
   CK(cudaMemcpy(dx, x, L.N * 8, cudaMemcpyHostToDevice));
   CK(cudaMemset(dy, 0, L.N * 8));
   OpView<double> A{L.d, L.mcoef, L.mask, nullptr};
-  launch_smooth<double>(A, dx, db, dy, omega, 0);
+  launch_smooth<double>(A, L.lf64, dx, db, dy, omega, 0);
   cudaError_t e = cudaMemcpy(x, dy, L.N * 8, cudaMemcpyDeviceToHost);
   cudaFree(db);
   cudaFree(dx);
@@ -1236,6 +1284,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     r = ensure_mg<float>(ctx, g);
     float* dz = nullptr;
     if (!r && cudaMalloc(&dz, N * 4) != cudaSuccess) r = VFS_ERR_NOMEM;
+    if (!r) cudaMemsetAsync(dz, 0, N * 4, g.s);
     if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s);
     if (!r) {
       std::vector<float> hz(N);
@@ -1248,6 +1297,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     r = ensure_mg<double>(ctx, g);
     double* dz = nullptr;
     if (!r && cudaMalloc(&dz, N * 8) != cudaSuccess) r = VFS_ERR_NOMEM;
+    if (!r) cudaMemsetAsync(dz, 0, N * 8, g.s);
     if (!r) r = precond<double>(ctx, g, *p, dv, dz, F.x64[1], nullptr, g.s);
     if (!r) {
       cudaStreamSynchronize(g.s);

@@ -38,9 +38,12 @@ int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, 
 // multigrid operator apply in precision T (testing hook / residual)
 template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s);
-// one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0
+// one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0;
+// lf = precomputed line factors [c'_j | 1/m_j] (2N of T)
 template <typename T>
-int launch_smooth(const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
+int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
+template <typename T>
+int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
 // fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc
 template <typename T>
 int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
@@ -56,7 +59,7 @@ int launch_prolong(const Dims& f, const uint8_t* code, const Dims& c, const T* x
 // x = Binv b over the packed interior of the coarsest level
 template <typename T>
 int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const int* skip, cudaStream_t s);
-// fine-level preconditioner input: out = T(aj * v)
+// fine-level preconditioner input: out = T(aj * v), or T(v) when aj is null
 template <typename T>
 int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s);
 

@@ -41,7 +41,7 @@ struct KrylovState {
   int done;       // 1 once converged (or broken down)
   int it;         // preconditioner applications so far
   int reorth;     // 1 if the second Gram-Schmidt pass is needed this column
-  double rtol, bnorm, beta, resid;
+  double rtol, atol, bnorm, beta, resid;  // converged: resid <= rtol*bnorm and (atol <= 0 or resid <= atol)
   double hn, inv_hn;
   double* H;      // (m+1) x m, column-major: H[j*(m+1) + i]
   double* cs;     // m
