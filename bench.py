@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="sphere", choices=["channel", "sphere", "terrain"])
     ap.add_argument("--scale", type=int, default=1, help="divide each grid extent (quick runs)")
+    ap.add_argument("--grid", default=None, help="NIxNJxNK override of the sphere workload (profiling sizes)")
     ap.add_argument("--rtol", type=float, default=1e-9)
     ap.add_argument("--div-tol", type=float, default=1e-8, help="max |div u| the solve must reach")
     ap.add_argument("--nu", type=int, default=2)
@@ -59,7 +60,12 @@ def parse():
 
 
 def make_case(args):
+    import math
     from vfs_v3p2_gb300 import synth
+    if args.grid:
+        ni, nj, nk = (int(v) for v in args.grid.lower().split("x"))
+        return synth.channel_case(ni, nj, nk, seed=1002, spheres=[(math.pi, 0.0, math.pi / 2, 0.3)], sigma=0.1,
+                                  levels=5, profile=synth.poiseuille, name=f"sphere_{ni}x{nj}x{nk}")
     if args.config == "channel":
         return synth.c1_channel(args.scale)
     if args.config == "terrain":

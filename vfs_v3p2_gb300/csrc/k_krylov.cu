@@ -167,6 +167,58 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
   return (int)cudaGetLastError();
 }
 
+// Fused CGS2 middle pass: w <- w - V h (h from the first pass), and the
+// second pass's dots V_q . w computed on the updated element while the basis
+// values are still in registers.  NV = compile-time capacity (>= nv).
+template <int NV>
+__global__ void __launch_bounds__(KB) k_gs_update_dots(const KrylovState* st, const double* __restrict__ V, int nv,
+                                                       double* __restrict__ w, size_t n, double* parts, int ld) {
+  if (is_done(st)) return;
+  __shared__ double hs[NV];
+  __shared__ double red[KB / 32][NV];
+  for (int q = threadIdx.x; q < NV; q += blockDim.x) hs[q] = q < nv ? st->h[q] : 0.;
+  __syncthreads();
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) acc[q] = 0.;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    double v[NV];
+    double a = w[t];
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      v[q] = q < nv ? V[(size_t)q * n + t] : 0.;
+      a = fma(-hs[q], v[q], a);
+    }
+    w[t] = a;
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q] = fma(v[q], a, acc[q]);
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    double x = warp_sum(acc[q]);
+    if (lane == 0) red[wp][q] = x;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+    double x = 0.;
+    for (int u = 0; u < KB / 32; u++) x += red[u][q];
+    parts[(size_t)blockIdx.x * ld + q] = x;
+  }
+}
+
+int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s) {
+  const int nb = krylov_nblocks(n);
+  const int ld = 72;
+  if (nv <= 8) k_gs_update_dots<8><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
+  else if (nv <= 16) k_gs_update_dots<16><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
+  else if (nv <= 32) k_gs_update_dots<32><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
+  else return -1;
+  ++g_launches;
+  k_multidot_finish<<<1, KB, 0, s>>>(st, parts, nb, nv, ld, 2); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
 // Close Arnoldi column j: ||w||, Hessenberg column, Givens rotation, residual
 // estimate |g[j+1]|, convergence test, 1 / h[j+1][j] for the next basis vector.
 __global__ void k_arnoldi_finish(KrylovState* st, const double* __restrict__ parts, int nparts) {
@@ -266,6 +318,27 @@ int launch_norm2(const double* v, size_t n, double* parts, double* out, cudaStre
   k_sqrt_sum<<<1, KB, 0, s>>>(parts, nb, out); ++g_launches;
   return (int)cudaGetLastError();
 }
+
+// Next basis vector and multigrid input in one sweep: V_{j+1} = w / h_{j+1,j}
+// and out = T(V_{j+1}) over the interior; ghost entries of w are zero.
+template <typename T>
+__global__ void __launch_bounds__(KB) k_vnext_in(const KrylovState* st, const double* __restrict__ w, double* __restrict__ vn,
+                                                  T* __restrict__ out, size_t n) {
+  if (is_done(st)) return;
+  const double f = st->inv_hn;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const double v = w[t] * f;
+    vn[t] = v;
+    out[t] = (T)v;
+  }
+}
+template <typename T>
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s) {
+  k_vnext_in<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, out, n); ++g_launches;
+  return (int)cudaGetLastError();
+}
+template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t);
+template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t);
 
 int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s) {
   return (int)cudaMemcpyAsync(hst, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s);

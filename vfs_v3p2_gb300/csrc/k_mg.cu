@@ -30,65 +30,88 @@ __host__ __forceinline__ dim3 tile_grid(const Dims& d) {
   const int _k1 = min(_k0 + KCHUNK, (d).mz - 1);                           \
   for (int k = _k0; k < _k1; k++)
 
-// sum_m coef[m] * x[nbr(m)] for interior cell (i, j, k), accumulated in A.
-template <typename TC, typename TX_, typename TA>
-__device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef, unsigned mask, const TX_* __restrict__ x,
-                                      int i, int j, int k) {
+// Slot sets known at compile time: MASK_CH holds the slots of grids whose
+// metric has no i-j and no j-k cross terms (x-z skew, y stretching: the
+// channel and sphere grids), MASK_ALL all 19.  A level whose nonzero slots
+// fit MASK_CH runs the 11-slot instantiation.  With the set fixed at compile
+// time every load of a stencil is issued before its FMAs (no per-slot
+// branch), which keeps ~2 x slots loads in flight per cell.
+constexpr unsigned MASK_ALL = 0x7FFFFu;
+constexpr unsigned MASK_CH = (1u << CP) | (1u << EP) | (1u << WP) | (1u << NP) | (1u << SP) | (1u << TP) | (1u << BP) |
+                             (1u << TE) | (1u << BE) | (1u << TW) | (1u << BW);
+
+// sum_m coef[m] * x[nbr(m)] over the slots of MASK for interior cell (i, j, k).
+template <unsigned MASK, typename TC, typename TX_, typename TA>
+__device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x, int i, int j,
+                                      int k) {
   const size_t N = ncell(d);
   const size_t c = cidx(d, i, j, k);
   const int im = wrapi(i - 1, d.mx, d.ip), ip1 = wrapi(i + 1, d.mx, d.ip);
   const int jm = wrapi(j - 1, d.my, d.jp), jp1 = wrapi(j + 1, d.my, d.jp);
   const int km = wrapi(k - 1, d.mz, d.kp), kp1 = wrapi(k + 1, d.mz, d.kp);
   const int II[3] = {im, i, ip1}, JJ[3] = {jm, j, jp1}, KK[3] = {km, k, kp1};
-  TA s = TA(0);
+  TC cv[19];
+  TX_ xv[19];
 #pragma unroll
   for (int m = 0; m < 19; m++) {
-    if (mask & (1u << m)) {
-      const size_t n = cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]);
-      s = fma((TA)__ldg(coef + (size_t)m * N + c), (TA)__ldg(x + n), s);
+    if (MASK & (1u << m)) {
+      cv[m] = __ldg(coef + (size_t)m * N + c);
+      xv[m] = __ldg(x + cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]));
     }
   }
+  TA s = TA(0);
+#pragma unroll
+  for (int m = 0; m < 19; m++)
+    if (MASK & (1u << m)) s = fma((TA)cv[m], (TA)xv[m], s);
   return s;
 }
+
+__host__ __forceinline__ bool fits_ch(unsigned mask) { return (mask & ~MASK_CH) == 0u; }
 
 // ---------------------------------------------------------------------------
 // FP64 outer operator: y = A x, or y = b - A x.
 // ---------------------------------------------------------------------------
-template <typename TXin>
+template <unsigned MASK, typename TXin>
 __global__ void __launch_bounds__(TX* TY) k_apply64(OpView<double> A, const TXin* __restrict__ x, const double* __restrict__ b,
                                                     double* __restrict__ y) {
   if (skipped(A.skip)) return;
   TILE_LOOP(A.d) {
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    double s = stencil<double, TXin, double>(A.d, A.coef, A.mask, x, i, j, k);
+    double s = stencil<MASK, double, TXin, double>(A.d, A.coef, x, i, j, k);
     y[c] = b ? b[c] - s : s;
   }
 }
 
 int launch_apply64(const OpView<double>& A, const double* x, const double* b, double* y, cudaStream_t s) {
-  k_apply64<double><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  if (fits_ch(A.mask)) k_apply64<MASK_CH, double><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  else k_apply64<MASK_ALL, double><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, double* y, cudaStream_t s) {
-  k_apply64<float><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  if (fits_ch(A.mask)) k_apply64<MASK_CH, float><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  else k_apply64<MASK_ALL, float><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 
-template <typename T>
+template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(TX* TY) k_apply_mg(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                      T* __restrict__ y) {
   if (skipped(A.skip)) return;
   TILE_LOOP(A.d) {
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    T s = stencil<T, T, T>(A.d, A.coef, A.mask, x, i, j, k);
+    T s = stencil<MASK, T, T, T>(A.d, A.coef, x, i, j, k);
     y[c] = b ? b[c] - s : s;
   }
 }
 template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s) {
-  k_apply_mg<T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y); ++g_launches;
+  if (fits_ch(A.mask)) k_apply_mg<MASK_CH, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  else k_apply_mg<MASK_ALL, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 
@@ -104,7 +127,7 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // j-periodic seam and to non-fluid cells stay in the residual; non-fluid
 // cells have delta = 0.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi,
                                                 const T* __restrict__ b, T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
@@ -128,7 +151,7 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
       const size_t c = cidx(d, i, j, k);
       const T cp = __ldg(A.coef + c);
       if (cp != T(0)) {
-        const T ax = xi ? stencil<T, T, T>(d, A.coef, A.mask, xi, i, j, k) : T(0);
+        const T ax = xi ? stencil<MASK, T, T, T>(d, A.coef, xi, i, j, k) : T(0);
         r = __ldg(b + c) - ax;
         a = (j > 1) ? __ldg(A.coef + (size_t)SP * N + c) : T(0);
         lc = __ldg(lf + c);
@@ -179,14 +202,17 @@ template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_smooth<MASK_ALL, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
   const int tw = smooth_tw<T>(ni, nj);
   const size_t sm = (size_t)4 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
-  k_smooth<T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw); ++g_launches;
+  if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  else k_smooth<MASK_ALL, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 
@@ -226,7 +252,7 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // coarse interior cell: bc = 0.125 * sum over the 8 children of
 // (b - A x) * max(0, 1 - nvert_f), 0 on solid coarse cells; xc = 0.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                         const double* __restrict__ nvf, Dims c, const double* __restrict__ nvc,
                                                         int si, int sj, int sk, T* __restrict__ bc, T* __restrict__ xc) {
@@ -247,7 +273,7 @@ __global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __
         const double w = fmax(0., 1. - nvf[fc]);
         T r = T(0);
         if (w != 0.) {
-          T ax = x ? stencil<T, T, T>(A.d, A.coef, A.mask, x, fi, fj, fk) : T(0);
+          T ax = x ? stencil<MASK, T, T, T>(A.d, A.coef, x, fi, fj, fk) : T(0);
           r = (b[fc] - ax) * (T)w;
         }
         acc += r;
@@ -259,10 +285,69 @@ __global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __
   }
 }
 
+// Full-coarsening fast path: a block owns a coarse tile of 32 x 4 x 1 cells,
+// i.e. the fine tile 64 x 8 x 2.  Its 256 threads compute the 1024 fine
+// residuals (four each, coalesced over fine i), weight them by
+// max(0, 1 - nvert_f) into shared memory, and 128 threads sum the 2 x 2 x 2
+// children of each coarse cell in the reference's order.
+template <unsigned MASK, typename T>
+__global__ void __launch_bounds__(256) k_resrestrict_tiled(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+                                                           const double* __restrict__ nvf, Dims c,
+                                                           const double* __restrict__ nvc, T* __restrict__ bc,
+                                                           T* __restrict__ xc) {
+  if (skipped(A.skip)) return;
+  __shared__ T sr[2][8][64];
+  const Dims f = A.d;
+  const int ci0 = 1 + blockIdx.x * 32, cj0 = 1 + blockIdx.y * 4, ck = 1 + blockIdx.z;
+  const int fi0 = 2 * ci0 - 1, fj0 = 2 * cj0 - 1, fk0 = 2 * ck - 1;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int ii = tx + 32 * (q & 1), kk = q >> 1;
+    const int fi = fi0 + ii, fj = fj0 + ty, fk = fk0 + kk;
+    T r = T(0);
+    if (fi <= f.mx - 2 && fj <= f.my - 2) {
+      const size_t fc = cidx(f, fi, fj, fk);
+      const double w = fmax(0., 1. - nvf[fc]);
+      if (w != 0.) {
+        const T ax = x ? stencil<MASK, T, T, T>(f, A.coef, x, fi, fj, fk) : T(0);
+        r = (b[fc] - ax) * (T)w;
+      }
+    }
+    sr[kk][ty][ii] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < 128) {
+    const int cx = threadIdx.x & 31, cy = threadIdx.x >> 5;
+    const int ci = ci0 + cx, cj = cj0 + cy;
+    if (ci <= c.mx - 2 && cj <= c.my - 2) {
+      const size_t q = cidx(c, ci, cj, ck);
+      T acc = T(0);
+      if (!(nvc[q] > 0.1)) {
+        // children (ih, jh, kh) - {0, 1} in MyRestriction's order
+        const int ih = 2 * cx + 1, jh = 2 * cy + 1;
+        acc = (sr[1][jh][ih] + sr[1][jh][ih - 1] + sr[1][jh - 1][ih] + sr[0][jh][ih] + sr[1][jh - 1][ih - 1] +
+               sr[0][jh - 1][ih] + sr[0][jh][ih - 1] + sr[0][jh - 1][ih - 1]) * T(0.125);
+      }
+      bc[q] = acc;
+      xc[q] = T(0);
+    }
+  }
+}
+
 template <typename T>
 int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
                              const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
-  k_resrestrict<T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc); ++g_launches;
+  const bool ch = fits_ch(A.mask);
+  if (!si && !sj && !sk) {
+    dim3 g((c.mx - 2 + 31) / 32, (c.my - 2 + 3) / 4, c.mz - 2);
+    if (ch) k_resrestrict_tiled<MASK_CH, T><<<g, 256, 0, s>>>(A, x, b, nvf, c, nvc, bc, xc);
+    else k_resrestrict_tiled<MASK_ALL, T><<<g, 256, 0, s>>>(A, x, b, nvf, c, nvc, bc, xc);
+  } else {
+    if (ch) k_resrestrict<MASK_CH, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc);
+    else k_resrestrict<MASK_ALL, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc);
+  }
+  ++g_launches;
   return (int)cudaGetLastError();
 }
 

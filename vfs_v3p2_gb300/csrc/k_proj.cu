@@ -18,10 +18,13 @@ constexpr int RB = 256;  // reduction block size
 #define GRID_LOOP(d)                                                                          \
   for (size_t _t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; _t < ncell(d);              \
        _t += (size_t)gridDim.x * blockDim.x)
-#define DECOMP(d, i, j, k)               \
-  int i = (int)(_t % (d).mx);            \
-  int j = (int)((_t / (d).mx) % (d).my); \
-  int k = (int)(_t / ((size_t)(d).mx * (d).my))
+// 32-bit index split (grids stay below 2^31 cells)
+#define DECOMP(d, i, j, k)                          \
+  const unsigned _u = (unsigned)_t;                 \
+  const unsigned _q = _u / (unsigned)(d).mx;        \
+  int i = (int)(_u - _q * (unsigned)(d).mx);        \
+  int k = (int)(_q / (unsigned)(d).my);             \
+  int j = (int)(_q - (unsigned)k * (unsigned)(d).my)
 
 static inline int nblk(size_t n, int bs = 256) {
   size_t b = (n + bs - 1) / bs;
@@ -289,7 +292,11 @@ int launch_update_pressure(const Dims& d, const double* nvert, const double* phi
 // kcsi.kzet, keta.kzet, kzet.kzet) and M the face Jacobians iaj, jaj, kaj,
 // multiplied in the reference's order: (dpdc * dot) * iaj.
 // ---------------------------------------------------------------------------
-__global__ void k_projection(Dims d, const double* __restrict__ pd, const double* __restrict__ iaj,
+// x / coeff is skipped when coeff == 1 (x / 1.0 == x exactly); r1 = r2 = r3
+// = 1 (no level set), so their divisions are always exact and omitted.
+__device__ __forceinline__ double div_c(double x, double coeff) { return coeff == 1.0 ? x : x / coeff; }
+
+__global__ void __launch_bounds__(128) k_projection(Dims d, const double* __restrict__ pd, const double* __restrict__ iaj,
                              const double* __restrict__ jaj, const double* __restrict__ kaj, const double* __restrict__ nvert,
                              const double* __restrict__ phi, double dt, double st, double coeff, Ucont u) {
   const size_t N = ncell(d);
@@ -300,7 +307,6 @@ __global__ void k_projection(Dims d, const double* __restrict__ pd, const double
     const size_t c = _t;
 #define NV(ii, jj, kk) nvert[cidx(d, ii, jj, kk)]
 #define PH(ii, jj, kk) phi[cidx(d, ii, jj, kk)]
-    const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
     double dpdc, dpde, dpdz;
     if (j > 0 && j < my - 1 && k > 0 && k < mz - 1)
       if ((i > 0 && i < mx - 2) || (ip && i == mx - 2)) {
@@ -328,7 +334,7 @@ __global__ void k_projection(Dims d, const double* __restrict__ pd, const double
         }
         if ((NV(i, j, k) + NV(i + 1, j, k)) < THR) {
           const double a = iaj[c];
-          u.x[c] -= (dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt * st / coeff / r1;
+          u.x[c] -= div_c((dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt * st, coeff);
         }
       }
     if (i > 0 && i < mx - 1 && k > 0 && k < mz - 1)
@@ -357,7 +363,7 @@ __global__ void k_projection(Dims d, const double* __restrict__ pd, const double
         }
         if ((NV(i, j, k) + NV(i, j + 1, k)) < THR) {
           const double a = jaj[c];
-          u.y[c] -= (dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt * st / coeff / r2;
+          u.y[c] -= div_c((dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt * st, coeff);
         }
       }
     if (i > 0 && i < mx - 1 && j > 0 && j < my - 1)
@@ -386,7 +392,7 @@ __global__ void k_projection(Dims d, const double* __restrict__ pd, const double
         else dpdz = PH(i, j, k + 1) - PH(i, j, k);
         if ((NV(i, j, k) + NV(i, j, k + 1)) < THR) {
           const double a = kaj[c];
-          u.z[c] -= (dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt * st / coeff / r3;
+          u.z[c] -= div_c((dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt * st, coeff);
         }
       }
 #undef PH
@@ -497,6 +503,32 @@ int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const dou
                       cudaStream_t s) {
   const int nb = nblk(ncell(d), RB);
   k_divergence<<<nb, RB, 0, s>>>(d, u, aj, nvert, parts); ++g_launches;
+  k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// max |r| over the cells the Divergence check keeps (main.c:1279-1349: the
+// cell and its six face neighbours free of nvert): with st = 1 the projection
+// leaves div u = dt / coeff * r there for the aj-scaled residual r.
+__global__ void __launch_bounds__(RB) k_masked_absmax(Dims d, const double* __restrict__ r, const double* __restrict__ nvert,
+                                                      double* parts) {
+  __shared__ double sh[32];
+  double mxv = 0.;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k)) continue;
+    const size_t c = _t;
+    if (nvert[c] + nvert[cidx(d, i, j, k + 1)] + nvert[cidx(d, i, j, k - 1)] + nvert[cidx(d, i, j + 1, k)] +
+            nvert[cidx(d, i, j - 1, k)] + nvert[cidx(d, i + 1, j, k)] + nvert[cidx(d, i - 1, j, k)] > 0.1)
+      continue;
+    mxv = fmax(mxv, fabs(r[c]));
+  }
+  mxv = block_max(mxv, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = mxv;
+}
+int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s) {
+  const int nb = nblk(ncell(d), RB);
+  k_masked_absmax<<<nb, RB, 0, s>>>(d, r, nvert, parts); ++g_launches;
   k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -124,6 +124,7 @@ struct Grid {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
+  double nfluid = 0.;  // fluid interior cells of the finest level
   size_t bytes = 0;
   std::vector<void*> allocs;
   Ucont U() const { size_t N = ncell(d); return Ucont{u, u + N, u + 2 * N}; }
@@ -335,12 +336,13 @@ MGCfg mgcfg(const vfs_solve_params& p) {
 }
 
 // z = M^{-1} v on the finest level (v FP64, z in T), optional skip flag.
+// with_input == false: the finest-level input buffer already holds T(v).
 template <typename T>
 int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T* z, T* tmp, const int* skip,
-            cudaStream_t s) {
+            cudaStream_t s, bool with_input = true) {
   Level& F = g.lev[g.L - 1];
   T* bf = bbuf<T>(F);
-  dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s), s);
+  if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s), s);
   T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p), skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
@@ -379,7 +381,7 @@ template <>
 double* zbase<double>(Grid& g) { return g.Z64; }
 
 template <typename T>
-int fg_start(vfs_ctx* ctx, Fgmres& f) {
+int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   Grid& g = *f.g;
   const vfs_solve_params& p = *f.p;
   const size_t N = ncell(g.d);
@@ -387,7 +389,7 @@ int fg_start(vfs_ctx* ctx, Fgmres& f) {
   KrylovState h{};
   h.m = p.restart;
   h.rtol = p.rtol;
-  h.atol = p.div_tol > 0. ? p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
+  h.atol = atol;
   double* a = g.starr;
   h.H = a; a += (size_t)(p.restart + 1) * p.restart;
   h.cs = a; a += p.restart + 2;
@@ -401,7 +403,7 @@ int fg_start(vfs_ctx* ctx, Fgmres& f) {
     if (r) return r;
   }
   CK(cudaMemcpyAsync(g.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-  if (!p.warm_start) CK(cudaMemsetAsync(g.phi, 0, N * sizeof(double), s));
+  if (!warm) CK(cudaMemsetAsync(g.phi, 0, N * sizeof(double), s));
   Level& F = g.lev[g.L - 1];
   dbg("scale_rhs", 0, launch_scale_in<double>(F.d, F.M + F.N * MP_AJ, g.b, g.bs, nullptr, s), s);
   dbg("bnorm", 0, launch_norm_init(g.st, g.bs, N, g.parts, 1, s), s);
@@ -428,7 +430,9 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
   T* zj = Z + (size_t)f.j * N;
   double* vj = g.V + (size_t)f.j * N;
   Level& F = g.lev[g.L - 1];
-  int r = precond<T>(ctx, g, p, vj, zj, xbuf<T>(F)[1], skip, s);
+  // the input T(v_j) of the preconditioner was written by the previous
+  // iteration's basis update, except at the start of a cycle
+  int r = precond<T>(ctx, g, p, vj, zj, xbuf<T>(F)[1], skip, s, f.j == 0);
   if (r) return r;
   {
     const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
@@ -437,12 +441,18 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
     if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + sizeof(T) + 8.0));
   }
   dbg("apply64", g.L - 1, 0, s);
-  dbg("multidot1", 0, launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s), s);
-  dbg("gs_update1", 0, launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 1, s), s);
-  dbg("multidot2", 0, launch_multidot(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s), s);
-  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, f.j + 1, g.w, N, g.parts, 2, s), s);
+  const int nv = f.j + 1;
+  // CGS2: dots, fused (update + second dots), (update + norm)
+  dbg("multidot1", 0, launch_multidot(g.st, g.V, nv, g.w, N, g.parts, 1, s), s);
+  int fr = launch_gs_update_dots(g.st, g.V, nv, g.w, N, g.parts, s);
+  if (fr == -1) {
+    launch_gs_update(g.st, g.V, nv, g.w, N, g.parts, 1, s);
+    launch_multidot(g.st, g.V, nv, g.w, N, g.parts, 2, s);
+  }
+  dbg("gs_update_dots", 0, fr == -1 ? 0 : fr, s);
+  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, nv, g.w, N, g.parts, 2, s), s);
   dbg("arnoldi", 0, launch_arnoldi_finish(g.st, nb, g.parts, s), s);
-  dbg("vnext", 0, launch_vnext(g.st, g.w, g.V + (size_t)(f.j + 1) * N, N, s), s);
+  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, g.V + (size_t)(f.j + 1) * N, bbuf<T>(F), N, s), s);
   f.it++;
   f.j++;
   launch_status_copy(g.st, &g.hstat[f.it & 1], s);
@@ -467,33 +477,95 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
   return VFS_OK;
 }
 
-// Close a solve: true residual, null-space removal, phi finish, info.
-int fg_finish(vfs_ctx* ctx, Fgmres& f, vfs_solve_info* info) {
+// True aj-scaled residual of the current phi: ||r|| into scal[16] and the
+// masked max |r| (the divergence the projection will leave, times coeff/dt)
+// into scal[17].  Reads back the Krylov state.
+int fg_check(vfs_ctx* ctx, Fgmres& f, KrylovState* h, double* rn, double* rmax) {
   Grid& g = *f.g;
   const size_t N = ncell(g.d);
   cudaStream_t s = g.s;
   Level& F = g.lev[g.L - 1];
   dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
   dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
+  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s), s);
+  double v[2];
+  CK(cudaMemcpyAsync(h, g.st, sizeof(*h), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(v, g.scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *rn = v[0];
+  *rmax = v[1];
+  if (!(h->bnorm == h->bnorm) || !(h->resid == h->resid) || !(v[0] == v[0])) return fail(ctx, VFS_ERR_NUMERIC, "NaN in the solve");
+  return VFS_OK;
+}
+
+// Close a solve: null-space removal, phi finish, info.
+int fg_close(vfs_ctx* ctx, Fgmres& f, const KrylovState& h, double rn, bool conv, int iters, vfs_solve_info* info) {
+  Grid& g = *f.g;
+  cudaStream_t s = g.s;
+  Level& F = g.lev[g.L - 1];
   dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s), s);
   dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
   CK(cudaEventRecord(g.t1, s));
-  KrylovState h{};
-  double rn = 0.;
-  CK(cudaMemcpyAsync(&h, g.st, sizeof(h), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&rn, g.scal + 16, sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  CK(cudaEventSynchronize(g.t1));
   if (info) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, g.t0, g.t1);
-    info->iterations = h.it;
-    info->converged = (h.done && h.resid <= h.rtol * h.bnorm && (h.atol <= 0. || h.resid <= h.atol)) || h.bnorm == 0.;
+    info->iterations = iters;
+    info->converged = conv;
     info->bnorm = h.bnorm;
     info->relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
     info->time_ms = ms;
   }
-  if (!(h.bnorm == h.bnorm) || !(h.resid == h.resid) || !(rn == rn)) return fail(ctx, VFS_ERR_NUMERIC, "NaN in the solve");
   return VFS_OK;
+}
+
+// One FGMRES run until its device flag or maxit; returns iterations used.
+template <typename T>
+int fg_run(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
+  int r = fg_start<T>(ctx, f, atol, warm);
+  if (r) return r;
+  while (!f.finished) {
+    r = fg_step<T>(ctx, f);
+    if (r) return r;
+  }
+  return VFS_OK;
+}
+
+double initial_atol(const Grid& g, const vfs_solve_params& p) {
+  if (p.div_tol <= 0.) return 0.;
+  const double rmax_tol = p.div_tol * g.coeff / (g.dt * g.st_);
+  // max |r| is typically 1/20 .. 1/200 of ||r||_2 / sqrt(n); start optimistic
+  return rmax_tol * std::sqrt(std::max(g.nfluid, 1.)) * 0.05;
+}
+
+// After a first FGMRES run (f finished): check the true residual; with
+// div_tol > 0 check the exact masked max |r| (the divergence the projection
+// leaves, dt st / coeff per unit) and, while it is above div_tol, continue
+// from the current phi with a tighter L2 target.  The returned phi leaves
+// max |div u| <= div_tol.
+template <typename T>
+int solve_finish_rounds(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, Fgmres& f, double atol, vfs_solve_info* info) {
+  const double rmax_tol = p.div_tol > 0. ? p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
+  int iters = 0;
+  KrylovState h{};
+  double rn = 0., rmax = 0.;
+  vfs_solve_params pr = p;
+  for (int round = 0;; round++) {
+    int r = fg_check(ctx, f, &h, &rn, &rmax);
+    if (r) return r;
+    iters += h.it;
+    const bool rel_ok = rn <= p.rtol * h.bnorm * 1.0000001 || h.bnorm == 0.;
+    const bool div_ok = p.div_tol <= 0. || rmax <= rmax_tol;
+    if ((rel_ok && div_ok) || iters >= p.maxit || h.bnorm == 0. || round == 7) {
+      f.p = &p;
+      return fg_close(ctx, f, h, rn, rel_ok && div_ok, iters, info);
+    }
+    atol = std::min(atol > 0. ? atol : rn, rn) * (div_ok ? 1. : 0.5 * rmax_tol / rmax);
+    pr.maxit = p.maxit - iters;
+    f.p = &pr;
+    r = fg_run<T>(ctx, f, atol, true);
+    if (r) return r;
+  }
 }
 
 template <typename T>
@@ -503,14 +575,11 @@ int solve_one(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, vfs_solve_info* 
   r = ensure_krylov(ctx, g, p.restart, sizeof(T) == 4 ? VFS_MIXED : VFS_FP64);
   if (r) return r;
   CK(cudaEventRecord(g.t0, g.s));
+  const double atol = initial_atol(g, p);
   Fgmres f{&g, &p};
-  r = fg_start<T>(ctx, f);
+  r = fg_run<T>(ctx, f, atol, p.warm_start != 0);
   if (r) return r;
-  while (!f.finished) {
-    r = fg_step<T>(ctx, f);
-    if (r) return r;
-  }
-  return fg_finish(ctx, f, info);
+  return solve_finish_rounds<T>(ctx, g, p, f, atol, info);
 }
 
 int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
@@ -694,6 +763,10 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   GAB(g.aos, 3 * N);
   GAB(g.parts, (size_t)krylov_nblocks(N) * 72 + 4096);
   GAB(g.scal, 64);
+  for (int k = 1; k < d.mz - 1; k++)
+    for (int j = 1; j < d.my - 1; j++)
+      for (int i = 1; i < d.mx - 1; i++)
+        if (desc->nvert[cidx(d, i, j, k)] < 0.1) g.nfluid += 1.;
   Level& F = g.lev[L - 1];
   if (cudaMemcpyAsync(F.coor, desc->coor, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess ||
       cudaMemcpyAsync(F.nvert, desc->nvert, N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess)
@@ -1007,7 +1080,8 @@ int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, 
     CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
     step_pre(g, dt, st, coeff);
     fs[q] = Fgmres{&g, p};
-    r = mixed ? fg_start<float>(ctx, fs[q]) : fg_start<double>(ctx, fs[q]);
+    const double atol = initial_atol(g, *p);
+    r = mixed ? fg_start<float>(ctx, fs[q], atol, p->warm_start != 0) : fg_start<double>(ctx, fs[q], atol, p->warm_start != 0);
     if (r) return r;
   }
   // interleave the iterations of all grids, each on its own stream
@@ -1024,7 +1098,9 @@ int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, 
   int rc = VFS_OK;
   for (int q = 0; q < n; q++) {
     vfs_solve_info tmp{};
-    r = fg_finish(ctx, fs[q], infos ? &infos[q] : &tmp);
+    const double atol = initial_atol(*gs[q], *p);
+    r = mixed ? solve_finish_rounds<float>(ctx, *gs[q], *p, fs[q], atol, infos ? &infos[q] : &tmp)
+              : solve_finish_rounds<double>(ctx, *gs[q], *p, fs[q], atol, infos ? &infos[q] : &tmp);
     if (r) return r;
     step_post(*gs[q], dt, st, coeff);
   }

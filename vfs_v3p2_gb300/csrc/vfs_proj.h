@@ -28,6 +28,7 @@ int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s)
 int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const double* phi, double dt,
                       double st, double coeff, const Ucont& u, cudaStream_t s);
 int launch_contra2cart(const Dims& d, const double* M, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
+int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s);
 int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
                       cudaStream_t s);
 
@@ -59,6 +60,10 @@ int launch_vec_scale_first(KrylovState* st, const double* r, double* v0, size_t 
 int launch_multidot(KrylovState* st, const double* V, int nv, const double* w, size_t n, double* parts, int pass,
                     cudaStream_t s);
 int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, int pass, cudaStream_t s);
+// second CGS pass fused with the first update (nv <= 32); returns -1 if nv is too large
+int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s);
+template <typename T>
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s);
 int launch_arnoldi_finish(KrylovState* st, int nparts, const double* parts, cudaStream_t s);
 int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStream_t s);
 int launch_lsq_update(KrylovState* st, cudaStream_t s);
