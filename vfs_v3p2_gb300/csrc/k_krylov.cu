@@ -90,9 +90,13 @@ int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStr
 
 // Multi-dot partials: parts[b * ld + q] = sum over the block's cells of V_q . w
 // for q < nv, chunks of 4 columns per sweep (w is re-read from L2).
+// nv < 0: use the device's current column count st->j + 1 (graph-replayable).
+__device__ __forceinline__ int nv_of(const KrylovState* st, int nv) { return nv < 0 ? st->j + 1 : nv; }
+
 __global__ void __launch_bounds__(KB) k_multidot(const KrylovState* st, const double* __restrict__ V, int nv,
                                                  const double* __restrict__ w, size_t n, double* parts, int ld) {
   if (is_done(st)) return;
+  nv = nv_of(st, nv);
   __shared__ double sh[32];
   for (int q0 = 0; q0 < nv; q0 += 4) {
     double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
@@ -120,6 +124,7 @@ __global__ void __launch_bounds__(KB) k_multidot(const KrylovState* st, const do
 // Sum the multi-dot partials into st->h (and accumulate the column in hacc).
 __global__ void k_multidot_finish(KrylovState* st, const double* __restrict__ parts, int nparts, int nv, int ld, int pass) {
   if (is_done(st)) return;
+  nv = nv_of(st, nv);
   __shared__ double sh[32];
   for (int q = 0; q < nv; q++) {
     double s = 0.;
@@ -146,6 +151,7 @@ int launch_multidot(KrylovState* st, const double* V, int nv, const double* w, s
 __global__ void __launch_bounds__(KB) k_gs_update(const KrylovState* st, const double* __restrict__ V, int nv,
                                                   double* __restrict__ w, size_t n, double* parts) {
   if (is_done(st)) return;
+  nv = nv_of(st, nv);
   __shared__ double sh[32];
   __shared__ double hs[72];
   for (int q = threadIdx.x; q < nv; q += blockDim.x) hs[q] = st->h[q];
@@ -169,11 +175,16 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
 
 // Fused CGS2 middle pass: w <- w - V h (h from the first pass), and the
 // second pass's dots V_q . w computed on the updated element while the basis
-// values are still in registers.  NV = compile-time capacity (>= nv).
-template <int NV>
+// values are still in registers.  NV = compile-time capacity; the kernel does
+// its work only when NV0 < nv <= NV, so a fixed sequence of launches with
+// increasing capacities serves every column count (graph-replayable) while
+// the FP64 FMAs issued stay within 4 of 2 nv per element.
+template <int NV0, int NV>
 __global__ void __launch_bounds__(KB) k_gs_update_dots(const KrylovState* st, const double* __restrict__ V, int nv,
                                                        double* __restrict__ w, size_t n, double* parts, int ld) {
   if (is_done(st)) return;
+  nv = nv_of(st, nv);
+  if (nv <= NV0 || nv > NV) return;
   __shared__ double hs[NV];
   __shared__ double red[KB / 32][NV];
   for (int q = threadIdx.x; q < NV; q += blockDim.x) hs[q] = q < nv ? st->h[q] : 0.;
@@ -207,14 +218,19 @@ __global__ void __launch_bounds__(KB) k_gs_update_dots(const KrylovState* st, co
   }
 }
 
-int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s) {
+// nv < 0: device column count, capacity chosen from cap (>= the largest nv).
+int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s,
+                          int cap) {
   const int nb = krylov_nblocks(n);
   const int ld = 72;
-  if (nv <= 8) k_gs_update_dots<8><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
-  else if (nv <= 16) k_gs_update_dots<16><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
-  else if (nv <= 32) k_gs_update_dots<32><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld);
-  else return -1;
-  ++g_launches;
+  if (nv > 32 || (nv < 0 && cap > 32)) return -1;
+  // nv >= 0: the one bucket holding nv; nv < 0: every bucket up to cap
+  const int lo = nv < 0 ? 0 : nv, hi = nv < 0 ? cap : nv;
+  if (lo <= 4) { k_gs_update_dots<0, 4><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches; }
+  if (lo <= 8 && hi > 4) { k_gs_update_dots<4, 8><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches; }
+  if (lo <= 16 && hi > 8) { k_gs_update_dots<8, 16><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches; }
+  if (lo <= 24 && hi > 16) { k_gs_update_dots<16, 24><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches; }
+  if (hi > 24) { k_gs_update_dots<24, 32><<<nb, KB, 0, s>>>(st, V, nv, w, n, parts, ld); ++g_launches; }
   k_multidot_finish<<<1, KB, 0, s>>>(st, parts, nb, nv, ld, 2); ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -321,11 +337,13 @@ int launch_norm2(const double* v, size_t n, double* parts, double* out, cudaStre
 
 // Next basis vector and multigrid input in one sweep: V_{j+1} = w / h_{j+1,j}
 // and out = T(V_{j+1}) over the interior; ghost entries of w are zero.
+// vn == nullptr: the target is V + st->j * n (the column just opened).
 template <typename T>
-__global__ void __launch_bounds__(KB) k_vnext_in(const KrylovState* st, const double* __restrict__ w, double* __restrict__ vn,
-                                                  T* __restrict__ out, size_t n) {
+__global__ void __launch_bounds__(KB) k_vnext_in(const KrylovState* st, const double* __restrict__ w, double* vn,
+                                                  T* __restrict__ out, size_t n, double* V) {
   if (is_done(st)) return;
   const double f = st->inv_hn;
+  if (!vn) vn = V + (size_t)st->j * n;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const double v = w[t] * f;
     vn[t] = v;
@@ -333,12 +351,12 @@ __global__ void __launch_bounds__(KB) k_vnext_in(const KrylovState* st, const do
   }
 }
 template <typename T>
-int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s) {
-  k_vnext_in<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, out, n); ++g_launches;
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V) {
+  k_vnext_in<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, out, n, V); ++g_launches;
   return (int)cudaGetLastError();
 }
-template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t);
-template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t);
+template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t, double*);
+template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t, double*);
 
 int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s) {
   return (int)cudaMemcpyAsync(hst, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s);

@@ -12,6 +12,7 @@
 // no i-j or j-k cross terms streams 11 coefficient arrays instead of 19.
 #include "vfs_common.cuh"
 #include "vfs_kernels.h"
+#include "vfs_proj.h"
 
 namespace vfs {
 
@@ -41,22 +42,25 @@ constexpr unsigned MASK_CH = (1u << CP) | (1u << EP) | (1u << WP) | (1u << NP) |
                              (1u << TE) | (1u << BE) | (1u << TW) | (1u << BW);
 
 // sum_m coef[m] * x[nbr(m)] over the slots of MASK for interior cell (i, j, k).
+// Addresses are one 32-bit base plus three per-axis offsets with the periodic
+// wrap folded in (i - 1 of i = 1 is mx - 2, i + 1 of i = mx - 2 is 1); grids
+// stay below 2^31 cells, so 19 * N fits as well.
 template <unsigned MASK, typename TC, typename TX_, typename TA>
 __device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x, int i, int j,
                                       int k) {
-  const size_t N = ncell(d);
-  const size_t c = cidx(d, i, j, k);
-  const int im = wrapi(i - 1, d.mx, d.ip), ip1 = wrapi(i + 1, d.mx, d.ip);
-  const int jm = wrapi(j - 1, d.my, d.jp), jp1 = wrapi(j + 1, d.my, d.jp);
-  const int km = wrapi(k - 1, d.mz, d.kp), kp1 = wrapi(k + 1, d.mz, d.kp);
-  const int II[3] = {im, i, ip1}, JJ[3] = {jm, j, jp1}, KK[3] = {km, k, kp1};
+  const int sy = d.mx, sz = d.mx * d.my;
+  const int N = sz * d.mz;
+  const int c = k * sz + j * sy + i;
+  const int oi[3] = {(i == 1 && d.ip) ? d.mx - 3 : -1, 0, (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1};
+  const int oj[3] = {((j == 1 && d.jp) ? d.my - 3 : -1) * sy, 0, ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy};
+  const int ok[3] = {((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, 0, ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz};
   TC cv[19];
   TX_ xv[19];
 #pragma unroll
   for (int m = 0; m < 19; m++) {
     if (MASK & (1u << m)) {
-      cv[m] = __ldg(coef + (size_t)m * N + c);
-      xv[m] = __ldg(x + cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]));
+      cv[m] = __ldg(coef + (m * N + c));
+      xv[m] = __ldg(x + (c + oi[slot_di(m) + 1] + oj[slot_dj(m) + 1] + ok[slot_dk(m) + 1]));
     }
   }
   TA s = TA(0);
@@ -96,6 +100,31 @@ int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, 
   return (int)cudaGetLastError();
 }
 
+// Outer operator inside the Krylov iteration: w = A z for the
+// preconditioned direction z (multigrid precision) and the copy of z into its
+// Krylov slot Z[st->j]; z[c] is loaded for the stencil's centre anyway.
+template <unsigned MASK, typename T>
+__global__ void __launch_bounds__(TX* TY) k_apply64_krylov(OpView<double> A, const T* __restrict__ z, T* __restrict__ Z,
+                                                           const KrylovState* st, double* __restrict__ w) {
+  if (skipped(A.skip)) return;
+  T* zj = Z + (size_t)st->j * ncell(A.d);
+  TILE_LOOP(A.d) {
+    if (!_in) continue;
+    const size_t c = cidx(A.d, i, j, k);
+    w[c] = stencil<MASK, double, T, double>(A.d, A.coef, z, i, j, k);
+    zj[c] = z[c];
+  }
+}
+template <typename T>
+int launch_apply64_krylov(const OpView<double>& A, const T* z, T* Z, const KrylovState* st, double* w, cudaStream_t s) {
+  if (fits_ch(A.mask)) k_apply64_krylov<MASK_CH, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, z, Z, st, w);
+  else k_apply64_krylov<MASK_ALL, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, z, Z, st, w);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+template int launch_apply64_krylov<float>(const OpView<double>&, const float*, float*, const KrylovState*, double*, cudaStream_t);
+template int launch_apply64_krylov<double>(const OpView<double>&, const double*, double*, const KrylovState*, double*, cudaStream_t);
+
 template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(TX* TY) k_apply_mg(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                      T* __restrict__ y) {
@@ -134,49 +163,46 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
   extern __shared__ unsigned char smraw[];
   const Dims d = A.d;
   const int nj = d.my - 2;
-  T* sr = (T*)smraw;
-  T* sa = sr + TW * nj;
-  T* sl = sa + TW * nj;  // c'_j
-  T* si = sl + TW * nj;  // 1 / m_j
+  T* su = (T*)smraw;     // r_j / m_j, then y_j, then delta_j
+  T* sp = su + TW * nj;  // a_j / m_j
+  T* sl = sp + TW * nj;  // c'_j
   const size_t N = ncell(d);
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
-#pragma unroll 2
   for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
     const int il = idx % TW, jl = idx / TW;
     const int i = i0 + il, j = 1 + jl;
-    T r = T(0), a = T(0), lc = T(0), li = T(1);
+    T u = T(0), pp = T(0), lc = T(0);
     if (i <= d.mx - 2) {
       const size_t c = cidx(d, i, j, k);
-      const T cp = __ldg(A.coef + c);
-      if (cp != T(0)) {
+      if (__ldg(A.coef + c) != T(0)) {
         const T ax = xi ? stencil<MASK, T, T, T>(d, A.coef, xi, i, j, k) : T(0);
-        r = __ldg(b + c) - ax;
-        a = (j > 1) ? __ldg(A.coef + (size_t)SP * N + c) : T(0);
+        u = (__ldg(b + c) - ax) * __ldg(lf + N + c);
+        pp = __ldg(lf + 2 * N + c);
         lc = __ldg(lf + c);
-        li = __ldg(lf + N + c);
       }
     }
-    sr[idx] = r;
-    sa[idx] = a;
+    su[idx] = u;
+    sp[idx] = pp;
     sl[idx] = lc;
-    si[idx] = li;
   }
   __syncthreads();
   if (threadIdx.x < TW) {
     const int il = threadIdx.x;
-    T dprev = T(0);
+    T y = T(0);
+#pragma unroll 8
     for (int jl = 0; jl < nj; jl++) {
       const int q = jl * TW + il;
-      dprev = (sr[q] - sa[q] * dprev) * si[q];
-      sr[q] = dprev;
+      y = fma(-sp[q], y, su[q]);
+      su[q] = y;
     }
     T xn = T(0);
+#pragma unroll 8
     for (int jl = nj - 1; jl >= 0; jl--) {
       const int q = jl * TW + il;
-      xn = sr[q] - sl[q] * xn;
-      sr[q] = xn;
+      xn = fma(-sl[q], xn, su[q]);
+      su[q] = xn;
     }
   }
   __syncthreads();
@@ -186,14 +212,14 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
     if (i > d.mx - 2) continue;
     const size_t c = cidx(d, i, j, k);
     const T x0 = xi ? xi[c] : T(0);
-    xo[c] = x0 + omega * sr[idx];
+    xo[c] = x0 + omega * su[idx];
   }
 }
 
 template <typename T>
 static int smooth_tw(int ni, int nj) {
-  int tw = 16;
-  while (tw > 4 && (size_t)4 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
+  int tw = 32;
+  while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   return tw;
 }
@@ -208,7 +234,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
   const int tw = smooth_tw<T>(ni, nj);
-  const size_t sm = (size_t)4 * tw * nj * sizeof(T);
+  const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
   if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
   else k_smooth<MASK_ALL, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
@@ -217,8 +243,11 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
 }
 
 // Thomas factors of the y-line tridiagonal (SP, CP, NP) of every column, in
-// FP64 from the aj-scaled FP64 operator: lf[c] = c'_j, lf[N + c] = 1/m_j, as
-// T.  Non-fluid cells are identity rows; j-periodic seam couplings stay off.
+// FP64 from the aj-scaled FP64 operator, stored as T: lf[c] = c'_j,
+// lf[N + c] = 1/m_j, lf[2N + c] = a_j/m_j (a_j the SP coupling), so that the
+// forward substitution is y_j = r_j/m_j - (a_j/m_j) y_{j-1} and the backward
+// one delta_j = y_j - c'_j delta_{j+1}.  Non-fluid cells are identity rows;
+// j-periodic seam couplings stay off the line.
 template <typename T>
 __global__ void k_line_factors(Dims d, const double* __restrict__ mcoef, T* __restrict__ lf) {
   const size_t N = ncell(d);
@@ -237,6 +266,7 @@ __global__ void k_line_factors(Dims d, const double* __restrict__ mcoef, T* __re
       cprev = cc * inv;
       lf[c] = (T)cprev;
       lf[N + c] = (T)inv;
+      lf[2 * N + c] = (T)(a * inv);
     }
   }
 }

@@ -62,6 +62,8 @@ const bool g_debug = [] {
 int g_debug_err = 0;
 void dbg(const char* stage, int level, int rc, cudaStream_t s) {
   if (!g_debug || g_debug_err) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return;
   cudaError_t e = rc ? (cudaError_t)rc : cudaStreamSynchronize(s);
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -83,7 +85,7 @@ struct Level {
   double* coef = nullptr;
   double* mcoef = nullptr;
   float* mcoef32 = nullptr;
-  float* lf32 = nullptr;   // y-line Thomas factors [c' | 1/m]
+  float* lf32 = nullptr;   // y-line Thomas factors [c' | 1/m | a/m]
   double* lf64 = nullptr;
   unsigned mask = 0;
   uint8_t* pcode = nullptr;
@@ -124,6 +126,10 @@ struct Grid {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
+  cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1;
+  unsigned long long ig_kernels = 0;  // kernels per replay
+  double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
   size_t bytes = 0;
   std::vector<void*> allocs;
@@ -189,6 +195,7 @@ void grid_free(vfs_ctx* ctx, Grid* g) {
   if (g->s) cudaStreamSynchronize(g->s);
   for (void* p : g->allocs) cudaFree(p);
   if (ctx) ctx->used -= std::min(ctx->used, g->bytes);
+  if (g->ig_exec) cudaGraphExecDestroy(g->ig_exec);
   if (g->hstat) cudaFreeHost(g->hstat);
   for (auto& e : g->ev) if (e) cudaEventDestroy(e);
   if (g->t0) cudaEventDestroy(g->t0);
@@ -276,29 +283,39 @@ template <typename T>
 void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
   int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s);
-  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 3));
+  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 6));
   dbg("smooth", l, rc, s);
+}
+
+// Number of buffer writes of a level's schedule (smoothing sweeps, plus the
+// prolongation when no pre-sweep wrote first): the result lands in
+// bufs[(writes - 1) & 1], so the caller's first buffer is swapped in when
+// needed to make the V-cycle's result always land in xa.
+int level_writes(const Grid& g, int l, const MGCfg& c) {
+  if (l == 0) return g.lev[0].Binv ? 1 : c.ncoarse;
+  return c.nu1 + (c.nu1 == 0 ? 1 : 0) + c.nu2;
 }
 
 template <typename T>
 T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, cudaStream_t s) {
   Level& L = g.lev[l];
   OpView<T> A = mgview<T>(L, skip);
+  const int W = level_writes(g, l, c);
+  T* bufs[2] = {xa, xb};
+  if (((W - 1) & 1) == 1) std::swap(bufs[0], bufs[1]);
   if (l == 0) {
     if (binv<T>(L)) {
-      dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, xa, skip, s), s);
-      return xa;
+      dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, bufs[0], skip, s), s);
+      return bufs[0];
     }
     T* cur = nullptr;
-    T* bufs[2] = {xa, xb};
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
       launch_smooth<T>(A, lf_of<T>(L), cur, b, o, (T)c.omega_c, s);
       cur = o;
     }
-    return cur ? cur : xa;
+    return cur;
   }
-  T* bufs[2] = {xa, xb};
   int q = 0;
   T* cur = nullptr;
   for (; q < c.nu1; q++) {
@@ -380,6 +397,15 @@ float* zbase<float>(Grid& g) { return g.Z32; }
 template <>
 double* zbase<double>(Grid& g) { return g.Z64; }
 
+// Opening of a cycle: v0 = r / beta and the preconditioner input T(v0).
+template <typename T>
+void fg_open_cycle(Grid& g, cudaStream_t s) {
+  const size_t N = ncell(g.d);
+  Level& F = g.lev[g.L - 1];
+  dbg("v0", 0, launch_vec_scale_first(g.st, g.V, g.V, N, s), s);
+  dbg("scale_in", 0, launch_scale_in<T>(F.d, nullptr, g.V, bbuf<T>(F), &g.st->done, s), s);
+}
+
 template <typename T>
 int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   Grid& g = *f.g;
@@ -409,72 +435,131 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   dbg("bnorm", 0, launch_norm_init(g.st, g.bs, N, g.parts, 1, s), s);
   dbg("residual0", 0, apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s), s);
   dbg("beta", 0, launch_norm_init(g.st, g.V, N, g.parts, 0, s), s);
-  dbg("v0", 0, launch_vec_scale_first(g.st, g.V, g.V, N, s), s);
+  fg_open_cycle<T>(g, s);
+  g.hstat[0] = 0;
   f.it = 0;
   f.j = 0;
   f.observed = f.finished = false;
   return VFS_OK;
 }
 
-// Issue one Arnoldi iteration (and the cycle end / restart when due); check
-// the status of the previous iteration.  Sets f.finished when done.
+// One Arnoldi iteration as a fixed launch sequence (column index, basis
+// slots and Krylov scalars all come from the device state), so it can be
+// captured in a CUDA graph and replayed: V-cycle on T(v_j), w = A z_j with z
+// stored to Z[j], CGS2, Hessenberg/Givens update, v_{j+1} and T(v_{j+1}),
+// and a copy of the convergence flag to pinned memory (monotonic 0 -> 1).
 template <typename T>
-int fg_step(vfs_ctx* ctx, Fgmres& f) {
-  Grid& g = *f.g;
-  const vfs_solve_params& p = *f.p;
+void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const size_t N = ncell(g.d);
-  cudaStream_t s = g.s;
   const int* skip = &g.st->done;
-  const int nb = krylov_nblocks(N);
-  T* Z = zbase<T>(g);
-  T* zj = Z + (size_t)f.j * N;
-  double* vj = g.V + (size_t)f.j * N;
   Level& F = g.lev[g.L - 1];
-  // the input T(v_j) of the preconditioner was written by the previous
-  // iteration's basis update, except at the start of a cycle
-  int r = precond<T>(ctx, g, p, vj, zj, xbuf<T>(F)[1], skip, s, f.j == 0);
-  if (r) return r;
+  T* zt = xbuf<T>(F)[0];
+  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mgcfg(p), skip, s);
   {
     const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
-    dbg("precond_done", g.L - 1, 0, s);
-    apply_outer(g, zj, nullptr, g.w, skip, s);
-    if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + sizeof(T) + 8.0));
+    OpView<double> A{F.d, F.mcoef, F.mask, skip};
+    launch_apply64_krylov<T>(A, zt, zbase<T>(g), g.st, g.w, s);
+    if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + 2 * sizeof(T) + 8.0));
   }
   dbg("apply64", g.L - 1, 0, s);
-  const int nv = f.j + 1;
-  // CGS2: dots, fused (update + second dots), (update + norm)
-  dbg("multidot1", 0, launch_multidot(g.st, g.V, nv, g.w, N, g.parts, 1, s), s);
-  int fr = launch_gs_update_dots(g.st, g.V, nv, g.w, N, g.parts, s);
-  if (fr == -1) {
-    launch_gs_update(g.st, g.V, nv, g.w, N, g.parts, 1, s);
-    launch_multidot(g.st, g.V, nv, g.w, N, g.parts, 2, s);
+  dbg("multidot1", 0, launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 1, s), s);
+  if (g.m + 1 <= 32) {
+    dbg("gs_update_dots", 0, launch_gs_update_dots(g.st, g.V, -1, g.w, N, g.parts, s, g.m + 1), s);
+  } else {
+    launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 1, s);
+    launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 2, s);
   }
-  dbg("gs_update_dots", 0, fr == -1 ? 0 : fr, s);
-  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, nv, g.w, N, g.parts, 2, s), s);
-  dbg("arnoldi", 0, launch_arnoldi_finish(g.st, nb, g.parts, s), s);
-  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, g.V + (size_t)(f.j + 1) * N, bbuf<T>(F), N, s), s);
+  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 2, s), s);
+  dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
+  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, nullptr, bbuf<T>(F), N, s, g.V), s);
+  launch_status_copy(g.st, g.hstat, s);
+}
+
+bool graphs_allowed(const Grid& g) { return g_probe.kind == 0 && !g_debug && g.m + 1 <= 32; }
+
+// The per-grid iteration graph (captured on first use; re-captured when the
+// solve parameters change).
+template <typename T>
+int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphExec_t* out) {
+  const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
+  if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega) {
+    *out = g.ig_exec;
+    return VFS_OK;
+  }
+  if (g.ig_exec) {
+    cudaGraphExecDestroy(g.ig_exec);
+    g.ig_exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  const unsigned long long n0 = g_launches.load();
+  CK(cudaStreamBeginCapture(g.s, cudaStreamCaptureModeThreadLocal));
+  issue_iteration<T>(g, p, g.s);
+  CK(cudaStreamEndCapture(g.s, &graph));
+  // captured launches run on replay, not now: count them per replay instead
+  g.ig_kernels = g_launches.load() - n0;
+  g_launches -= g.ig_kernels;
+  cudaError_t e = cudaGraphInstantiate(&g.ig_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  g.ig_prec = prec;
+  g.ig_nu1 = p.nu1;
+  g.ig_nu2 = p.nu2;
+  g.ig_omega = p.omega;
+  *out = g.ig_exec;
+  return VFS_OK;
+}
+
+// Close a cycle (least squares, x update) and, unless finished, open the next
+// one from the true residual of the updated phi.
+template <typename T>
+void fg_cycle_end(Grid& g, bool last, cudaStream_t s) {
+  const size_t N = ncell(g.d);
+  dbg("lsq", 0, launch_lsq_update(g.st, s), s);
+  dbg("x_update", 0, launch_x_update<T>(g.st, zbase<T>(g), N, g.phi, s), s);
+  dbg("restart_reset", 0, launch_restart_reset(g.st, s), s);
+  if (last) return;
+  apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s);
+  launch_norm_init(g.st, g.V, N, g.parts, 0, s);
+  fg_open_cycle<T>(g, s);
+}
+
+// Host bookkeeping after an iteration was issued on stream s: pipelined status
+// check (the flag of the previous iteration) and the cycle end when due.
+template <typename T>
+int fg_after(vfs_ctx* ctx, Fgmres& f, cudaStream_t s) {
+  Grid& g = *f.g;
+  const vfs_solve_params& p = *f.p;
   f.it++;
   f.j++;
-  launch_status_copy(g.st, &g.hstat[f.it & 1], s);
   CK(cudaEventRecord(g.ev[f.it & 1], s));
   if (f.it >= 2) {
     CK(cudaEventSynchronize(g.ev[(f.it - 1) & 1]));
-    if (g.hstat[(f.it - 1) & 1]) f.observed = true;
+    if (g.hstat[0]) f.observed = true;
   }
-  if (f.observed || f.it >= p.maxit || f.j == f.p->restart) {
-    dbg("lsq", 0, launch_lsq_update(g.st, s), s);
-    dbg("x_update", 0, launch_x_update<T>(g.st, Z, N, g.phi, s), s);
-    dbg("restart_reset", 0, launch_restart_reset(g.st, s), s);
-    if (f.observed || f.it >= p.maxit) {
-      f.finished = true;
-      return VFS_OK;
-    }
-    apply_outer(g, g.phi, g.bs, g.V, skip, s);
-    launch_norm_init(g.st, g.V, N, g.parts, 0, s);
-    launch_vec_scale_first(g.st, g.V, g.V, N, s);
+  if (f.observed || f.it >= p.maxit || f.j == p.restart) {
+    const bool last = f.observed || f.it >= p.maxit;
+    fg_cycle_end<T>(g, last, s);
+    f.finished = last;
     f.j = 0;
   }
   return VFS_OK;
+}
+
+// Issue one iteration of one grid (graph replay when allowed) and do its
+// bookkeeping.  Sets f.finished when done.
+template <typename T>
+int fg_step(vfs_ctx* ctx, Fgmres& f) {
+  Grid& g = *f.g;
+  if (graphs_allowed(g)) {
+    cudaGraphExec_t ex = nullptr;
+    int r = iteration_graph<T>(ctx, g, *f.p, &ex);
+    if (r) return r;
+    CK(cudaGraphLaunch(ex, g.s));
+    g_launches += g.ig_kernels;
+  } else {
+    issue_iteration<T>(g, *f.p, g.s);
+  }
+  return fg_after<T>(ctx, f, g.s);
 }
 
 // True aj-scaled residual of the current phi: ||r|| into scal[16] and the
@@ -604,7 +689,7 @@ int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* i
 
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
-  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 2) * 8 + N * (19 + 2) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
+  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 3) * 8 + N * (19 + 3) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 3 + 3 + 3 + 3 + 3);                    // pd u ustar p phi b ucat aos
   return b;
@@ -746,8 +831,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.coef, 19 * Lv.N);
     GAB(Lv.mcoef, 19 * Lv.N);
     GAB(Lv.mcoef32, 19 * Lv.N);
-    GAB(Lv.lf32, 2 * Lv.N);
-    GAB(Lv.lf64, 2 * Lv.N);
+    GAB(Lv.lf32, 3 * Lv.N);
+    GAB(Lv.lf64, 3 * Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
   }
   const size_t N = ncell(d);

@@ -60,10 +60,16 @@ int launch_vec_scale_first(KrylovState* st, const double* r, double* v0, size_t 
 int launch_multidot(KrylovState* st, const double* V, int nv, const double* w, size_t n, double* parts, int pass,
                     cudaStream_t s);
 int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, int pass, cudaStream_t s);
-// second CGS pass fused with the first update (nv <= 32); returns -1 if nv is too large
-int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s);
+// In the Krylov kernels nv < 0 (and vn == nullptr) mean "take the column
+// count from the device state", so one iteration is a fixed launch sequence.
+// second CGS pass fused with the first update (capacity <= 32); returns -1 beyond
+int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s,
+                          int cap = 32);
 template <typename T>
-int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s);
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V = nullptr);
+// w = A z (aj-scaled FP64 operator, z in T) and Z[st->j] = z on the interior
+template <typename T>
+int launch_apply64_krylov(const OpView<double>& A, const T* z, T* Z, const KrylovState* st, double* w, cudaStream_t s);
 int launch_arnoldi_finish(KrylovState* st, int nparts, const double* parts, cudaStream_t s);
 int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStream_t s);
 int launch_lsq_update(KrylovState* st, cudaStream_t s);
