@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--div-tol", type=float, default=1e-8, help="max |div u| the solve must reach")
     ap.add_argument("--nu", type=int, default=2)
     ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -224,9 +225,9 @@ def main():
     ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
     ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart,
-                                div_tol=args.div_tol, maxit=400)
+                                div_tol=args.div_tol, maxit=400, orth=args.orth)
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart,
-                               div_tol=args.div_tol, maxit=400)
+                               div_tol=args.div_tol, maxit=400, orth=args.orth)
 
     def steps(params, K, base_slot):
         infos, divs = [], []
@@ -320,7 +321,7 @@ def main():
             "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": args.nu,
-                       "restart": args.restart,
+                       "restart": args.restart, "orth": args.orth,
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},

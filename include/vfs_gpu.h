@@ -42,6 +42,8 @@ extern "C" {
 
 #define VFS_FP64 0   /* plain: FP64 multigrid inside FP64 FGMRES */
 #define VFS_MIXED 1  /* FP32 multigrid (FP32 coefficients) inside FP64 FGMRES */
+#define VFS_ORTH_CGS 1
+#define VFS_ORTH_CGS2 2
 
 /* Fields for vfs_set_field / vfs_get_field. */
 #define VFS_FIELD_UCONT 0  /* 3 doubles per cell (AoS), contravariant flux */
@@ -78,6 +80,9 @@ typedef struct {
   double omega;    /* line-Jacobi damping */
   int warm_start;  /* 1: start from the resident phi, 0: from zero */
   double div_tol;  /* > 0: also require max |div u| <= div_tol after the projection */
+  int orth;        /* Gram-Schmidt of the Arnoldi step: VFS_ORTH_CGS (one
+                      classical pass, the reference's PETSc GMRES default) or
+                      VFS_ORTH_CGS2 (classical with one re-orthogonalisation) */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

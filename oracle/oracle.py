@@ -83,6 +83,9 @@ def lib():
         L.orc_mg_smooth.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_double]
         L.orc_fgmres.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, dp]
         L.orc_fgmres.restype = ctypes.c_int
+        L.orc_fgmres_ex.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    dp]
+        L.orc_fgmres_ex.restype = ctypes.c_int
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -277,16 +280,16 @@ class MG:
         lib().orc_mg_matvec(self.h, l, _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
         return y
 
-    def fgmres(self, b, x0=None, rtol=1e-12, maxit=200, restart=30):
+    def fgmres(self, b, x0=None, rtol=1e-12, maxit=200, restart=30, orth=2):
         x = np.zeros(_shape(self.d)) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
         info = np.zeros(3)
-        rc = lib().orc_fgmres(self.h, _p(np.ascontiguousarray(b, dtype=np.float64)), _p(x), rtol, maxit, restart,
-                              _p(info))
+        rc = lib().orc_fgmres_ex(self.h, _p(np.ascontiguousarray(b, dtype=np.float64)), _p(x), rtol, maxit, restart,
+                                 orth, _p(info))
         return x, dict(converged=(rc == 0), iterations=int(info[0]), relres=float(info[1]), bnorm=float(info[2]))
 
 
 def projection_step(grid, ucont, levels=3, dt=0.04, st=1.0, coeff=1.0, immersed=0, rtol=1e-12, maxit=400,
-                    restart=30, p=None, mg=None):
+                    restart=30, p=None, mg=None, orth=2):
     """The whole CPU pressure-projection step, in the reference's order
     (poisson_hypre.c:580-771, solvers.c:874-930): flux balance, RHS with the
     compatibility fix, FGMRES+GMG solve, null-space removal, phi finish,
@@ -299,7 +302,7 @@ def projection_step(grid, ucont, levels=3, dt=0.04, st=1.0, coeff=1.0, immersed=
     own = mg is None
     if own:
         mg = MG(d, grid.coor, grid.nvert, levels)
-    phi, info = mg.fgmres(b, rtol=rtol, maxit=maxit, restart=restart)
+    phi, info = mg.fgmres(b, rtol=rtol, maxit=maxit, restart=restart, orth=orth)
     if own:
         mg.close()
     remove_mean(d, grid.nvert, phi)

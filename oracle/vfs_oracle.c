@@ -1377,7 +1377,16 @@ static double dot(const double* a, const double* b, size_t n) {
  * preconditioner applications.  x holds the initial guess on entry.
  * info[0] = iterations, info[1] = final true ||b - A x|| / ||b||,
  * info[2] = ||b||. */
+/* orth selects the Gram-Schmidt variant of the Arnoldi step:
+ *   1  classical, one pass (the reference's KSP is created with PETSc's
+ *      defaults, mhv_poisson.c:2166-2178, and GMRES there orthogonalises by
+ *      classical Gram-Schmidt without refinement);
+ *   2  classical with one re-orthogonalisation pass (CGS2). */
+int orc_fgmres_ex(orc_mg* mg, const double* b, double* x, double rtol, int maxit, int restart, int orth, double* info);
 int orc_fgmres(orc_mg* mg, const double* b, double* x, double rtol, int maxit, int restart, double* info) {
+  return orc_fgmres_ex(mg, b, x, rtol, maxit, restart, 2, info);
+}
+int orc_fgmres_ex(orc_mg* mg, const double* b, double* x, double rtol, int maxit, int restart, int orth, double* info) {
   orc_level* F = &mg->lev[mg->L - 1];
   const size_t N = (size_t)F->d.mx * F->d.my * F->d.mz;
   const int m = restart;
@@ -1404,7 +1413,7 @@ int orc_fgmres(orc_mg* mg, const double* b, double* x, double rtol, int maxit, i
       double* zj = Z + (size_t)j * N;
       orc_mg_apply(mg, vj, zj);
       orc_matvec(&F->d, F->coef, zj, w);
-      for (int pass = 0; pass < 2; pass++) {
+      for (int pass = 0; pass < (orth == 2 ? 2 : 1); pass++) {
         for (int q = 0; q <= j; q++) h[q] = dot(V + (size_t)q * N, w, N);
         for (int q = 0; q <= j; q++) {
           const double* vq = V + (size_t)q * N;

@@ -108,7 +108,10 @@ def test_projection_operator_consistency(spheres):
     assert np.abs(lhs - rhs).max() < 1e-12 * max(1.0, np.abs(rhs).max())
 
 
-def test_fgmres_matches_direct_solve():
+@pytest.mark.parametrize("orth", [1, 2])
+def test_fgmres_matches_direct_solve(orth):
+    """Both Gram-Schmidt variants (one classical pass, as PETSc's GMRES
+    default; CGS2) reach the direct solution of the bordered system."""
     case = synth.channel_case(16, 12, 16, seed=3, spheres=[(math.pi, 0.0, math.pi / 2, 0.6)], levels=3)
     grid = case.grid
     d, M, g, coef = _setup(grid)
@@ -116,7 +119,7 @@ def test_fgmres_matches_direct_solve():
     O.volume_flux(d, 1, u, grid.nvert, M)
     b, _ = O.rhs(d, u, grid.nvert)
     mg = O.MG(d, grid.coor, grid.nvert, 3)
-    x, info = mg.fgmres(b, rtol=1e-13, maxit=300)
+    x, info = mg.fgmres(b, rtol=1e-13, maxit=300, orth=orth)
     assert info["converged"]
     A, gid = O.csr(d, coef, grid.nvert)
     n = A.shape[0]

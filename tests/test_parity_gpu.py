@@ -154,11 +154,13 @@ def test_rhs_flux_projection_divergence(gpu_ctx, loaded):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_full_step_parity(gpu_ctx, loaded, precision):
+@pytest.mark.parametrize("orth", ["cgs", "cgs2"])
+def test_full_step_parity(gpu_ctx, loaded, precision, orth):
     case, gid, d, mg = loaded
     g = case.grid
-    ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg)
-    params = capi.default_params(precision=precision, rtol=1e-12, maxit=300, restart=30)
+    ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg,
+                            orth=1 if orth == "cgs" else 2)
+    params = capi.default_params(precision=precision, rtol=1e-12, maxit=300, restart=30, orth=orth)
     u = np.ascontiguousarray(case.ucont.copy())
     p = np.zeros(g.nvert.shape)
     info, divmax = gpu_ctx.projection_step(gid, params, u, p)
@@ -171,7 +173,7 @@ def test_full_step_parity(gpu_ctx, loaded, precision):
     assert np.abs(p[fl] - ref["p"][fl]).max() <= 1e-8 * np.abs(ref["p"][fl]).max()
     assert np.abs(u - ref["ucont"]).max() <= 1e-8 * np.abs(ref["ucont"]).max()
     ref_settings = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=5e-9, maxit=10,
-                                     mg=mg)
+                                     mg=mg, orth=1)
     assert divmax <= ref_settings["divmax"]
     assert divmax < 1e-8
 

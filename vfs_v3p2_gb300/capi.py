@@ -25,6 +25,7 @@ VFS_ERR_BUSY = 7
 
 VFS_FP64 = 0
 VFS_MIXED = 1
+ORTH_CGS, ORTH_CGS2 = 1, 2
 
 FIELD_UCONT = 0
 FIELD_P = 1
@@ -59,7 +60,8 @@ class GridDesc(ctypes.Structure):
 class SolveParams(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
-                ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double)]
+                ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
+                ("orth", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -165,6 +167,8 @@ def default_params(**kw) -> SolveParams:
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
             v = {"fp64": VFS_FP64, "mixed": VFS_MIXED}[v]
+        if k == "orth" and isinstance(v, str):
+            v = {"cgs": ORTH_CGS, "cgs2": ORTH_CGS2}[v]
         setattr(p, k, v)
     return p
 

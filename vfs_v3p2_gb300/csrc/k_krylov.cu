@@ -1,10 +1,15 @@
 // Flexible GMRES(m) in FP64 with all scalars on the device.
 //
 // The Krylov basis V (m+1 vectors) is FP64; the preconditioned directions Z
-// are in the multigrid precision T.  Gram-Schmidt is classical with one
-// re-orthogonalisation pass (CGS2), each pass a deterministic multi-dot
-// (fixed block partials summed in index order by one block) followed by one
-// fused update sweep.  The Hessenberg column, Givens rotations and the
+// are in the multigrid precision T.  Basis vector q is vs[q] * V_q: with one
+// classical Gram-Schmidt pass (the default) the update sweep stores the
+// orthogonalised column unnormalised, together with the multigrid input of
+// the next iteration and its norm partials, and the scale 1 / ||.|| follows
+// from the reduction; the matrix-vector product and the solution update
+// apply vs.  With CGS2 (classical with one re-orthogonalisation pass) the
+// columns are stored normalised (vs = 1).  Every pass is a deterministic
+// multi-dot or norm (fixed block partials summed in index order by one
+// block) or one fused update sweep.  The Hessenberg column, Givens rotations and the
 // residual estimate live in a KrylovState in device memory and are updated
 // by a single-block kernel, so the host enqueues iterations without reading
 // anything back; every kernel returns immediately once st->done is set.
@@ -61,6 +66,7 @@ __global__ void k_norm_finish(KrylovState* st, const double* __restrict__ parts,
       for (int q = 0; q < (st->m + 1) * st->m; q++) st->H[q] = 0.;
       st->j = 0;
       st->inv_hn = nrm > 0. ? 1. / nrm : 0.;
+      st->vs[0] = 1.;  // V_0 is stored normalised
       if (met(st, nrm)) st->done = 1;
     }
   }
@@ -129,7 +135,7 @@ __global__ void k_multidot_finish(KrylovState* st, const double* __restrict__ pa
   for (int q = 0; q < nv; q++) {
     double s = 0.;
     for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[(size_t)p * ld + q];
-    s = block_sum(s, sh);
+    s = block_sum(s, sh) * st->vs[q];
     if (threadIdx.x == 0) {
       st->h[q] = s;
       st->hacc[q] = (pass == 1) ? s : st->hacc[q] + s;
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(KB) k_gs_update(const KrylovState* st, const d
   nv = nv_of(st, nv);
   __shared__ double sh[32];
   __shared__ double hs[72];
-  for (int q = threadIdx.x; q < nv; q += blockDim.x) hs[q] = st->h[q];
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) hs[q] = st->h[q] * st->vs[q];
   __syncthreads();
   double s = 0.;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -173,6 +179,40 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
   return (int)cudaGetLastError();
 }
 
+// One-pass classical Gram-Schmidt update of column j = st->j: the
+// orthogonalised vector u = w - sum_q h_q vs_q V_q is stored unnormalised as
+// V_{j+1}, its multigrid-precision copy as the next preconditioner input, and
+// the partials of ||u||^2 go to parts (k_arnoldi_finish sets vs_{j+1}).
+template <typename T>
+__global__ void __launch_bounds__(KB) k_cgs_update(const KrylovState* st, double* V, const double* __restrict__ w,
+                                                   T* __restrict__ out, size_t n, double* parts) {
+  if (is_done(st)) return;
+  const int nv = st->j + 1;
+  __shared__ double sh[32];
+  __shared__ double hs[72];
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) hs[q] = st->h[q] * st->vs[q];
+  __syncthreads();
+  double* vn = V + (size_t)nv * n;
+  double s = 0.;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    double a = w[t];
+#pragma unroll 4
+    for (int q = 0; q < nv; q++) a = fma(-hs[q], V[(size_t)q * n + t], a);
+    vn[t] = a;
+    out[t] = (T)a;
+    s = fma(a, a, s);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+template <typename T>
+int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s) {
+  k_cgs_update<T><<<krylov_nblocks(n), KB, 0, s>>>(st, V, w, out, n, parts); ++g_launches;
+  return (int)cudaGetLastError();
+}
+template int launch_cgs_update<float>(KrylovState*, double*, const double*, float*, size_t, double*, cudaStream_t);
+template int launch_cgs_update<double>(KrylovState*, double*, const double*, double*, size_t, double*, cudaStream_t);
+
 // Fused CGS2 middle pass: w <- w - V h (h from the first pass), and the
 // second pass's dots V_q . w computed on the updated element while the basis
 // values are still in registers.  NV = compile-time capacity; the kernel does
@@ -187,7 +227,7 @@ __global__ void __launch_bounds__(KB) k_gs_update_dots(const KrylovState* st, co
   if (nv <= NV0 || nv > NV) return;
   __shared__ double hs[NV];
   __shared__ double red[KB / 32][NV];
-  for (int q = threadIdx.x; q < NV; q += blockDim.x) hs[q] = q < nv ? st->h[q] : 0.;
+  for (int q = threadIdx.x; q < NV; q += blockDim.x) hs[q] = q < nv ? st->h[q] * st->vs[q] : 0.;
   __syncthreads();
   double acc[NV];
 #pragma unroll
@@ -266,6 +306,7 @@ __global__ void k_arnoldi_finish(KrylovState* st, const double* __restrict__ par
   st->resid = fabs(st->g[j + 1]);
   st->hn = hn;
   st->inv_hn = hn > 0. ? 1. / hn : 0.;
+  st->vs[j + 1] = st->orth2 ? 1. : st->inv_hn;  // CGS2 normalises the column in k_vnext_in
   st->j = j + 1;
   st->it += 1;
   if (met(st, st->resid) || hn == 0. || !(st->resid == st->resid)) st->done = 1;
@@ -295,7 +336,7 @@ template <typename T>
 __global__ void __launch_bounds__(KB) k_x_update(const KrylovState* st, const T* __restrict__ Z, size_t n, double* x) {
   __shared__ double ys[72];
   const int J = st->j;
-  for (int q = threadIdx.x; q < J; q += blockDim.x) ys[q] = st->y[q];
+  for (int q = threadIdx.x; q < J; q += blockDim.x) ys[q] = st->y[q] * st->vs[q];
   __syncthreads();
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     double a = x[t];

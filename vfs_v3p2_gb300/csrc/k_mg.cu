@@ -42,9 +42,10 @@ constexpr unsigned MASK_CH = (1u << CP) | (1u << EP) | (1u << WP) | (1u << NP) |
                              (1u << TE) | (1u << BE) | (1u << TW) | (1u << BW);
 
 // sum_m coef[m] * x[nbr(m)] over the slots of MASK for interior cell (i, j, k).
-// Addresses are one 32-bit base plus three per-axis offsets with the periodic
-// wrap folded in (i - 1 of i = 1 is mx - 2, i + 1 of i = mx - 2 is 1); grids
-// stay below 2^31 cells, so 19 * N fits as well.
+// Addresses are one 32-bit cell offset plus three per-axis offsets with the
+// periodic wrap folded in (i - 1 of i = 1 is mx - 2, i + 1 of i = mx - 2 is
+// 1); grids stay below 2^31 cells (checked at creation).  The slot base
+// coef + m N is formed in 64 bits (uniform across the block).
 template <unsigned MASK, typename TC, typename TX_, typename TA>
 __device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x, int i, int j,
                                       int k) {
@@ -59,7 +60,7 @@ __device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef
 #pragma unroll
   for (int m = 0; m < 19; m++) {
     if (MASK & (1u << m)) {
-      cv[m] = __ldg(coef + (m * N + c));
+      cv[m] = __ldg((coef + (size_t)m * N) + c);
       xv[m] = __ldg(x + (c + oi[slot_di(m) + 1] + oj[slot_dj(m) + 1] + ok[slot_dk(m) + 1]));
     }
   }
@@ -100,18 +101,21 @@ int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, 
   return (int)cudaGetLastError();
 }
 
-// Outer operator inside the Krylov iteration: w = A z for the
-// preconditioned direction z (multigrid precision) and the copy of z into its
-// Krylov slot Z[st->j]; z[c] is loaded for the stencil's centre anyway.
+// Outer operator inside the Krylov iteration: z (multigrid precision) is the
+// V-cycle applied to the stored column V_j, so the flexible direction of the
+// basis vector vs_j V_j is vs_j z; w = vs_j (A z) in FP64, and z is copied to
+// its Krylov slot Z[st->j] (the solution update applies vs_j again); z[c] is
+// loaded for the stencil's centre anyway.
 template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(TX* TY) k_apply64_krylov(OpView<double> A, const T* __restrict__ z, T* __restrict__ Z,
                                                            const KrylovState* st, double* __restrict__ w) {
   if (skipped(A.skip)) return;
   T* zj = Z + (size_t)st->j * ncell(A.d);
+  const double vs = st->vs[st->j];
   TILE_LOOP(A.d) {
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    w[c] = stencil<MASK, double, T, double>(A.d, A.coef, z, i, j, k);
+    w[c] = vs * stencil<MASK, double, T, double>(A.d, A.coef, z, i, j, k);
     zj[c] = z[c];
   }
 }
@@ -166,22 +170,28 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
   T* su = (T*)smraw;     // r_j / m_j, then y_j, then delta_j
   T* sp = su + TW * nj;  // a_j / m_j
   T* sl = sp + TW * nj;  // c'_j
-  const size_t N = ncell(d);
+  const int N = (int)ncell(d);
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
+  // every load of a cell is issued unconditionally (all addresses are
+  // interior cells; non-fluid rows have finite factors) and non-fluid cells
+  // are selected out afterwards, so no load waits on another
+#pragma unroll 2
   for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
     const int il = idx % TW, jl = idx / TW;
     const int i = i0 + il, j = 1 + jl;
     T u = T(0), pp = T(0), lc = T(0);
     if (i <= d.mx - 2) {
-      const size_t c = cidx(d, i, j, k);
-      if (__ldg(A.coef + c) != T(0)) {
-        const T ax = xi ? stencil<MASK, T, T, T>(d, A.coef, xi, i, j, k) : T(0);
-        u = (__ldg(b + c) - ax) * __ldg(lf + N + c);
-        pp = __ldg(lf + 2 * N + c);
-        lc = __ldg(lf + c);
-      }
+      const int c = k * d.mx * d.my + j * d.mx + i;
+      const T cp = __ldg(A.coef + c);
+      const T ax = xi ? stencil<MASK, T, T, T>(d, A.coef, xi, i, j, k) : T(0);
+      const T r = (__ldg(b + c) - ax) * __ldg((lf + (size_t)N) + c);
+      const T ap = __ldg((lf + 2 * (size_t)N) + c), cl = __ldg(lf + c);
+      const bool fl = cp != T(0);
+      u = fl ? r : T(0);
+      pp = fl ? ap : T(0);
+      lc = fl ? cl : T(0);
     }
     su[idx] = u;
     sp[idx] = pp;
@@ -301,12 +311,9 @@ __global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __
         const int fi = ih - oi[t], fj = jh - oj[t], fk = kh - ok[t];
         const size_t fc = cidx(A.d, fi, fj, fk);
         const double w = fmax(0., 1. - nvf[fc]);
-        T r = T(0);
-        if (w != 0.) {
-          T ax = x ? stencil<MASK, T, T, T>(A.d, A.coef, x, fi, fj, fk) : T(0);
-          r = (b[fc] - ax) * (T)w;
-        }
-        acc += r;
+        const T ax = x ? stencil<MASK, T, T, T>(A.d, A.coef, x, fi, fj, fk) : T(0);
+        const T rr = (b[fc] - ax) * (T)w;
+        acc += (w != 0.) ? rr : T(0);
       }
       acc *= T(0.125);
     }
@@ -339,10 +346,10 @@ __global__ void __launch_bounds__(256) k_resrestrict_tiled(OpView<T> A, const T*
     if (fi <= f.mx - 2 && fj <= f.my - 2) {
       const size_t fc = cidx(f, fi, fj, fk);
       const double w = fmax(0., 1. - nvf[fc]);
-      if (w != 0.) {
-        const T ax = x ? stencil<MASK, T, T, T>(f, A.coef, x, fi, fj, fk) : T(0);
-        r = (b[fc] - ax) * (T)w;
-      }
+      // loads unconditional, weight applied by select (no load waits on nvert)
+      const T ax = x ? stencil<MASK, T, T, T>(f, A.coef, x, fi, fj, fk) : T(0);
+      const T rr = (b[fc] - ax) * (T)w;
+      r = (w != 0.) ? rr : T(0);
     }
     sr[kk][ty][ii] = r;
   }

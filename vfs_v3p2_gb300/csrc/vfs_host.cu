@@ -127,7 +127,7 @@ struct Grid {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
-  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1;
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -253,7 +253,7 @@ int ensure_krylov(vfs_ctx* ctx, Grid& g, int m, int prec) {
     GA(g.V, (size_t)(m + 1) * N);
     GA(g.w, N);
     g.m = m;
-    GA(g.starr, (size_t)(m + 1) * m + 6 * (m + 2));
+    GA(g.starr, (size_t)(m + 1) * m + 7 * (m + 2));
   }
   if (prec == VFS_MIXED && !g.Z32) GA(g.Z32, (size_t)g.m * N);
   if (prec == VFS_FP64 && !g.Z64) GA(g.Z64, (size_t)g.m * N);
@@ -423,7 +423,9 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   h.g = a; a += p.restart + 2;
   h.y = a; a += p.restart + 2;
   h.h = a; a += p.restart + 2;
-  h.hacc = a;
+  h.hacc = a; a += p.restart + 2;
+  h.vs = a;
+  h.orth2 = p.orth == VFS_ORTH_CGS2;
   if (!g.st) {
     int r = galloc(ctx, g, (unsigned char**)&g.st, sizeof(KrylovState));
     if (r) return r;
@@ -463,6 +465,13 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   }
   dbg("apply64", g.L - 1, 0, s);
   dbg("multidot1", 0, launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 1, s), s);
+  if (p.orth == VFS_ORTH_CGS) {
+    // one pass: update, next column, next preconditioner input, norm partials
+    dbg("cgs_update", 0, launch_cgs_update<T>(g.st, g.V, g.w, bbuf<T>(F), N, g.parts, s), s);
+    dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
+    launch_status_copy(g.st, g.hstat, s);
+    return;
+  }
   if (g.m + 1 <= 32) {
     dbg("gs_update_dots", 0, launch_gs_update_dots(g.st, g.V, -1, g.w, N, g.parts, s, g.m + 1), s);
   } else {
@@ -475,14 +484,19 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   launch_status_copy(g.st, g.hstat, s);
 }
 
-bool graphs_allowed(const Grid& g) { return g_probe.kind == 0 && !g_debug && g.m + 1 <= 32; }
+// The CGS2 sequence is graph-replayable up to 32 basis columns (the fused
+// middle pass's largest capacity); the one-pass sequence for any restart.
+bool graphs_allowed(const Grid& g, const vfs_solve_params& p) {
+  return g_probe.kind == 0 && !g_debug && (p.orth == VFS_ORTH_CGS || g.m + 1 <= 32);
+}
 
 // The per-grid iteration graph (captured on first use; re-captured when the
 // solve parameters change).
 template <typename T>
 int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphExec_t* out) {
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
-  if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega) {
+  if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
+      g.ig_orth == p.orth) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -505,6 +519,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_nu1 = p.nu1;
   g.ig_nu2 = p.nu2;
   g.ig_omega = p.omega;
+  g.ig_orth = p.orth;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -550,7 +565,7 @@ int fg_after(vfs_ctx* ctx, Fgmres& f, cudaStream_t s) {
 template <typename T>
 int fg_step(vfs_ctx* ctx, Fgmres& f) {
   Grid& g = *f.g;
-  if (graphs_allowed(g)) {
+  if (graphs_allowed(g, *f.p)) {
     cudaGraphExec_t ex = nullptr;
     int r = iteration_graph<T>(ctx, g, *f.p, &ex);
     if (r) return r;
@@ -675,6 +690,8 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (!(p->rtol > 0.)) return fail(ctx, VFS_ERR_ARG, "rtol must be > 0");
   if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
+  if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
+    return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   return VFS_OK;
 }
 
@@ -713,6 +730,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->omega = 0.8;
   p->warm_start = 0;
   p->div_tol = 0.;
+  p->orth = VFS_ORTH_CGS;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -788,6 +806,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     if (n < 2) return fail(ctx, VFS_ERR_ARG, "too many multigrid levels for this grid");
   }
   if (ext[1] > 3000) return fail(ctx, VFS_ERR_ARG, "the y-line smoother supports at most 3000 cells in j");
+  if ((double)(ext[0] + 2) * (ext[1] + 2) * (ext[2] + 2) > 2147483647.)
+    return fail(ctx, VFS_ERR_ARG, "a grid holds at most 2^31 - 1 cells including ghosts");
   Grid* gp = new Grid();
   Grid& g = *gp;
   g.d = d;

@@ -51,6 +51,8 @@ struct KrylovState {
   double* y;      // m
   double* h;      // m+1 dots of the current pass
   double* hacc;   // m+1 accumulated dots of the column
+  double* vs;     // m+1 column scales: basis vector q is vs[q] * V_q
+  int orth2;      // 1: CGS2 (columns stored normalised, vs = 1)
 };
 
 // parts must hold nblocks * (m + 2) doubles.
@@ -65,6 +67,8 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
 // second CGS pass fused with the first update (capacity <= 32); returns -1 beyond
 int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s,
                           int cap = 32);
+template <typename T>
+int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s);
 template <typename T>
 int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V = nullptr);
 // w = A z (aj-scaled FP64 operator, z in T) and Z[st->j] = z on the interior
