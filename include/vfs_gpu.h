@@ -167,7 +167,9 @@ int vfs_get_metrics(vfs_ctx* ctx, int grid, int level, double* out);
 int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out);
 int vfs_get_level_dims(vfs_ctx* ctx, int grid, int level, int dims[3]);
 int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out);
-/* y = A x with the operator `which` (as vfs_get_coef) of a level. */
+/* y = A x with the operator `which` (as vfs_get_coef) of a level; which 3 =
+ * the aj-scaled FP64 operator applied to x rounded to FP32 (the Krylov
+ * product of the mixed-precision solve). */
 int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, double* y);
 /* One multigrid preconditioner application z = M^{-1} v on the finest level. */
 int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_params* p, const double* v, double* z);

@@ -90,6 +90,27 @@ def test_operator_apply(gpu_ctx, loaded):
         assert np.abs(got32 - refm).max() <= 1e-5 * np.abs(refm).max()  # FP32 coefficients and arithmetic
 
 
+def test_krylov_product_fp32_operand_exact(gpu_ctx, loaded):
+    """The mixed solver's FP64 product on FP32 directions widens each operand
+    on the integer pipe; it must equal the FP64 product of the same rounded
+    values bit for bit, across zeros, signed zeros, FP32 subnormals and the
+    exponent range."""
+    case, gid, d, mg = loaded
+    L = case.levels - 1
+    shp = (d.mz, d.my, d.mx)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal(shp) * np.exp2(rng.integers(-100, 100, size=shp))
+    flat = x.reshape(-1)
+    flat[::7] = 0.0
+    flat[3::11] = -0.0
+    flat[5::13] = 3e-41   # FP32 subnormal
+    flat[6::17] = -1e-44
+    x32 = x.astype(np.float32).astype(np.float64)
+    y3 = gpu_ctx.apply_op(gid, L, 3, x)
+    y1 = gpu_ctx.apply_op(gid, L, 1, x32)
+    assert np.array_equal(y3, y1)
+
+
 def test_transfer_and_smoother(gpu_ctx, loaded):
     case, gid, d, mg = loaded
     rng = np.random.default_rng(6)

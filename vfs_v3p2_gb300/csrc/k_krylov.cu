@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(KB) k_x_update(const KrylovState* st, const T*
   __syncthreads();
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     double a = x[t];
-    for (int q = 0; q < J; q++) a = fma(ys[q], (double)Z[(size_t)q * n + t], a);
+    for (int q = 0; q < J; q++) a = fma(ys[q], to_acc<double>(Z[(size_t)q * n + t]), a);
     x[t] = a;
   }
 }

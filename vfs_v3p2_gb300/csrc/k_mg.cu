@@ -17,6 +17,12 @@
 namespace vfs {
 
 constexpr int TX = 32, TY = 8, KCHUNK = 4;
+// Register budget of the stencil kernels: resident blocks per SM the
+// compiler must allow (4 -> 64 registers, room for a cell's coefficient and
+// neighbour loads to be in flight together).
+#ifndef VFS_STENCIL_MINB
+#define VFS_STENCIL_MINB 4
+#endif
 
 __host__ __forceinline__ dim3 tile_grid(const Dims& d) {
   const int ni = d.mx - 2, nj = d.my - 2, nk = d.mz - 2;
@@ -71,19 +77,60 @@ __device__ __forceinline__ TA stencil(const Dims& d, const TC* __restrict__ coef
   return s;
 }
 
+// The two halves of stencil(), for kernels that gather several cells before
+// summing: the MASK slots' coefficients and neighbour values (x == nullptr:
+// coefficients only), then the sum in slot order.
+template <unsigned MASK, typename TC, typename TX_>
+__device__ __forceinline__ void stencil_gather(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x,
+                                               int i, int j, int k, TC* cv, TX_* xv) {
+  const int sy = d.mx, sz = d.mx * d.my;
+  const int N = sz * d.mz;
+  const int c = k * sz + j * sy + i;
+  const int oi[3] = {(i == 1 && d.ip) ? d.mx - 3 : -1, 0, (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1};
+  const int oj[3] = {((j == 1 && d.jp) ? d.my - 3 : -1) * sy, 0, ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy};
+  const int ok[3] = {((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, 0, ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz};
+#pragma unroll
+  for (int m = 0; m < 19; m++) {
+    if (MASK & (1u << m)) {
+      cv[m] = __ldg((coef + (size_t)m * N) + c);
+      xv[m] = x ? __ldg(x + (c + oi[slot_di(m) + 1] + oj[slot_dj(m) + 1] + ok[slot_dk(m) + 1])) : TX_(0);
+    }
+  }
+}
+template <unsigned MASK, typename TA, typename TC, typename TX_>
+__device__ __forceinline__ TA stencil_dot(const TC* cv, const TX_* xv) {
+  TA s = TA(0);
+#pragma unroll
+  for (int m = 0; m < 19; m++)
+    if (MASK & (1u << m)) s = fma((TA)cv[m], to_acc<TA>(xv[m]), s);
+  return s;
+}
+
+// Stencil at (i, j, k) clamped into the interior (columns and rows past the
+// last interior one of a partial tile read the last one's data; the caller
+// discards them), with every load issued before the first FMA.
+template <unsigned MASK, typename TA, typename TC, typename TX_>
+__device__ __forceinline__ TA stencil_clamped(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x,
+                                              int i, int j, int k) {
+  TC cv[19];
+  TX_ xv[19];
+  stencil_gather<MASK>(d, coef, x, min(i, d.mx - 2), min(j, d.my - 2), k, cv, xv);
+  return stencil_dot<MASK, TA>(cv, xv);
+}
+
 __host__ __forceinline__ bool fits_ch(unsigned mask) { return (mask & ~MASK_CH) == 0u; }
 
 // ---------------------------------------------------------------------------
 // FP64 outer operator: y = A x, or y = b - A x.
 // ---------------------------------------------------------------------------
 template <unsigned MASK, typename TXin>
-__global__ void __launch_bounds__(TX* TY) k_apply64(OpView<double> A, const TXin* __restrict__ x, const double* __restrict__ b,
+__global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_apply64(OpView<double> A, const TXin* __restrict__ x, const double* __restrict__ b,
                                                     double* __restrict__ y) {
   if (skipped(A.skip)) return;
   TILE_LOOP(A.d) {
+    const double s = stencil_clamped<MASK, double>(A.d, A.coef, x, i, j, k);
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    double s = stencil<MASK, double, TXin, double>(A.d, A.coef, x, i, j, k);
     y[c] = b ? b[c] - s : s;
   }
 }
@@ -107,15 +154,16 @@ int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, 
 // its Krylov slot Z[st->j] (the solution update applies vs_j again); z[c] is
 // loaded for the stencil's centre anyway.
 template <unsigned MASK, typename T>
-__global__ void __launch_bounds__(TX* TY) k_apply64_krylov(OpView<double> A, const T* __restrict__ z, T* __restrict__ Z,
+__global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_apply64_krylov(OpView<double> A, const T* __restrict__ z, T* __restrict__ Z,
                                                            const KrylovState* st, double* __restrict__ w) {
   if (skipped(A.skip)) return;
   T* zj = Z + (size_t)st->j * ncell(A.d);
   const double vs = st->vs[st->j];
   TILE_LOOP(A.d) {
+    const double s = stencil_clamped<MASK, double>(A.d, A.coef, z, i, j, k);
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    w[c] = vs * stencil<MASK, double, T, double>(A.d, A.coef, z, i, j, k);
+    w[c] = vs * s;
     zj[c] = z[c];
   }
 }
@@ -130,13 +178,13 @@ template int launch_apply64_krylov<float>(const OpView<double>&, const float*, f
 template int launch_apply64_krylov<double>(const OpView<double>&, const double*, double*, const KrylovState*, double*, cudaStream_t);
 
 template <unsigned MASK, typename T>
-__global__ void __launch_bounds__(TX* TY) k_apply_mg(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+__global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_apply_mg(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                      T* __restrict__ y) {
   if (skipped(A.skip)) return;
   TILE_LOOP(A.d) {
+    const T s = stencil_clamped<MASK, T>(A.d, A.coef, x, i, j, k);
     if (!_in) continue;
     const size_t c = cidx(A.d, i, j, k);
-    T s = stencil<MASK, T, T, T>(A.d, A.coef, x, i, j, k);
     y[c] = b ? b[c] - s : s;
   }
 }
@@ -160,9 +208,23 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // j-periodic seam and to non-fluid cells stay in the residual; non-fluid
 // cells have delta = 0.
 // ---------------------------------------------------------------------------
+#ifndef VFS_SMOOTH_NT
+#define VFS_SMOOTH_NT 256  // threads per block
+#endif
+#ifndef VFS_SMOOTH_MINB
+#define VFS_SMOOTH_MINB 4  // resident blocks per SM the register budget must allow
+#endif
+#ifndef VFS_SMOOTH_U
+#define VFS_SMOOTH_U 1  // cells whose loads one thread issues together in phase 1
+#endif
+#ifndef VFS_SMOOTH_TWMAX
+#define VFS_SMOOTH_TWMAX 32  // columns per block
+#endif
+
 template <unsigned MASK, typename T>
-__global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi,
-                                                const T* __restrict__ b, T* __restrict__ xo, T omega, int TW) {
+__global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
+    k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
+             T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
   extern __shared__ unsigned char smraw[];
   const Dims d = A.d;
@@ -174,28 +236,44 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
-  // every load of a cell is issued unconditionally (all addresses are
-  // interior cells; non-fluid rows have finite factors) and non-fluid cells
-  // are selected out afterwards, so no load waits on another
-#pragma unroll 2
-  for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
-    const int il = idx % TW, jl = idx / TW;
-    const int i = i0 + il, j = 1 + jl;
-    T u = T(0), pp = T(0), lc = T(0);
-    if (i <= d.mx - 2) {
+  constexpr int U = VFS_SMOOTH_U;
+  // Phase 1 in batches of U cells per thread: every load of the batch is
+  // issued before any arithmetic (all addresses are interior cells: columns
+  // past the last one are clamped onto it and discarded; non-fluid rows have
+  // finite factors and are selected out).  The line factors a_j/m_j and c'_j
+  // are formed from the SP and NP coefficients the stencil loads anyway; only
+  // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
+  // b and only CP, SP, NP of the stencil are loaded.
+  for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
+    T cv[U][19], xv[U][19], bb[U], inv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = min(base + u * VFS_SMOOTH_NT, nt - 1);
+      const int il = idx % TW, jl = idx / TW;
+      const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
       const int c = k * d.mx * d.my + j * d.mx + i;
-      const T cp = __ldg(A.coef + c);
-      const T ax = xi ? stencil<MASK, T, T, T>(d, A.coef, xi, i, j, k) : T(0);
-      const T r = (__ldg(b + c) - ax) * __ldg((lf + (size_t)N) + c);
-      const T ap = __ldg((lf + 2 * (size_t)N) + c), cl = __ldg(lf + c);
-      const bool fl = cp != T(0);
-      u = fl ? r : T(0);
-      pp = fl ? ap : T(0);
-      lc = fl ? cl : T(0);
+      if (xi) {
+        stencil_gather<MASK>(d, A.coef, xi, i, j, k, cv[u], xv[u]);
+      } else {
+        cv[u][CP] = __ldg(A.coef + c);
+        cv[u][SP] = __ldg((A.coef + (size_t)SP * N) + c);
+        cv[u][NP] = __ldg((A.coef + (size_t)NP * N) + c);
+      }
+      bb[u] = __ldg(b + c);
+      inv[u] = __ldg(lf + c);
     }
-    su[idx] = u;
-    sp[idx] = pp;
-    sl[idx] = lc;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = base + u * VFS_SMOOTH_NT;
+      if (idx >= nt) break;
+      const int jl = idx / TW;
+      const bool live = (i0 + idx % TW <= d.mx - 2) && cv[u][CP] != T(0);
+      const T ax = xi ? stencil_dot<MASK, T>(cv[u], xv[u]) : T(0);
+      const T a = jl > 0 ? cv[u][SP] : T(0), cn = jl < nj - 1 ? cv[u][NP] : T(0);
+      su[idx] = live ? (bb[u] - ax) * inv[u] : T(0);
+      sp[idx] = live ? a * inv[u] : T(0);
+      sl[idx] = live ? cn * inv[u] : T(0);
+    }
   }
   __syncthreads();
   if (threadIdx.x < TW) {
@@ -216,11 +294,11 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < nt; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < nt; idx += VFS_SMOOTH_NT) {
     const int il = idx % TW, jl = idx / TW;
     const int i = i0 + il, j = 1 + jl;
     if (i > d.mx - 2) continue;
-    const size_t c = cidx(d, i, j, k);
+    const int c = k * d.mx * d.my + j * d.mx + i;
     const T x0 = xi ? xi[c] : T(0);
     xo[c] = x0 + omega * su[idx];
   }
@@ -228,7 +306,7 @@ __global__ void __launch_bounds__(256) k_smooth(OpView<T> A, const T* __restrict
 
 template <typename T>
 static int smooth_tw(int ni, int nj) {
-  int tw = 32;
+  int tw = VFS_SMOOTH_TWMAX;
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   return tw;
@@ -246,15 +324,16 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   const int tw = smooth_tw<T>(ni, nj);
   const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
-  if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
-  else k_smooth<MASK_ALL, T><<<g, 256, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  else k_smooth<MASK_ALL, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
   ++g_launches;
   return (int)cudaGetLastError();
 }
 
-// Thomas factors of the y-line tridiagonal (SP, CP, NP) of every column, in
-// FP64 from the aj-scaled FP64 operator, stored as T: lf[c] = c'_j,
-// lf[N + c] = 1/m_j, lf[2N + c] = a_j/m_j (a_j the SP coupling), so that the
+// Thomas pivots of the y-line tridiagonal (a_j = SP, b_j = CP, c_j = NP) of
+// every column, in FP64 from the aj-scaled FP64 operator, stored as T:
+// lf[c] = 1/m_j with m_j = b_j - a_j c'_{j-1}, c'_j = c_j / m_j.  The sweep
+// forms a_j/m_j and c'_j = c_j/m_j from its own coefficients, so that the
 // forward substitution is y_j = r_j/m_j - (a_j/m_j) y_{j-1} and the backward
 // one delta_j = y_j - c'_j delta_{j+1}.  Non-fluid cells are identity rows;
 // j-periodic seam couplings stay off the line.
@@ -274,9 +353,7 @@ __global__ void k_line_factors(Dims d, const double* __restrict__ mcoef, T* __re
       const double m = bb - a * cprev;
       const double inv = 1. / m;
       cprev = cc * inv;
-      lf[c] = (T)cprev;
-      lf[N + c] = (T)inv;
-      lf[2 * N + c] = (T)(a * inv);
+      lf[c] = (T)inv;
     }
   }
 }
@@ -293,7 +370,7 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // (b - A x) * max(0, 1 - nvert_f), 0 on solid coarse cells; xc = 0.
 // ---------------------------------------------------------------------------
 template <unsigned MASK, typename T>
-__global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+__global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                         const double* __restrict__ nvf, Dims c, const double* __restrict__ nvc,
                                                         int si, int sj, int sk, T* __restrict__ bc, T* __restrict__ xc) {
   if (skipped(A.skip)) return;
@@ -328,7 +405,7 @@ __global__ void __launch_bounds__(TX* TY) k_resrestrict(OpView<T> A, const T* __
 // max(0, 1 - nvert_f) into shared memory, and 128 threads sum the 2 x 2 x 2
 // children of each coarse cell in the reference's order.
 template <unsigned MASK, typename T>
-__global__ void __launch_bounds__(256) k_resrestrict_tiled(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
+__global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                            const double* __restrict__ nvf, Dims c,
                                                            const double* __restrict__ nvc, T* __restrict__ bc,
                                                            T* __restrict__ xc) {
@@ -342,16 +419,15 @@ __global__ void __launch_bounds__(256) k_resrestrict_tiled(OpView<T> A, const T*
   for (int q = 0; q < 4; q++) {
     const int ii = tx + 32 * (q & 1), kk = q >> 1;
     const int fi = fi0 + ii, fj = fj0 + ty, fk = fk0 + kk;
-    T r = T(0);
-    if (fi <= f.mx - 2 && fj <= f.my - 2) {
-      const size_t fc = cidx(f, fi, fj, fk);
-      const double w = fmax(0., 1. - nvf[fc]);
-      // loads unconditional, weight applied by select (no load waits on nvert)
-      const T ax = x ? stencil<MASK, T, T, T>(f, A.coef, x, fi, fj, fk) : T(0);
-      const T rr = (b[fc] - ax) * (T)w;
-      r = (w != 0.) ? rr : T(0);
-    }
-    sr[kk][ty][ii] = r;
+    // loads unconditional and clamped into the interior, the nvert weight
+    // and the tile edge applied by select (no load waits on another)
+    const int fic = min(fi, f.mx - 2), fjc = min(fj, f.my - 2);
+    const size_t fc = cidx(f, fic, fjc, fk);
+    const double w = fmax(0., 1. - nvf[fc]);
+    const T bv = b[fc];
+    const T ax = x ? stencil_clamped<MASK, T>(f, A.coef, x, fic, fjc, fk) : T(0);
+    const T rr = (bv - ax) * (T)w;
+    sr[kk][ty][ii] = (w != 0. && fi <= f.mx - 2 && fj <= f.my - 2) ? rr : T(0);
   }
   __syncthreads();
   if (threadIdx.x < 128) {

@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <atomic>
 
@@ -121,6 +122,47 @@ __device__ __forceinline__ T block_max(T v, T* sh) {
   __syncthreads();
   return v;
 }
+
+// Exact binary32 -> binary64 widening on the integer pipe, without branches.
+// IEEE 754 fixes the result field by field: a normal number's exponent is
+// rebiased by 1023 - 127 = 896 and its 23-bit fraction becomes the top of the
+// 52-bit one; zero keeps its sign; a subnormal m 2^-149 with leading bit p
+// becomes exponent p - 149 with the bits below p as fraction; infinities and
+// NaNs keep their fraction under exponent 2047, a NaN's with the quiet bit
+// set (a conversion returns a quiet NaN).  (The
+// FP64 pipe, which the hardware conversion uses, is the scarce unit of the
+// FP64 Krylov kernels.)
+__host__ __device__ __forceinline__ double widen(float f) {
+#ifdef __CUDA_ARCH__
+  const unsigned u = __float_as_uint(f);
+  const int p = 31 - __clz((u & 0x007fffffu) | 1u);  // leading bit of a subnormal fraction
+#else
+  unsigned u;
+  memcpy(&u, &f, sizeof u);
+  const int p = 31 - __builtin_clz((u & 0x007fffffu) | 1u);
+#endif
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x007fffffu;
+  const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+  const unsigned long long sub = ((unsigned long long)(p + 874) << 52) |
+                                 ((unsigned long long)(m ^ (1u << p)) << (52 - p));
+  const unsigned mq = (e == 0xffu && m != 0u) ? (m | 0x00400000u) : m;
+  const unsigned long long nrm = ((unsigned long long)(e == 0xffu ? 2047u : e + 896u) << 52) |
+                                 ((unsigned long long)mq << 29);
+  const unsigned long long mag = e != 0u ? nrm : (m != 0u ? sub : 0ull);
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)(sgn | mag));
+#else
+  const unsigned long long bits = sgn | mag;
+  double d;
+  memcpy(&d, &bits, sizeof d);
+  return d;
+#endif
+}
+// Operand conversion into an accumulator type (widen() for float -> double).
+template <typename TA, typename TX_>
+__device__ __forceinline__ TA to_acc(TX_ v) { return (TA)v; }
+template <>
+__device__ __forceinline__ double to_acc<double, float>(float v) { return widen(v); }
 
 }  // namespace vfs
 

@@ -85,7 +85,7 @@ struct Level {
   double* coef = nullptr;
   double* mcoef = nullptr;
   float* mcoef32 = nullptr;
-  float* lf32 = nullptr;   // y-line Thomas factors [c' | 1/m | a/m]
+  float* lf32 = nullptr;   // y-line Thomas pivots 1/m
   double* lf64 = nullptr;
   unsigned mask = 0;
   uint8_t* pcode = nullptr;
@@ -278,12 +278,12 @@ int popcount(unsigned m) {
 size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.mz - 2); }
 
 // A full smoothing sweep (x != 0) streams the active coefficient slots, x,
-// b and writes x: (slots + 3) words per interior cell.
+// b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
 void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
   int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s);
-  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 6));
+  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 4));
   dbg("smooth", l, rc, s);
 }
 
@@ -706,7 +706,7 @@ int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* i
 
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
-  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 3) * 8 + N * (19 + 3) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
+  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1) * 8 + N * (19 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 3 + 3 + 3 + 3 + 3);                    // pd u ustar p phi b ucat aos
   return b;
@@ -851,8 +851,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.coef, 19 * Lv.N);
     GAB(Lv.mcoef, 19 * Lv.N);
     GAB(Lv.mcoef32, 19 * Lv.N);
-    GAB(Lv.lf32, 3 * Lv.N);
-    GAB(Lv.lf64, 3 * Lv.N);
+    GAB(Lv.lf32, Lv.N);
+    GAB(Lv.lf64, Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
   }
   const size_t N = ncell(d);
@@ -1382,7 +1382,23 @@ int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, 
     cudaFree(dy);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
     for (size_t q = 0; q < N; q++) y[q] = hy[q];
-  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1 or 2");
+  } else if (which == 3) {
+    // the mixed solver's Krylov product: FP64 aj-scaled operator on FP32 x
+    std::vector<float> hx(N);
+    for (size_t q = 0; q < N; q++) hx[q] = (float)x[q];
+    float* dx;
+    double* dy;
+    CK(cudaMalloc(&dx, N * 4));
+    CK(cudaMalloc(&dy, N * 8));
+    CK(cudaMemcpy(dx, hx.data(), N * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dy, 0, N * 8));
+    OpView<double> A{L.d, L.mcoef, L.mask, nullptr};
+    launch_apply64_xf(A, dx, nullptr, dy, 0);
+    cudaError_t e = cudaMemcpy(y, dy, N * 8, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
+  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1, 2 or 3");
   return VFS_OK;
 }
 

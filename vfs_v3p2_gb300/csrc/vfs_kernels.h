@@ -39,7 +39,7 @@ int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, 
 template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s);
 // one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0;
-// lf = precomputed line factors [c'_j | 1/m_j | a_j/m_j] (3N of T)
+// lf = precomputed y-line Thomas pivots 1/m_j (N of T)
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
 template <typename T>
