@@ -51,7 +51,10 @@ def parse():
     ap.add_argument("--grid", default=None, help="NIxNJxNK override of the sphere workload (profiling sizes)")
     ap.add_argument("--rtol", type=float, default=1e-9)
     ap.add_argument("--div-tol", type=float, default=1e-8, help="max |div u| the solve must reach")
-    ap.add_argument("--nu", type=int, default=2)
+    ap.add_argument("--nu", type=int, default=3, help="pre- and post-smoothing sweeps")
+    ap.add_argument("--nu1", type=int, default=None, help="pre-smoothing sweeps (overrides --nu)")
+    ap.add_argument("--nu2", type=int, default=None, help="post-smoothing sweeps (overrides --nu)")
+    ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -224,10 +227,12 @@ def main():
     ctx.poisson_lhs(gid)
     ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
     ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
-    mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart,
-                                div_tol=args.div_tol, maxit=400, orth=args.orth)
-    fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=args.nu, nu2=args.nu, restart=args.restart,
-                               div_tol=args.div_tol, maxit=400, orth=args.orth)
+    nu1 = args.nu if args.nu1 is None else args.nu1
+    nu2 = args.nu if args.nu2 is None else args.nu2
+    mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
+                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega)
+    fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
+                               div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega)
 
     def steps(params, K, base_slot):
         infos, divs = [], []
@@ -320,8 +325,8 @@ def main():
             "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
-                       "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": args.nu,
-                       "restart": args.restart, "orth": args.orth,
+                       "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2],
+                       "restart": args.restart, "orth": args.orth, "omega": args.omega,
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},

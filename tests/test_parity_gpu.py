@@ -181,7 +181,7 @@ def test_full_step_parity(gpu_ctx, loaded, precision, orth):
     g = case.grid
     ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg,
                             orth=1 if orth == "cgs" else 2)
-    params = capi.default_params(precision=precision, rtol=1e-12, maxit=300, restart=30, orth=orth)
+    params = capi.default_params(precision=precision, rtol=1e-12, maxit=300, restart=30, orth=orth, div_tol=1e-8)
     u = np.ascontiguousarray(case.ucont.copy())
     p = np.zeros(g.nvert.shape)
     info, divmax = gpu_ctx.projection_step(gid, params, u, p)
@@ -208,7 +208,8 @@ def test_mixed_precision_error_vs_fp64_oracle(gpu_ctx):
     gpu_ctx.poisson_lhs(gid)
     ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=1, rtol=1e-13, maxit=400)
     u = np.ascontiguousarray(case.ucont.copy())
-    info, divmax = gpu_ctx.projection_step(gid, capi.default_params(precision="mixed", rtol=1e-12), u, None)
+    info, divmax = gpu_ctx.projection_step(gid, capi.default_params(precision="mixed", rtol=1e-12, div_tol=1e-8), u,
+                                           None)
     phi = gpu_ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape)
     fl = (g.nvert < 0.1)
     fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False

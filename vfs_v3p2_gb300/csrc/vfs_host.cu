@@ -688,6 +688,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->maxit < 1) return fail(ctx, VFS_ERR_ARG, "maxit must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 + p->nu2 < 1) return fail(ctx, VFS_ERR_ARG, "need at least one smoothing sweep");
   if (!(p->rtol > 0.)) return fail(ctx, VFS_ERR_ARG, "rtol must be > 0");
+  if (!(p->omega > 0. && p->omega < 2.)) return fail(ctx, VFS_ERR_ARG, "omega must be in (0, 2)");
   if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
@@ -725,9 +726,9 @@ void vfs_default_params(vfs_solve_params* p) {
   p->rtol = 1e-9;
   p->maxit = 200;
   p->restart = 30;
-  p->nu1 = 2;
-  p->nu2 = 2;
-  p->omega = 0.8;
+  p->nu1 = 3;
+  p->nu2 = 3;
+  p->omega = 0.9;
   p->warm_start = 0;
   p->div_tol = 0.;
   p->orth = VFS_ORTH_CGS;
