@@ -169,9 +169,34 @@ def test_rhs_flux_projection_divergence(gpu_ctx, loaded):
     ucat = gpu_ctx.get_field(gid, capi.FIELD_UCAT, u.shape)
     fl = (g.nvert < 0.1)
     fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
-    assert np.array_equal(ucat[fl], ucat_ref[fl])
+    # precomputed inverse metric vs per-cell Cramer's rule: rounding only
+    assert np.abs(ucat[fl] - ucat_ref[fl]).max() <= 1e-13 * np.abs(ucat_ref[fl]).max()
     dv = O.divergence(d, u_ref, O.metric(M, d, "aj"), g.nvert)
     assert gpu_ctx.divergence_max(gid) == dv
+
+
+def test_projection_fractional_nvert_bitexact(gpu_ctx):
+    """Non-integer nvert values take the FP64 pair tests of the projection
+    (integer ones the byte path); both must reproduce the reference's
+    branch choices, so the corrected fluxes are bit-exact either way."""
+    case = synth.channel_case(32, 16, 16, seed=15, spheres=[(math.pi, 0.0, math.pi / 2, 0.6)], sigma=0.5, levels=3)
+    g = case.grid
+    nv = g.nvert * 0.35  # 0, 0.35 (IB band) and 1.4 (solid)
+    gid = gpu_ctx.grid_create(g.coor, nv, case.levels, 1)
+    gpu_ctx.poisson_lhs(gid)
+    d = O.dims_of(g)
+    M = O.form_metrics(d, g.coor)
+    rng = np.random.default_rng(16)
+    phi = rng.normal(size=nv.shape)
+    O.phi_finish(d, nv, phi)
+    u = case.ucont.copy()
+    u_ref = u.copy()
+    O.projection(d, M, nv, phi, u_ref)
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
+    gpu_ctx.L.vfs_set_field(gpu_ctx.h, gid, capi.FIELD_PHI, capi.dptr(phi))
+    gpu_ctx.projection(gid)
+    assert np.array_equal(gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape), u_ref)
+    gpu_ctx.grid_destroy(gid)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

@@ -296,16 +296,31 @@ int launch_update_pressure(const Dims& d, const double* nvert, const double* phi
 // = 1 (no level set), so their divisions are always exact and omitted.
 __device__ __forceinline__ double div_c(double x, double coeff) { return coeff == 1.0 ? x : x / coeff; }
 
+template <bool NVI>
 __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __restrict__ pd, const double* __restrict__ iaj,
                              const double* __restrict__ jaj, const double* __restrict__ kaj, const double* __restrict__ nvert,
-                             const double* __restrict__ phi, double dt, double st, double coeff, Ucont u) {
+                             const uint8_t* __restrict__ nb8, const double* __restrict__ phi, double dt, double st,
+                             double coeff, Ucont u) {
   const size_t N = ncell(d);
   const int mx = d.mx, my = d.my, mz = d.mz, ip = d.ip, jp = d.jp, kp = d.kp;
   const double THR = VFS_THR;
+  auto gt2 = [&](size_t a, size_t b) -> bool {
+    if (NVI) return (nb8[a] | nb8[b]) != 0;
+    return nvert[a] + nvert[b] > THR;
+  };
+  auto lt2 = [&](size_t a, size_t b) -> bool {
+    if (NVI) return (nb8[a] | nb8[b]) == 0;
+    return nvert[a] + nvert[b] < THR;
+  };
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     const size_t c = _t;
-#define NV(ii, jj, kk) nvert[cidx(d, ii, jj, kk)]
+// nvert pair tests: with NVI every nvert is an integer in [0, 127] and nb8
+// holds it as a byte, so a + b > 0.1 <=> (a | b) != 0 and a + b < 0.1 <=>
+// (a | b) == 0 exactly (no FP64 add and compare)
+#define NVX(ii, jj, kk) cidx(d, ii, jj, kk)
+#define GT2(A, B) gt2(NVX A, NVX B)
+#define LT2(A, B) lt2(NVX A, NVX B)
 #define PH(ii, jj, kk) phi[cidx(d, ii, jj, kk)]
     double dpdc, dpde, dpdz;
     if (j > 0 && j < my - 1 && k > 0 && k < mz - 1)
@@ -314,25 +329,25 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __rest
         if (i == mx - 2 && ip) dpdc = PH(1, j, k) - PH(i, j, k);
         dpde = 0.;
         dpdz = 0.;
-        if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > THR) {
-          if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < THR && (j != 1))
+        if ((j == my - 2 && !jp) || GT2((i, j + 1, k), (i + 1, j + 1, k))) {
+          if (LT2((i, j - 1, k), (i + 1, j - 1, k)) && (j != 1))
             dpde = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.5;
-        } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > THR) {
-          if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < THR)
+        } else if ((j == 1 && !jp) || GT2((i, j - 1, k), (i + 1, j - 1, k))) {
+          if (LT2((i, j + 1, k), (i + 1, j + 1, k)))
             dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
         } else {
           dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.25;
         }
-        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > THR) {
-          if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < THR && (k != 1))
+        if ((k == mz - 2 && !kp) || GT2((i, j, k + 1), (i + 1, j, k + 1))) {
+          if (LT2((i, j, k - 1), (i + 1, j, k - 1)) && (k != 1))
             dpdz = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.5;
-        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > THR) {
-          if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < THR)
+        } else if ((k == 1 && !kp) || GT2((i, j, k - 1), (i + 1, j, k - 1))) {
+          if (LT2((i, j, k + 1), (i + 1, j, k + 1)))
             dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
         } else {
           dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.25;
         }
-        if ((NV(i, j, k) + NV(i + 1, j, k)) < THR) {
+        if (LT2((i, j, k), (i + 1, j, k))) {
           const double a = iaj[c];
           u.x[c] -= div_c((dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt * st, coeff);
         }
@@ -341,27 +356,27 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __rest
       if ((j > 0 && j < my - 2) || (jp && j == my - 2)) {
         dpdc = 0.;
         dpdz = 0.;
-        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > THR) {
-          if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < THR && (i != 1))
+        if ((i == mx - 2 && !ip) || GT2((i + 1, j, k), (i + 1, j + 1, k))) {
+          if (LT2((i - 1, j, k), (i - 1, j + 1, k)) && (i != 1))
             dpdc = (PH(i, j, k) + PH(i, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.5;
-        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > THR) {
-          if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < THR)
+        } else if ((i == 1 && !ip) || GT2((i - 1, j, k), (i - 1, j + 1, k))) {
+          if (LT2((i + 1, j, k), (i + 1, j + 1, k)))
             dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
         } else {
           dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
         }
         if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
         else dpde = PH(i, j + 1, k) - PH(i, j, k);
-        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > THR) {
-          if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < THR && (k != 1))
+        if ((k == mz - 2 && !kp) || GT2((i, j, k + 1), (i, j + 1, k + 1))) {
+          if (LT2((i, j, k - 1), (i, j + 1, k - 1)) && (k != 1))
             dpdz = (PH(i, j, k) + PH(i, j + 1, k) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.5;
-        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > THR) {
-          if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < THR)
+        } else if ((k == 1 && !kp) || GT2((i, j, k - 1), (i, j + 1, k - 1))) {
+          if (LT2((i, j, k + 1), (i, j + 1, k + 1)))
             dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
         } else {
           dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.25;
         }
-        if ((NV(i, j, k) + NV(i, j + 1, k)) < THR) {
+        if (LT2((i, j, k), (i, j + 1, k))) {
           const double a = jaj[c];
           u.y[c] -= div_c((dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt * st, coeff);
         }
@@ -370,33 +385,35 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __rest
       if ((k > 0 && k < mz - 2) || (kp && k == mz - 2)) {
         dpdc = 0.;
         dpde = 0.;
-        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > THR) {
-          if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < THR && (i != 1))
+        if ((i == mx - 2 && !ip) || GT2((i + 1, j, k), (i + 1, j, k + 1))) {
+          if (LT2((i - 1, j, k), (i - 1, j, k + 1)) && (i != 1))
             dpdc = (PH(i, j, k) + PH(i, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.5;
-        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > THR) {
-          if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < THR)
+        } else if ((i == 1 && !ip) || GT2((i - 1, j, k), (i - 1, j, k + 1))) {
+          if (LT2((i + 1, j, k), (i + 1, j, k + 1)))
             dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
         } else {
           dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.25;
         }
-        if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > THR) {
-          if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < THR && (j != 1))
+        if ((j == my - 2 && !jp) || GT2((i, j + 1, k), (i, j + 1, k + 1))) {
+          if (LT2((i, j - 1, k), (i, j - 1, k + 1)) && (j != 1))
             dpde = (PH(i, j, k) + PH(i, j, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.5;
-        } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > THR) {
-          if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < THR)
+        } else if ((j == 1 && !jp) || GT2((i, j - 1, k), (i, j - 1, k + 1))) {
+          if (LT2((i, j + 1, k), (i, j + 1, k + 1)))
             dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
         } else {
           dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
         }
         if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
         else dpdz = PH(i, j, k + 1) - PH(i, j, k);
-        if ((NV(i, j, k) + NV(i, j, k + 1)) < THR) {
+        if (LT2((i, j, k), (i, j, k + 1))) {
           const double a = kaj[c];
           u.z[c] -= div_c((dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt * st, coeff);
         }
       }
 #undef PH
-#undef NV
+#undef NVX
+#undef GT2
+#undef LT2
   }
 }
 
@@ -444,38 +461,74 @@ int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s)
   return (int)cudaGetLastError();
 }
 
-int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const double* phi, double dt,
-                      double st, double coeff, const Ucont& u, cudaStream_t s) {
+int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const uint8_t* nb8,
+                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s) {
   const size_t N = ncell(d);
-  k_projection<<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, phi, dt, st, coeff, u); ++g_launches;
+  if (nb8)
+    k_projection<true><<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, nb8, phi,
+                                                     dt, st, coeff, u);
+  else
+    k_projection<false><<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, nb8,
+                                                      phi, dt, st, coeff, u);
+  ++g_launches;
   k_ucont_ghosts<<<nblk(N), 256, 0, s>>>(d, u); ++g_launches;
   return (int)cudaGetLastError();
 }
 
-// Contra2Cart (rhs.c:144-183): Cartesian velocity at fluid cells.
-__global__ void k_contra2cart(Dims d, const double* __restrict__ M, const double* __restrict__ nvert, Ucont u, double* ucat) {
+// Contra2Cart (rhs.c:144-183): Cartesian velocity at fluid cells, the
+// solution of [csi; eta; zet] ucat = q for the cell-centred contravariant
+// fluxes q.  The reference solves each cell's 3 x 3 system by Cramer's rule
+// (three FP64 divisions); the metric is static, so its inverse (adjugate /
+// determinant, same cofactors) is formed once per grid and the step applies
+// it with nine multiply-adds.  Agrees with Cramer's rule to rounding.
+__global__ void k_inverse_metric(Dims d, const double* __restrict__ M, const double* __restrict__ nvert, double* minv) {
   const size_t N = ncell(d);
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
-    if (!interior(d, i, j, k) || !(nvert[_t] < 0.1)) continue;
+    double* o = minv + 9 * _t;
+    if (!interior(d, i, j, k) || !(nvert[_t] < 0.1)) {
+      for (int q = 0; q < 9; q++) o[q] = 0.;
+      continue;
+    }
     const size_t c = _t;
     const double* A = M + N * MP_CSI + 3 * c;
     const double* B = M + N * MP_ETA + 3 * c;
     const double* E = M + N * MP_ZET + 3 * c;
+    const double det = A[0] * (B[1] * E[2] - B[2] * E[1]) - A[1] * (B[0] * E[2] - B[2] * E[0]) + A[2] * (B[0] * E[1] - B[1] * E[0]);
+    const double r = 1. / det;
+    o[0] = (B[1] * E[2] - B[2] * E[1]) * r;
+    o[1] = -(A[1] * E[2] - A[2] * E[1]) * r;
+    o[2] = (A[1] * B[2] - A[2] * B[1]) * r;
+    o[3] = -(B[0] * E[2] - B[2] * E[0]) * r;
+    o[4] = (A[0] * E[2] - A[2] * E[0]) * r;
+    o[5] = -(A[0] * B[2] - A[2] * B[0]) * r;
+    o[6] = (B[0] * E[1] - B[1] * E[0]) * r;
+    o[7] = -(A[0] * E[1] - A[1] * E[0]) * r;
+    o[8] = (A[0] * B[1] - A[1] * B[0]) * r;
+  }
+}
+int launch_inverse_metric(const Dims& d, const double* M, const double* nvert, double* minv, cudaStream_t s) {
+  k_inverse_metric<<<nblk(ncell(d)), 256, 0, s>>>(d, M, nvert, minv); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+__global__ void k_contra2cart(Dims d, const double* __restrict__ minv, const double* __restrict__ nvert, Ucont u,
+                              double* ucat) {
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    if (!interior(d, i, j, k) || !(nvert[_t] < 0.1)) continue;
+    const size_t c = _t;
+    const double* m = minv + 9 * c;
     const double q0 = 0.5 * (u.x[cidx(d, i - 1, j, k)] + u.x[c]);
     const double q1 = 0.5 * (u.y[cidx(d, i, j - 1, k)] + u.y[c]);
     const double q2 = 0.5 * (u.z[cidx(d, i, j, k - 1)] + u.z[c]);
-    const double det = A[0] * (B[1] * E[2] - B[2] * E[1]) - A[1] * (B[0] * E[2] - B[2] * E[0]) + A[2] * (B[0] * E[1] - B[1] * E[0]);
-    const double det0 = q0 * (B[1] * E[2] - B[2] * E[1]) - q1 * (A[1] * E[2] - A[2] * E[1]) + q2 * (A[1] * B[2] - A[2] * B[1]);
-    const double det1 = -q0 * (B[0] * E[2] - B[2] * E[0]) + q1 * (A[0] * E[2] - A[2] * E[0]) - q2 * (A[0] * B[2] - A[2] * B[0]);
-    const double det2 = q0 * (B[0] * E[1] - B[1] * E[0]) - q1 * (A[0] * E[1] - A[1] * E[0]) + q2 * (A[0] * B[1] - A[1] * B[0]);
-    ucat[3 * c] = det0 / det;
-    ucat[3 * c + 1] = det1 / det;
-    ucat[3 * c + 2] = det2 / det;
+    ucat[3 * c] = m[0] * q0 + m[1] * q1 + m[2] * q2;
+    ucat[3 * c + 1] = m[3] * q0 + m[4] * q1 + m[5] * q2;
+    ucat[3 * c + 2] = m[6] * q0 + m[7] * q1 + m[8] * q2;
   }
 }
-int launch_contra2cart(const Dims& d, const double* M, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s) {
-  k_contra2cart<<<nblk(ncell(d)), 256, 0, s>>>(d, M, nvert, u, ucat); ++g_launches;
+int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s) {
+  k_contra2cart<<<nblk(ncell(d)), 256, 0, s>>>(d, minv, nvert, u, ucat); ++g_launches;
   return (int)cudaGetLastError();
 }
 

@@ -103,6 +103,8 @@ struct Grid {
   int L = 1, si = 0, sj = 0, sk = 0, immersed = 0;
   Level lev[MAXLEV];
   double* pd = nullptr;
+  double* minv = nullptr;   // per-cell inverse metric (9, row-major), Contra2Cart
+  uint8_t* nb8 = nullptr;   // nvert as bytes when all are integers in [0, 127], else null
   double* u = nullptr;      // SoA Ucont: x | y | z
   double* ustar = nullptr;  // SoA resident U*
   double* p = nullptr;
@@ -709,7 +711,7 @@ size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1) * 8 + N * (19 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
-  if (finest) b += N * 8 * (9 + 3 + 3 + 3 + 3 + 3);                    // pd u ustar p phi b ucat aos
+  if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
   return b;
 }
 
@@ -859,6 +861,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   const size_t N = ncell(d);
   GAB(tmp, 9 * N);
   GAB(g.pd, 9 * N);
+  GAB(g.minv, 9 * N);
   GAB(g.u, 3 * N);
   GAB(g.ustar, 3 * N);
   GAB(g.p, N);
@@ -873,6 +876,20 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     for (int j = 1; j < d.my - 1; j++)
       for (int i = 1; i < d.mx - 1; i++)
         if (desc->nvert[cidx(d, i, j, k)] < 0.1) g.nfluid += 1.;
+  // integer nvert (the IB flags 0 / 1 / solid) lets the projection test
+  // nvert pairs with byte ors; any other value keeps the FP64 tests
+  std::vector<uint8_t> nbh(N);
+  bool integral = true;
+  for (size_t c = 0; c < N && integral; c++) {
+    const double v = desc->nvert[c];
+    integral = v >= 0. && v <= 127. && v == (double)(int)v;
+    nbh[c] = integral ? (uint8_t)(int)v : 0;
+  }
+  if (integral) {
+    GAB(g.nb8, N);
+    if (cudaMemcpyAsync(g.nb8, nbh.data(), N, cudaMemcpyHostToDevice, g.s) != cudaSuccess)
+      return bail(cuda_fail(ctx, cudaGetLastError(), "upload"));
+  }
   Level& F = g.lev[L - 1];
   if (cudaMemcpyAsync(F.coor, desc->coor, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess ||
       cudaMemcpyAsync(F.nvert, desc->nvert, N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess)
@@ -881,6 +898,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     launch_coarsen(g.lev[l + 1].d, g.lev[l].d, g.si, g.sj, g.sk, g.lev[l + 1].coor, g.lev[l + 1].nvert, g.lev[l].coor,
                    g.lev[l].nvert, g.s);
   for (int l = 0; l < L; l++) launch_form_metrics(g.lev[l].d, g.lev[l].coor, g.lev[l].M, tmp, g.s);
+  launch_inverse_metric(F.d, F.M, F.nvert, g.minv, g.s);
   cudaError_t e = cudaStreamSynchronize(g.s);
   if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "grid setup"));
   const int id = ctx->next_id++;
@@ -1080,8 +1098,8 @@ int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection");
   Level& F = g.lev[g.L - 1];
-  launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s);
-  launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s);
+  launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s);
+  launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s);
   CK(cudaStreamSynchronize(g.s));
   return VFS_OK;
 }
@@ -1116,8 +1134,8 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
 void step_post(Grid& g, double dt, double st, double coeff) {
   Level& F = g.lev[g.L - 1];
   dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
-  dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.phi, dt, st, coeff, g.U(), g.s), g.s);
-  dbg("contra2cart", 0, launch_contra2cart(F.d, F.M, F.nvert, g.U(), g.ucat, g.s), g.s);
+  dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
+  dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
   dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s), g.s);
 }
 

@@ -25,9 +25,14 @@ int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* pa
 int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStream_t s);
 int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s);
 int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s);
-int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const double* phi, double dt,
-                      double st, double coeff, const Ucont& u, cudaStream_t s);
-int launch_contra2cart(const Dims& d, const double* M, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
+// nb8: nvert as bytes when every value is an integer in [0, 127] (exact
+// integer pair tests), else nullptr (FP64 tests).
+int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const uint8_t* nb8,
+                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s);
+// minv: per-cell inverse of the metric matrix [csi; eta; zet] (9 doubles,
+// row-major), from launch_inverse_metric.
+int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
+int launch_inverse_metric(const Dims& d, const double* M, const double* nvert, double* minv, cudaStream_t s);
 int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s);
 int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
                       cudaStream_t s);
