@@ -371,7 +371,7 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // ---------------------------------------------------------------------------
 template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
-                                                        const double* __restrict__ nvf, Dims c, const double* __restrict__ nvc,
+                                                        const T* __restrict__ rw, Dims c, const double* __restrict__ nvc,
                                                         int si, int sj, int sk, T* __restrict__ bc, T* __restrict__ xc) {
   if (skipped(A.skip)) return;
   const int ia = si ? 0 : 1, ja = sj ? 0 : 1, ka = sk ? 0 : 1;
@@ -387,10 +387,10 @@ __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView
       for (int t = 0; t < 8; t++) {
         const int fi = ih - oi[t], fj = jh - oj[t], fk = kh - ok[t];
         const size_t fc = cidx(A.d, fi, fj, fk);
-        const double w = fmax(0., 1. - nvf[fc]);
+        const T w = rw[fc];
         const T ax = x ? stencil<MASK, T, T, T>(A.d, A.coef, x, fi, fj, fk) : T(0);
-        const T rr = (b[fc] - ax) * (T)w;
-        acc += (w != 0.) ? rr : T(0);
+        const T rr = (b[fc] - ax) * w;
+        acc += (w != T(0)) ? rr : T(0);
       }
       acc *= T(0.125);
     }
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView
 // children of each coarse cell in the reference's order.
 template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
-                                                           const double* __restrict__ nvf, Dims c,
+                                                           const T* __restrict__ rw, Dims c,
                                                            const double* __restrict__ nvc, T* __restrict__ bc,
                                                            T* __restrict__ xc) {
   if (skipped(A.skip)) return;
@@ -423,11 +423,11 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
     // and the tile edge applied by select (no load waits on another)
     const int fic = min(fi, f.mx - 2), fjc = min(fj, f.my - 2);
     const size_t fc = cidx(f, fic, fjc, fk);
-    const double w = fmax(0., 1. - nvf[fc]);
+    const T w = rw[fc];
     const T bv = b[fc];
     const T ax = x ? stencil_clamped<MASK, T>(f, A.coef, x, fic, fjc, fk) : T(0);
-    const T rr = (bv - ax) * (T)w;
-    sr[kk][ty][ii] = (w != 0. && fi <= f.mx - 2 && fj <= f.my - 2) ? rr : T(0);
+    const T rr = (bv - ax) * w;
+    sr[kk][ty][ii] = (w != T(0) && fi <= f.mx - 2 && fj <= f.my - 2) ? rr : T(0);
   }
   __syncthreads();
   if (threadIdx.x < 128) {
@@ -449,17 +449,33 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
 }
 
 template <typename T>
-int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
+int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T* rw, const Dims& c,
                              const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
   const bool ch = fits_ch(A.mask);
   if (!si && !sj && !sk) {
     dim3 g((c.mx - 2 + 31) / 32, (c.my - 2 + 3) / 4, c.mz - 2);
-    if (ch) k_resrestrict_tiled<MASK_CH, T><<<g, 256, 0, s>>>(A, x, b, nvf, c, nvc, bc, xc);
-    else k_resrestrict_tiled<MASK_ALL, T><<<g, 256, 0, s>>>(A, x, b, nvf, c, nvc, bc, xc);
+    if (ch) k_resrestrict_tiled<MASK_CH, T><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+    else k_resrestrict_tiled<MASK_ALL, T><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
   } else {
-    if (ch) k_resrestrict<MASK_CH, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc);
-    else k_resrestrict<MASK_ALL, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, nvf, c, nvc, si, sj, sk, bc, xc);
+    if (ch) k_resrestrict<MASK_CH, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
+    else k_resrestrict<MASK_ALL, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
   }
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Restriction weights of a level, max(0, 1 - nvert) (MyRestriction), in both
+// multigrid precisions; formed once per grid.
+__global__ void k_restrict_weights(size_t n, const double* __restrict__ nv, float* __restrict__ w32,
+                                   double* __restrict__ w64) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const double w = fmax(0., 1. - nv[t]);
+    w32[t] = (float)w;
+    w64[t] = w;
+  }
+}
+int launch_restrict_weights(size_t n, const double* nv, float* w32, double* w64, cudaStream_t s) {
+  k_restrict_weights<<<(unsigned)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096), 256, 0, s>>>(n, nv, w32, w64);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -495,25 +511,43 @@ int launch_restrict(const Dims& f, const T* x, const double* nvf, const Dims& c,
 // per fine interior cell, offsets from the precomputed code.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(TX* TY) k_prolong(Dims f, const uint8_t* __restrict__ code, Dims c, const T* __restrict__ xc,
-                                                    T* __restrict__ xf, int add, int si, int sj, int sk,
-                                                    const int* skip) {
+__global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_prolong(Dims f, const uint8_t* __restrict__ code, Dims c,
+                                                                      const T* __restrict__ xc, T* __restrict__ xf,
+                                                                      int add, int si, int sj, int sk, const int* skip) {
   if (skipped(skip)) return;
-  TILE_LOOP(f) {
-    if (!_in) continue;
-    const size_t q = cidx(f, i, j, k);
-    const uint8_t cd = code[q];
-    T v = T(0);
-    if (!(cd & 0x80)) {
-      const int ia = (cd & 3) - 1, ja = ((cd >> 2) & 3) - 1, ka = ((cd >> 4) & 3) - 1;
-      const int ic = si ? i : (i + 1) / 2, jc = sj ? j : (j + 1) / 2, kc = sk ? k : (k + 1) / 2;
+  // A thread owns KCHUNK cells of one (i, j) column: their codes (and old
+  // values) are loaded first, then all coarse values, so no load waits on
+  // another cell's.  Every candidate coarse index lies within the coarse
+  // level's ghost frame whatever the code, so the no-correction code (bit 7)
+  // is applied by select; columns and planes past the tile edge are clamped
+  // and not stored.
+  const int i = 1 + blockIdx.x * TX + threadIdx.x;
+  const int j = 1 + blockIdx.y * TY + threadIdx.y;
+  const bool in = (i <= f.mx - 2) && (j <= f.my - 2);
+  const int i1 = min(i, f.mx - 2), j1 = min(j, f.my - 2);
+  const int k0 = 1 + blockIdx.z * KCHUNK;
+  uint8_t cd[KCHUNK];
+  T xo[KCHUNK];
+#pragma unroll
+  for (int u = 0; u < KCHUNK; u++) {
+    const size_t q = cidx(f, i1, j1, min(k0 + u, f.mz - 2));
+    cd[u] = code[q];
+    xo[u] = add ? xf[q] : T(0);
+  }
+  const int ic = si ? i1 : (i1 + 1) / 2, jc = sj ? j1 : (j1 + 1) / 2;
+#pragma unroll
+  for (int u = 0; u < KCHUNK; u++) {
+    const int k = min(k0 + u, f.mz - 2);
+    const int kc = sk ? k : (k + 1) / 2;
+    const int ia = (cd[u] & 3) - 1, ja = ((cd[u] >> 2) & 3) - 1, ka = ((cd[u] >> 4) & 3) - 1;
 #define X(a, b, cc) xc[cidx(c, a, b, cc)]
-      v = (X(ic, jc, kc) * T(9) + X(ic, jc + ja, kc) * T(3) + X(ic + ia, jc, kc) * T(3) + X(ic + ia, jc + ja, kc)) * (T(3) / T(64)) +
-          (X(ic, jc, kc + ka) * T(9) + X(ic, jc + ja, kc + ka) * T(3) + X(ic + ia, jc, kc + ka) * T(3) +
-           X(ic + ia, jc + ja, kc + ka)) / T(64);
+    const T v = (X(ic, jc, kc) * T(9) + X(ic, jc + ja, kc) * T(3) + X(ic + ia, jc, kc) * T(3) + X(ic + ia, jc + ja, kc)) *
+                    (T(3) / T(64)) +
+                (X(ic, jc, kc + ka) * T(9) + X(ic, jc + ja, kc + ka) * T(3) + X(ic + ia, jc, kc + ka) * T(3) +
+                 X(ic + ia, jc + ja, kc + ka)) / T(64);
 #undef X
-    }
-    xf[q] = add ? xf[q] + v : v;
+    const T vv = (cd[u] & 0x80) ? T(0) : v;
+    if (in && k0 + u <= f.mz - 2) xf[cidx(f, i1, j1, k)] = add ? xo[u] + vv : vv;
   }
 }
 template <typename T>
@@ -583,7 +617,7 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
   template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t);                 \
   template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
-  template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const double*, const Dims&,           \
+  template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const T*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \
   template int launch_restrict<T>(const Dims&, const T*, const double*, const Dims&, const double*, int, int, int, T*, \
                                   cudaStream_t);                                                                      \

@@ -86,6 +86,8 @@ struct Level {
   double* mcoef = nullptr;
   float* mcoef32 = nullptr;
   float* lf32 = nullptr;   // y-line Thomas pivots 1/m
+  float* rw32 = nullptr;   // restriction weights max(0, 1 - nvert)
+  double* rw64 = nullptr;
   double* lf64 = nullptr;
   unsigned mask = 0;
   uint8_t* pcode = nullptr;
@@ -225,6 +227,9 @@ template <> double*& bbuf<double>(Level& L) { return L.b64; }
 template <typename T> T* lf_of(Level& L);
 template <> float* lf_of<float>(Level& L) { return L.lf32; }
 template <> double* lf_of<double>(Level& L) { return L.lf64; }
+template <typename T> T* rw_of(Level& L);
+template <> float* rw_of<float>(Level& L) { return L.rw32; }
+template <> double* rw_of<double>(Level& L) { return L.rw64; }
 template <typename T> T* binv(Level& L);
 template <> float* binv<float>(Level& L) { return L.Binv32; }
 template <> double* binv<double>(Level& L) { return L.Binv; }
@@ -327,7 +332,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   Level& C = g.lev[l - 1];
   T** xc = xbuf<T>(C);
-  dbg("residual_restrict", l, launch_residual_restrict<T>(A, cur, b, L.nvert, C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s), s);
+  dbg("residual_restrict", l, launch_residual_restrict<T>(A, cur, b, rw_of<T>(L), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s), s);
   T* ec = vcycle<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, skip, s);
   if (!cur) {
     cur = bufs[q & 1];
@@ -709,7 +714,7 @@ int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* i
 
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
-  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1) * 8 + N * (19 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 mcoef32 lf32 pcode
+  size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
   return b;
@@ -856,6 +861,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.mcoef32, 19 * Lv.N);
     GAB(Lv.lf32, Lv.N);
     GAB(Lv.lf64, Lv.N);
+    GAB(Lv.rw32, Lv.N);
+    GAB(Lv.rw64, Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
   }
   const size_t N = ncell(d);
@@ -898,6 +905,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     launch_coarsen(g.lev[l + 1].d, g.lev[l].d, g.si, g.sj, g.sk, g.lev[l + 1].coor, g.lev[l + 1].nvert, g.lev[l].coor,
                    g.lev[l].nvert, g.s);
   for (int l = 0; l < L; l++) launch_form_metrics(g.lev[l].d, g.lev[l].coor, g.lev[l].M, tmp, g.s);
+  for (int l = 0; l < L; l++) launch_restrict_weights(g.lev[l].N, g.lev[l].nvert, g.lev[l].rw32, g.lev[l].rw64, g.s);
   launch_inverse_metric(F.d, F.M, F.nvert, g.minv, g.s);
   cudaError_t e = cudaStreamSynchronize(g.s);
   if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "grid setup"));

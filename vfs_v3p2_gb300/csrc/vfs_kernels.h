@@ -44,10 +44,12 @@ template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
-// fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc
+// fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc.
+// rw = the fine level's weights max(0, 1 - nvert) in T (launch_restrict_weights)
 template <typename T>
-int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const double* nvf, const Dims& c,
+int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T* rw, const Dims& c,
                              const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s);
+int launch_restrict_weights(size_t n, const double* nv, float* w32, double* w64, cudaStream_t s);
 // plain restriction of a fine vector (testing hook)
 template <typename T>
 int launch_restrict(const Dims& f, const T* x, const double* nvf, const Dims& c, const double* nvc, int si, int sj, int sk,
