@@ -149,6 +149,40 @@ int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff);
 /* Divergence (main.c:1244-1390): max |div U| * aj over the fluid. */
 int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out);
 
+/* Allocation-free variant of the divergence check.  It has no counterpart in
+ * the reference: the reference's Divergence (main.c:1244-1390) works on its
+ * own PETSc vectors, while this entry point takes caller-owned device arrays
+ * and allocates nothing (no cudaMalloc/cudaFree or other allocating call).
+ *
+ * Who needs it: a caller that must not allocate device memory while a step is
+ * in flight, e.g. a host time loop that has handed all of HBM to its own
+ * allocator, or one that cannot afford the device-wide synchronisation
+ * cudaFree implies while other streams are busy; such a caller has no vfs_ctx
+ * and no grid buffers to lend.
+ *
+ * What it does: max over interior cells of |div U| * aj, 0 where the cell or
+ * a face neighbour has nvert (the same kernels as vfs_divergence_max), for
+ * the ghosted grid mx x my x mz ([mz][my][mx], i fastest) with periodic flags,
+ * contravariant fluxes as three component arrays ucont_x/_y/_z, aj and nvert,
+ * all device pointers on `device`.  The result is written to the device
+ * double *out, ordered on `stream` (a cudaStream_t; NULL = legacy default
+ * stream); the call does not synchronise.
+ *
+ * Scratch: the per-block maxima live in a file-scope static device array of
+ * 2432 doubles (19 KB) per device.  Nothing in it has to start at zero (every
+ * block writes its entry before the final reduction reads it).  Limits:
+ * grids of 2^31 cells or more (ghosts included) are rejected with
+ * VFS_ERR_ARG; `device` must be the calling thread's current device.
+ * Because the scratch is shared, calls whose kernels may overlap (different
+ * streams, or threads, on the same device without ordering between them)
+ * race and give undefined results: order them.  The first call on a device
+ * looks up the scratch address (cudaGetSymbolAddress, with that device
+ * current) and should come before any stream capture.  err (may be NULL)
+ * receives a message of at most err_len - 1 characters. */
+int vfs_divergence_max_noalloc(int device, int mx, int my, int mz, int i_periodic, int j_periodic, int k_periodic,
+                               const double* ucont_x, const double* ucont_y, const double* ucont_z, const double* aj,
+                               const double* nvert, double* out, void* stream, char* err, int err_len);
+
 /* The pressure section of Flow_Solver (solvers.c:871-931): VolumeFlux,
  * PoissonRHS, the solve, UpdatePressure, Projection, Divergence.
  * ucont_inout (nullable): host U* in, corrected U out; when NULL the

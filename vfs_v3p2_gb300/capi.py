@@ -97,6 +97,7 @@ SIGNATURES = {
     "vfs_update_pressure": ([_P, _I], _I),
     "vfs_projection": ([_P, _I, _D, _D, _D], _I),
     "vfs_divergence_max": ([_P, _I, _DP], _I),
+    "vfs_divergence_max_noalloc": ([_I, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, ctypes.c_char_p, _I], _I),
     "vfs_projection_step": ([_P, _I, _DP, _DP, _D, _D, _D, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo),
                              _DP], _I),
     "vfs_get_metrics": ([_P, _I, _I, _DP], _I),

@@ -7,6 +7,8 @@
 // reference's multiplies and adds in the reference's order, so for equal
 // inputs the outputs are bit-identical (reductions excepted, which sum in a
 // fixed tree order instead of the reference's loop order).
+#include <mutex>
+
 #include "vfs_common.cuh"
 #include "vfs_kernels.h"
 #include "vfs_proj.h"
@@ -592,5 +594,61 @@ int launch_finish_sums(const double* parts, int nparts, int nq, double* out, cud
 }
 
 int partial_blocks(const Dims& d) { return nblk(ncell(d), RB); }
+
+// ---- allocation-free divergence check (static device scratch) ----
+// The block maxima of k_divergence live in this file-scope array instead of
+// a grid's partials buffer.  nblk() caps a launch at 152 * 16 blocks, so the
+// array always holds one partial per block; every block writes its partial
+// before k_finish_max reads it, so nothing in it has to start at zero.
+constexpr int STATIC_PARTS = 152 * 16;
+static __device__ __align__(256) double g_static_parts[STATIC_PARTS];
+
+int divergence_max_static(int device, const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* out,
+                          cudaStream_t s, const char** why) {
+  constexpr int MAXDEV = 64;
+  static std::mutex mu;
+  static double* addr[MAXDEV] = {};
+  if (device < 0 || device >= MAXDEV) {
+    *why = "device index out of range";
+    return 1;
+  }
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) {
+    *why = cudaGetErrorString(e);
+    return 2;
+  }
+  if (cur != device) {
+    *why = "the device argument must be the calling thread's current device";
+    return 1;
+  }
+  double* parts = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[device]) {
+      // once per device, with that device current
+      e = cudaGetSymbolAddress((void**)&addr[device], g_static_parts);
+      if (e != cudaSuccess) {
+        addr[device] = nullptr;
+        *why = cudaGetErrorString(e);
+        return 2;
+      }
+    }
+    parts = addr[device];
+  }
+  const int nb = nblk(ncell(d), RB);
+  if (nb > STATIC_PARTS) {  // unreachable while nblk caps the grid; kept as the stated limit
+    *why = "more block partials than the static scratch holds";
+    return 1;
+  }
+  k_divergence<<<nb, RB, 0, s>>>(d, u, aj, nvert, parts); ++g_launches;
+  k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    *why = cudaGetErrorString(e);
+    return 2;
+  }
+  return 0;
+}
 
 }  // namespace vfs

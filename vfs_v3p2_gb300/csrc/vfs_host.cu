@@ -1112,6 +1112,28 @@ int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
   return VFS_OK;
 }
 
+int vfs_divergence_max_noalloc(int device, int mx, int my, int mz, int i_periodic, int j_periodic, int k_periodic,
+                               const double* ucont_x, const double* ucont_y, const double* ucont_z, const double* aj,
+                               const double* nvert, double* out, void* stream, char* err, int err_len) {
+  auto report = [&](int rc, const char* msg) {
+    if (err && err_len > 0) {
+      std::strncpy(err, msg, (size_t)err_len - 1);
+      err[err_len - 1] = 0;
+    }
+    return rc;
+  };
+  if (!ucont_x || !ucont_y || !ucont_z || !aj || !nvert || !out) return report(VFS_ERR_ARG, "null device pointer");
+  if (mx < 3 || my < 3 || mz < 3) return report(VFS_ERR_ARG, "every extent must be at least 3 (one interior cell)");
+  if ((double)mx * my * mz > 2147483647.)
+    return report(VFS_ERR_ARG, "a grid holds at most 2^31 - 1 cells including ghosts");
+  Dims d{mx, my, mz, i_periodic ? 1 : 0, j_periodic ? 1 : 0, k_periodic ? 1 : 0};
+  Ucont u{const_cast<double*>(ucont_x), const_cast<double*>(ucont_y), const_cast<double*>(ucont_z)};
+  const char* why = "";
+  const int rc = divergence_max_static(device, d, u, aj, nvert, out, (cudaStream_t)stream, &why);
+  if (rc) return report(rc == 1 ? VFS_ERR_ARG : VFS_ERR_CUDA, why);
+  return report(VFS_OK, "");
+}
+
 int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out) {
   if (!ctx || !out) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);

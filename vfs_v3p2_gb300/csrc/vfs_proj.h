@@ -33,6 +33,10 @@ int launch_projection(const Dims& d, const double* pd, const double* M, const do
 // row-major), from launch_inverse_metric.
 int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
 int launch_inverse_metric(const Dims& d, const double* M, const double* nvert, double* minv, cudaStream_t s);
+// Divergence check with its block partials in a static device array (no
+// allocation); returns 0, 1 (argument) or 2 (CUDA) and sets *why on error.
+int divergence_max_static(int device, const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* out,
+                          cudaStream_t s, const char** why);
 int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s);
 int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
                       cudaStream_t s);
