@@ -214,11 +214,14 @@ int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y
 /* One damped y-line Jacobi sweep on a level (FP64 aj-scaled operator). */
 int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x, double omega);
 
-/* ---- batched solves (many uneven grids in shared launches) ---- */
-/* Runs vfs_projection_step on n grids with resident U*; the launches of
- * all grids are interleaved on the context's streams. */
+/* ---- batched solves (many uneven grids, one graph launch per iteration) ---- */
+/* Runs vfs_projection_step (resident U*, pressure and fluxes stay resident)
+ * on n distinct grids.  Every FGMRES iteration of all grids is one CUDA graph
+ * launch (one branch per grid, running concurrently; converged grids skip
+ * their kernels).  p points to n_params = 1 (shared) or n (per grid) solve
+ * parameter sets; infos and divmax (may be NULL) receive n entries. */
 int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, double st, double coeff,
-                              const vfs_solve_params* p, vfs_solve_info* infos, double* divmax);
+                              const vfs_solve_params* p, int n_params, vfs_solve_info* infos, double* divmax);
 
 /* Device synchronisation of all work of a context. */
 int vfs_sync(vfs_ctx* ctx);

@@ -109,8 +109,8 @@ SIGNATURES = {
     "vfs_mg_restrict": ([_P, _I, _I, _DP, _DP], _I),
     "vfs_mg_prolong": ([_P, _I, _I, _DP, _DP], _I),
     "vfs_mg_smooth": ([_P, _I, _I, _DP, _DP, _D], _I),
-    "vfs_projection_step_batch": ([_P, _I, _IP, _D, _D, _D, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo),
-                                   _DP], _I),
+    "vfs_projection_step_batch": ([_P, _I, _IP, _D, _D, _D, ctypes.POINTER(SolveParams), _I,
+                                   ctypes.POINTER(SolveInfo), _DP], _I),
     "vfs_sync": ([_P], _I),
     "vfs_probe_begin": ([_P, _I], _I),
     "vfs_probe_end": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _DP, _DP], _I),
@@ -292,13 +292,17 @@ class Context:
                                               ctypes.byref(params), ctypes.byref(info), ctypes.byref(dm)))
         return info.as_dict(), dm.value
 
-    def projection_step_batch(self, grids, params: SolveParams, dt=0.04, st=1.0, coeff=1.0):
+    def projection_step_batch(self, grids, params, dt=0.04, st=1.0, coeff=1.0):
+        """params: one SolveParams for all grids or a sequence of one per grid."""
         n = len(grids)
         ids = (ctypes.c_int * n)(*grids)
         infos = (SolveInfo * n)()
         dm = np.zeros(n)
-        self.check(self.L.vfs_projection_step_batch(self.h, n, ids, dt, st, coeff, ctypes.byref(params), infos,
-                                                    dptr(dm)))
+        if isinstance(params, SolveParams):
+            parr, npar = (SolveParams * 1)(params), 1
+        else:
+            parr, npar = (SolveParams * n)(*params), n
+        self.check(self.L.vfs_projection_step_batch(self.h, n, ids, dt, st, coeff, parr, npar, infos, dptr(dm)))
         return [i.as_dict() for i in infos], dm
 
     def sync(self):

@@ -399,8 +399,9 @@ int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t
 template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t, double*);
 template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t, double*);
 
+// done and epoch (adjacent) to pinned host memory
 int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s) {
-  return (int)cudaMemcpyAsync(hst, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+  return (int)cudaMemcpyAsync(hst, &st->done, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
 }
 
 }  // namespace vfs

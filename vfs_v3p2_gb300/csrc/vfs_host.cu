@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -125,7 +126,12 @@ struct Grid {
   double* starr = nullptr;
   double* parts = nullptr;
   double* scal = nullptr;   // small device scalars (sums, divmax)
-  int* hstat = nullptr;     // pinned
+  int* hstat = nullptr;     // pinned: done, epoch of the last status copy
+  KrylovState* hk = nullptr;  // pinned copy of the Krylov state (convergence check)
+  double* hv = nullptr;     // pinned: ||r||, max |r|, max |div u|
+  int epoch = 0;            // solve rounds started on this grid
+  cudaEvent_t ev_chk = nullptr, ev_done = nullptr, ev_pend = nullptr;
+  long long busy = 0;       // ticket of the request in flight on this grid (serving)
   cudaStream_t s = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -144,6 +150,7 @@ struct Grid {
 
 struct vfs_ctx {
   int device = 0;
+  cudaStream_t s0 = nullptr;  // batch stream (ticks of the batch graph)
   std::vector<cudaEvent_t> marks;  // vfs_mark slots
   size_t budget = 0, used = 0;
   std::map<int, Grid*> grids;
@@ -201,6 +208,9 @@ void grid_free(vfs_ctx* ctx, Grid* g) {
   if (ctx) ctx->used -= std::min(ctx->used, g->bytes);
   if (g->ig_exec) cudaGraphExecDestroy(g->ig_exec);
   if (g->hstat) cudaFreeHost(g->hstat);
+  if (g->hk) cudaFreeHost(g->hk);
+  if (g->hv) cudaFreeHost(g->hv);
+  for (cudaEvent_t e : {g->ev_chk, g->ev_done, g->ev_pend}) if (e) cudaEventDestroy(e);
   for (auto& e : g->ev) if (e) cudaEventDestroy(e);
   if (g->t0) cudaEventDestroy(g->t0);
   if (g->t1) cudaEventDestroy(g->t1);
@@ -394,6 +404,7 @@ struct Fgmres {
   Grid* g;
   const vfs_solve_params* p;
   int it = 0, j = 0;
+  int epoch = 0;  // the round's epoch (status copies of other rounds are ignored)
   bool observed = false, finished = false;
 };
 
@@ -433,6 +444,8 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   h.hacc = a; a += p.restart + 2;
   h.vs = a;
   h.orth2 = p.orth == VFS_ORTH_CGS2;
+  h.epoch = ++g.epoch;
+  f.epoch = h.epoch;
   if (!g.st) {
     int r = galloc(ctx, g, (unsigned char**)&g.st, sizeof(KrylovState));
     if (r) return r;
@@ -556,7 +569,7 @@ int fg_after(vfs_ctx* ctx, Fgmres& f, cudaStream_t s) {
   CK(cudaEventRecord(g.ev[f.it & 1], s));
   if (f.it >= 2) {
     CK(cudaEventSynchronize(g.ev[(f.it - 1) & 1]));
-    if (g.hstat[0]) f.observed = true;
+    if (g.hstat[0] && g.hstat[1] == f.epoch) f.observed = true;
   }
   if (f.observed || f.it >= p.maxit || f.j == p.restart) {
     const bool last = f.observed || f.it >= p.maxit;
@@ -584,109 +597,11 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
   return fg_after<T>(ctx, f, g.s);
 }
 
-// True aj-scaled residual of the current phi: ||r|| into scal[16] and the
-// masked max |r| (the divergence the projection will leave, times coeff/dt)
-// into scal[17].  Reads back the Krylov state.
-int fg_check(vfs_ctx* ctx, Fgmres& f, KrylovState* h, double* rn, double* rmax) {
-  Grid& g = *f.g;
-  const size_t N = ncell(g.d);
-  cudaStream_t s = g.s;
-  Level& F = g.lev[g.L - 1];
-  dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
-  dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
-  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s), s);
-  double v[2];
-  CK(cudaMemcpyAsync(h, g.st, sizeof(*h), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(v, g.scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  *rn = v[0];
-  *rmax = v[1];
-  if (!(h->bnorm == h->bnorm) || !(h->resid == h->resid) || !(v[0] == v[0])) return fail(ctx, VFS_ERR_NUMERIC, "NaN in the solve");
-  return VFS_OK;
-}
-
-// Close a solve: null-space removal, phi finish, info.
-int fg_close(vfs_ctx* ctx, Fgmres& f, const KrylovState& h, double rn, bool conv, int iters, vfs_solve_info* info) {
-  Grid& g = *f.g;
-  cudaStream_t s = g.s;
-  Level& F = g.lev[g.L - 1];
-  dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s), s);
-  dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
-  CK(cudaEventRecord(g.t1, s));
-  CK(cudaEventSynchronize(g.t1));
-  if (info) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, g.t0, g.t1);
-    info->iterations = iters;
-    info->converged = conv;
-    info->bnorm = h.bnorm;
-    info->relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
-    info->time_ms = ms;
-  }
-  return VFS_OK;
-}
-
-// One FGMRES run until its device flag or maxit; returns iterations used.
-template <typename T>
-int fg_run(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
-  int r = fg_start<T>(ctx, f, atol, warm);
-  if (r) return r;
-  while (!f.finished) {
-    r = fg_step<T>(ctx, f);
-    if (r) return r;
-  }
-  return VFS_OK;
-}
-
 double initial_atol(const Grid& g, const vfs_solve_params& p) {
   if (p.div_tol <= 0.) return 0.;
   const double rmax_tol = p.div_tol * g.coeff / (g.dt * g.st_);
   // max |r| is typically 1/20 .. 1/200 of ||r||_2 / sqrt(n); start optimistic
   return rmax_tol * std::sqrt(std::max(g.nfluid, 1.)) * 0.05;
-}
-
-// After a first FGMRES run (f finished): check the true residual; with
-// div_tol > 0 check the exact masked max |r| (the divergence the projection
-// leaves, dt st / coeff per unit) and, while it is above div_tol, continue
-// from the current phi with a tighter L2 target.  The returned phi leaves
-// max |div u| <= div_tol.
-template <typename T>
-int solve_finish_rounds(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, Fgmres& f, double atol, vfs_solve_info* info) {
-  const double rmax_tol = p.div_tol > 0. ? p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
-  int iters = 0;
-  KrylovState h{};
-  double rn = 0., rmax = 0.;
-  vfs_solve_params pr = p;
-  for (int round = 0;; round++) {
-    int r = fg_check(ctx, f, &h, &rn, &rmax);
-    if (r) return r;
-    iters += h.it;
-    const bool rel_ok = rn <= p.rtol * h.bnorm * 1.0000001 || h.bnorm == 0.;
-    const bool div_ok = p.div_tol <= 0. || rmax <= rmax_tol;
-    if ((rel_ok && div_ok) || iters >= p.maxit || h.bnorm == 0. || round == 7) {
-      f.p = &p;
-      return fg_close(ctx, f, h, rn, rel_ok && div_ok, iters, info);
-    }
-    atol = std::min(atol > 0. ? atol : rn, rn) * (div_ok ? 1. : 0.5 * rmax_tol / rmax);
-    pr.maxit = p.maxit - iters;
-    f.p = &pr;
-    r = fg_run<T>(ctx, f, atol, true);
-    if (r) return r;
-  }
-}
-
-template <typename T>
-int solve_one(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, vfs_solve_info* info) {
-  int r = ensure_mg<T>(ctx, g);
-  if (r) return r;
-  r = ensure_krylov(ctx, g, p.restart, sizeof(T) == 4 ? VFS_MIXED : VFS_FP64);
-  if (r) return r;
-  CK(cudaEventRecord(g.t0, g.s));
-  const double atol = initial_atol(g, p);
-  Fgmres f{&g, &p};
-  r = fg_run<T>(ctx, f, atol, p.warm_start != 0);
-  if (r) return r;
-  return solve_finish_rounds<T>(ctx, g, p, f, atol, info);
 }
 
 int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
@@ -703,13 +618,385 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   return VFS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Solve jobs.  One solve (optionally with the step's flux balance and RHS
+// before it and pressure update, projection, Contra2Cart and divergence
+// after it) is a state machine whose waits are events the driver polls, so
+// that many grids' solves can be in flight together:
+//   START  inputs, step_pre, FGMRES start
+//   ITER   Arnoldi iterations (graph replays) until the device flag or maxit
+//   CHECK  true aj-scaled residual ||r|| and the exact masked max |r| (the
+//          divergence the projection will leave, times coeff / (dt st)) are
+//          on their way to pinned memory; when they arrive, either the solve
+//          closes or, while max |r| is above div_tol, another FGMRES round
+//          starts from the current phi with a tighter L2 target (at most 8)
+//   POST   null-space removal, phi finish, step_post and the outputs are on
+//          their way; when they arrive the job is DONE.
+// All of a job's work is ordered on its grid's stream.
+// ---------------------------------------------------------------------------
+enum JobPhase { J_START = 0, J_ITER, J_CHECK, J_POST, J_DONE };
+
+void step_pre(Grid& g, double dt, double st, double coeff);
+void step_post(Grid& g, double dt, double st, double coeff);
+
+struct Job {
+  Grid* g = nullptr;
+  vfs_solve_params p{};   // the caller's parameters
+  vfs_solve_params pr{};  // this round's (maxit shrinks over the rounds)
+  Fgmres f{};
+  bool pre = false, post = false;
+  const double* u_in = nullptr;  // host AoS U* (with pre); else the resident U*
+  const double* p_in = nullptr;  // host pressure (with pre), else the resident one
+  double* u_out = nullptr;       // host AoS corrected fluxes (with post)
+  double* p_out = nullptr;       // host pressure (with post)
+  double dt = 0.04, st = 1., coeff = 1.;
+  int phase = J_START, round = 0, iters = 0;
+  double atol = 0., rmax_tol = 0.;
+  vfs_solve_info info{};
+  double divmax = 0.;
+  int rc = VFS_OK;
+  std::string err;
+  bool pending = false;  // batch: work on the grid's stream since the last tick
+  long long ticket = 0;
+  bool mixed() const { return p.precision == VFS_MIXED; }
+};
+
+int job_fail(vfs_ctx* ctx, Job& J, int rc) {
+  J.rc = rc;
+  J.err = ctx->err;
+  J.phase = J_DONE;
+  return rc;
+}
+
+template <typename T>
+int job_start(vfs_ctx* ctx, Job& J) {
+  Grid& g = *J.g;
+  int r = ensure_mg<T>(ctx, g);
+  if (!r) r = ensure_krylov(ctx, g, J.p.restart, J.p.precision);
+  if (r) return job_fail(ctx, J, r);
+  const size_t N = ncell(g.d);
+  CK(cudaEventRecord(g.t0, g.s));
+  if (J.pre) {
+    if (J.u_in) {
+      CK(cudaMemcpyAsync(g.aos, J.u_in, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+      launch_aos2soa(N, g.aos, g.u, g.u + N, g.u + 2 * N, g.s);
+    } else {
+      CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
+    }
+    if (J.p_in) CK(cudaMemcpyAsync(g.p, J.p_in, N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+    step_pre(g, J.dt, J.st, J.coeff);
+  }
+  J.rmax_tol = J.p.div_tol > 0. ? J.p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
+  J.atol = initial_atol(g, J.p);
+  J.pr = J.p;
+  J.f = Fgmres{&g, &J.pr};
+  r = fg_start<T>(ctx, J.f, J.atol, J.p.warm_start != 0);
+  if (r) return job_fail(ctx, J, r);
+  J.phase = J_ITER;
+  J.pending = true;
+  return VFS_OK;
+}
+
+// After the FGMRES round ended: the true residual and its exact masked max
+// on their way to pinned memory.
+int job_check_enqueue(vfs_ctx* ctx, Job& J) {
+  Grid& g = *J.g;
+  const size_t N = ncell(g.d);
+  cudaStream_t s = g.s;
+  Level& F = g.lev[g.L - 1];
+  dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
+  dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
+  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s), s);
+  CK(cudaMemcpyAsync(g.hk, g.st, sizeof(KrylovState), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(g.hv, g.scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(g.ev_chk, s));
+  J.phase = J_CHECK;
+  J.pending = true;
+  return VFS_OK;
+}
+
+// The check arrived: close the solve or start another round.
+template <typename T>
+int job_check_eval(vfs_ctx* ctx, Job& J) {
+  Grid& g = *J.g;
+  const KrylovState h = *g.hk;
+  const double rn = g.hv[0], rmax = g.hv[1];
+  if (!(h.bnorm == h.bnorm) || !(h.resid == h.resid) || !(rn == rn)) {
+    fail(ctx, VFS_ERR_NUMERIC, "NaN in the solve");
+    return job_fail(ctx, J, VFS_ERR_NUMERIC);
+  }
+  J.iters += h.it;
+  const bool rel_ok = rn <= J.p.rtol * h.bnorm * 1.0000001 || h.bnorm == 0.;
+  const bool div_ok = J.p.div_tol <= 0. || rmax <= J.rmax_tol;
+  if ((rel_ok && div_ok) || J.iters >= J.p.maxit || h.bnorm == 0. || J.round == 7) {
+    cudaStream_t s = g.s;
+    Level& F = g.lev[g.L - 1];
+    const size_t N = ncell(g.d);
+    dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s), s);
+    dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
+    CK(cudaEventRecord(g.t1, s));
+    if (J.post) {
+      step_post(g, J.dt, J.st, J.coeff);
+      if (J.u_out) {
+        launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, s);
+        CK(cudaMemcpyAsync(J.u_out, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+      }
+      if (J.p_out) CK(cudaMemcpyAsync(J.p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(g.hv + 2, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaEventRecord(g.ev_done, s));
+    J.info.iterations = J.iters;
+    J.info.converged = rel_ok && div_ok;
+    J.info.bnorm = h.bnorm;
+    J.info.relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
+    J.phase = J_POST;
+    J.pending = true;
+    return VFS_OK;
+  }
+  J.atol = std::min(J.atol > 0. ? J.atol : rn, rn) * (div_ok ? 1. : 0.5 * J.rmax_tol / rmax);
+  J.pr.maxit = J.p.maxit - J.iters;
+  J.round++;
+  const int r = fg_start<T>(ctx, J.f, J.atol, true);
+  if (r) return job_fail(ctx, J, r);
+  J.phase = J_ITER;
+  J.pending = true;
+  return VFS_OK;
+}
+
+int job_post_eval(vfs_ctx* ctx, Job& J) {
+  (void)ctx;
+  Grid& g = *J.g;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, g.t0, g.t1);
+  J.info.time_ms = ms;
+  if (J.post) J.divmax = g.hv[2];
+  J.phase = J_DONE;
+  return VFS_OK;
+}
+
+// Advance one job on its own stream as far as it goes without waiting
+// (an iteration's bookkeeping waits for the previous iteration of the same
+// grid only).  Returns 1 if the job moved, 0 if it waits on the device.
+template <typename T>
+int job_advance(vfs_ctx* ctx, Job& J) {
+  Grid& g = *J.g;
+  switch (J.phase) {
+    case J_START:
+      job_start<T>(ctx, J);
+      return 1;
+    case J_ITER: {
+      const int r = fg_step<T>(ctx, J.f);
+      if (r) return job_fail(ctx, J, r), 1;
+      if (J.f.finished) job_check_enqueue(ctx, J);
+      return 1;
+    }
+    case J_CHECK: {
+      const cudaError_t e = cudaEventQuery(g.ev_chk);
+      if (e == cudaErrorNotReady) return 0;
+      if (e != cudaSuccess) return job_fail(ctx, J, cuda_fail(ctx, e, "check")), 1;
+      job_check_eval<T>(ctx, J);
+      return 1;
+    }
+    case J_POST: {
+      const cudaError_t e = cudaEventQuery(g.ev_done);
+      if (e == cudaErrorNotReady) return 0;
+      if (e != cudaSuccess) return job_fail(ctx, J, cuda_fail(ctx, e, "post")), 1;
+      job_post_eval(ctx, J);
+      return 1;
+    }
+    default:
+      return 0;
+  }
+}
+int job_advance_any(vfs_ctx* ctx, Job& J) { return J.mixed() ? job_advance<float>(ctx, J) : job_advance<double>(ctx, J); }
+
+// Block until one of the jobs' awaited events completes (no busy spin).
+void wait_any(std::vector<Job*>& jobs) {
+  for (Job* J : jobs) {
+    if (J->phase == J_CHECK) { cudaEventSynchronize(J->g->ev_chk); return; }
+    if (J->phase == J_POST) { cudaEventSynchronize(J->g->ev_done); return; }
+  }
+}
+
+// Run jobs to completion, each on its grid's stream (single solves; the
+// serving loop uses job_advance directly).
+int run_jobs_streams(vfs_ctx* ctx, std::vector<Job*>& jobs) {
+  for (;;) {
+    int moved = 0, live = 0;
+    for (Job* J : jobs) {
+      if (J->phase == J_DONE) continue;
+      moved += job_advance_any(ctx, *J);
+      if (J->phase != J_DONE) live++;
+    }
+    if (!live) return VFS_OK;
+    if (!moved) wait_any(jobs);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched iterations: ONE CUDA graph per tick holds the next Arnoldi iteration
+// of every grid in the batch, each as its own branch (captured from the
+// grid's stream, forked from and joined to the batch stream), so the
+// iterations of all grids run concurrently from one launch.  Grids whose
+// device flag is set skip their kernels; the graph is re-captured when a grid
+// needs iterations and is not in it, or when fewer than half of its branches
+// are still iterating.  Out-of-graph work of a grid (cycle ends, checks,
+// restarts) stays on the grid's stream, ordered after the latest tick, and
+// the next tick waits for it.
+// ---------------------------------------------------------------------------
+struct BatchGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<Job*> members;
+  unsigned long long kernels = 0;
+  ~BatchGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+int batch_capture(vfs_ctx* ctx, cudaStream_t s0, cudaEvent_t fork, std::vector<cudaEvent_t>& joins,
+                  std::vector<Job*>& members, BatchGraph& bg) {
+  if (bg.exec) {
+    cudaGraphExecDestroy(bg.exec);
+    bg.exec = nullptr;
+  }
+  while (joins.size() < members.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    joins.push_back(e);
+  }
+  const unsigned long long n0 = g_launches.load();
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(fork, s0);
+  for (size_t q = 0; q < members.size(); q++) {
+    Grid& g = *members[q]->g;
+    cudaStreamWaitEvent(g.s, fork, 0);
+    if (members[q]->mixed()) issue_iteration<float>(g, members[q]->p, g.s);
+    else issue_iteration<double>(g, members[q]->p, g.s);
+    cudaEventRecord(joins[q], g.s);
+    cudaStreamWaitEvent(s0, joins[q], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(s0, &graph);
+  bg.kernels = g_launches.load() - n0;
+  g_launches -= bg.kernels;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch capture");
+  e = cudaGraphInstantiate(&bg.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch graph instantiate");
+  bg.members = members;
+  return VFS_OK;
+}
+
+template <typename T>
+int batch_after_tick(vfs_ctx* ctx, Job& J, cudaEvent_t tick, bool have_prev) {
+  Grid& g = *J.g;
+  Fgmres& f = J.f;
+  f.it++;
+  f.j++;
+  if (have_prev && g.hstat[0] && g.hstat[1] == f.epoch) f.observed = true;
+  if (f.observed || f.it >= f.p->maxit || f.j == f.p->restart) {
+    const bool last = f.observed || f.it >= f.p->maxit;
+    CK(cudaStreamWaitEvent(g.s, tick, 0));
+    fg_cycle_end<T>(g, last, g.s);
+    J.pending = true;
+    f.finished = last;
+    f.j = 0;
+    if (last) return job_check_enqueue(ctx, J);
+  }
+  return VFS_OK;
+}
+
+int run_jobs_batch(vfs_ctx* ctx, std::vector<Job*>& jobs, cudaStream_t s0) {
+  cudaEvent_t fork = nullptr, ticks[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> joins;
+  BatchGraph bg;
+  auto cleanup = [&]() {
+    if (fork) cudaEventDestroy(fork);
+    for (cudaEvent_t e : ticks) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+  };
+  struct Guard {
+    std::function<void()> f;
+    ~Guard() { f(); }
+  } guard{cleanup};
+  CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ticks[0], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ticks[1], cudaEventDisableTiming));
+  for (Job* J : jobs) {
+    if (J->mixed()) job_start<float>(ctx, *J);
+    else job_start<double>(ctx, *J);
+  }
+  long long t = 0;
+  bool ticked_prev = false;
+  for (;;) {
+    std::vector<Job*> iter;
+    int live = 0;
+    for (Job* J : jobs) {
+      if (J->phase == J_DONE) continue;
+      live++;
+      if (J->phase == J_ITER) iter.push_back(J);
+    }
+    if (!live) return VFS_OK;
+    if (iter.empty()) {
+      // only checks and closes in flight: poll them, wait if none moved
+      int moved = 0;
+      for (Job* J : jobs) if (J->phase == J_CHECK || J->phase == J_POST) moved += job_advance_any(ctx, *J);
+      if (!moved) wait_any(jobs);
+      ticked_prev = false;
+      continue;
+    }
+    bool need = !bg.exec || iter.size() * 2 < bg.members.size();
+    for (Job* J : iter) {
+      if (std::find(bg.members.begin(), bg.members.end(), J) == bg.members.end()) need = true;
+    }
+    if (need) {
+      int r = batch_capture(ctx, s0, fork, joins, iter, bg);
+      if (r) return r;
+    }
+    // order the tick after every member's out-of-graph work
+    for (Job* J : bg.members) {
+      if (!J->pending) continue;
+      CK(cudaEventRecord(J->g->ev_pend, J->g->s));
+      CK(cudaStreamWaitEvent(s0, J->g->ev_pend, 0));
+      J->pending = false;
+    }
+    CK(cudaGraphLaunch(bg.exec, s0));
+    g_launches += bg.kernels;
+    cudaEvent_t tick = ticks[t & 1];
+    CK(cudaEventRecord(tick, s0));
+    const bool have_prev = ticked_prev;
+    if (have_prev) CK(cudaEventSynchronize(ticks[(t - 1) & 1]));
+    for (Job* J : bg.members) {
+      if (J->phase != J_ITER) continue;
+      const int r = J->mixed() ? batch_after_tick<float>(ctx, *J, tick, have_prev)
+                               : batch_after_tick<double>(ctx, *J, tick, have_prev);
+      if (r) job_fail(ctx, *J, r);
+    }
+    // checks and closes of other grids progress between ticks
+    for (Job* J : jobs) {
+      if (J->phase != J_CHECK && J->phase != J_POST) continue;
+      CK(cudaStreamWaitEvent(J->g->s, tick, 0));
+      job_advance_any(ctx, *J);
+    }
+    ticked_prev = true;
+    t++;
+  }
+}
+
 int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* info) {
   int r = check_params(ctx, p);
   if (r) return r;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the solve");
   if (g.m && p->restart > g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow after the first solve");
-  r = (p->precision == VFS_MIXED) ? solve_one<float>(ctx, g, *p, info) : solve_one<double>(ctx, g, *p, info);
-  return r;
+  Job J;
+  J.g = &g;
+  J.p = *p;
+  std::vector<Job*> jobs{&J};
+  r = run_jobs_streams(ctx, jobs);
+  if (r) return r;
+  if (J.rc) return J.rc;
+  if (info) *info = J.info;
+  return VFS_OK;
 }
 
 size_t level_bytes(const Dims& d, bool finest) {
@@ -770,6 +1057,7 @@ void vfs_destroy(vfs_ctx* ctx) {
   for (auto& e : ctx->marks) cudaEventDestroy(e);
   for (auto& kv : ctx->grids) grid_free(ctx, kv.second);
   ctx->grids.clear();
+  if (ctx->s0) cudaStreamDestroy(ctx->s0);
   delete ctx;
 }
 
@@ -833,7 +1121,12 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   cudaEventCreateWithFlags(&g.ev[1], cudaEventDisableTiming);
   cudaEventCreate(&g.t0);
   cudaEventCreate(&g.t1);
-  if (cudaMallocHost(&g.hstat, 4 * sizeof(int)) != cudaSuccess) return bail(cuda_fail(ctx, cudaGetLastError(), "pinned"));
+  if (cudaMallocHost(&g.hstat, 4 * sizeof(int)) != cudaSuccess || cudaMallocHost(&g.hk, sizeof(KrylovState)) != cudaSuccess ||
+      cudaMallocHost(&g.hv, 4 * sizeof(double)) != cudaSuccess)
+    return bail(cuda_fail(ctx, cudaGetLastError(), "pinned"));
+  cudaEventCreateWithFlags(&g.ev_chk, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&g.ev_done, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&g.ev_pend, cudaEventDisableTiming);
   // level extents, finest = L-1
   g.lev[L - 1].d = d;
   for (int l = L - 2; l >= 0; l--) {
@@ -1183,88 +1476,65 @@ int vfs_projection_step(vfs_ctx* ctx, int grid, double* ucont_inout, double* p_i
   if (r) return r;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection step");
   if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
-  const size_t N = ncell(g.d);
-  if (ucont_inout) {
-    CK(cudaMemcpyAsync(g.aos, ucont_inout, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s));
-    launch_aos2soa(N, g.aos, g.u, g.u + N, g.u + 2 * N, g.s);
-  } else {
-    CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
-  }
-  if (p_inout) CK(cudaMemcpyAsync(g.p, p_inout, N * sizeof(double), cudaMemcpyHostToDevice, g.s));
-  step_pre(g, dt, st, coeff);
-  vfs_solve_info tmp{};
-  r = do_solve(ctx, g, p, info ? info : &tmp);
+  if (g.m && p->restart > g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow after the first solve");
+  if (g.busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
+  Job J;
+  J.g = &g;
+  J.p = *p;
+  J.pre = J.post = true;
+  J.u_in = ucont_inout;
+  J.u_out = ucont_inout;
+  J.p_in = p_inout;
+  J.p_out = p_inout;
+  J.dt = dt;
+  J.st = st;
+  J.coeff = coeff;
+  std::vector<Job*> jobs{&J};
+  r = run_jobs_streams(ctx, jobs);
   if (r) return r;
-  step_post(g, dt, st, coeff);
-  if (ucont_inout) {
-    launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, g.s);
-    CK(cudaMemcpyAsync(ucont_inout, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
-  }
-  if (p_inout) CK(cudaMemcpyAsync(p_inout, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.s));
-  double dm = 0.;
-  CK(cudaMemcpyAsync(&dm, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
-  CK(cudaStreamSynchronize(g.s));
-  if (divmax) *divmax = dm;
-  const vfs_solve_info& i = info ? *info : tmp;
-  if (!i.converged) return fail(ctx, VFS_ERR_NOTCONV, "FGMRES stopped at maxit above rtol");
+  if (J.rc) return fail(ctx, J.rc, J.err);
+  if (info) *info = J.info;
+  if (divmax) *divmax = J.divmax;
+  if (!J.info.converged) return fail(ctx, VFS_ERR_NOTCONV, "FGMRES stopped at maxit above rtol");
   return VFS_OK;
 }
 
 int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, double st, double coeff,
-                              const vfs_solve_params* p, vfs_solve_info* infos, double* divmax) {
-  if (!ctx || n < 0 || (n && !grids)) return VFS_ERR_ARG;
-  int r = check_params(ctx, p);
+                              const vfs_solve_params* p, int n_params, vfs_solve_info* infos, double* divmax) {
+  if (!ctx || n < 0 || (n && !grids) || !p) return VFS_ERR_ARG;
+  if (n_params != 1 && n_params != n) return fail(ctx, VFS_ERR_ARG, "n_params must be 1 or n");
+  if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
+  std::vector<Job> js(n);
+  std::vector<Job*> jobs(n);
+  for (int q = 0; q < n; q++) {
+    const vfs_solve_params* pq = p + (n_params == 1 ? 0 : q);
+    int r = check_params(ctx, pq);
+    if (r) return r;
+    Grid* g = get_grid(ctx, grids[q]);
+    if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid in the batch");
+    if (!g->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the batch");
+    if (g->m && pq->restart > g->m) return fail(ctx, VFS_ERR_ARG, "restart cannot grow");
+    if (g->busy) return fail(ctx, VFS_ERR_BUSY, "a grid of the batch has a request in flight");
+    for (int u = 0; u < q; u++)
+      if (grids[u] == grids[q]) return fail(ctx, VFS_ERR_ARG, "a grid appears twice in the batch");
+    Job& J = js[q];
+    J.g = g;
+    J.p = *pq;
+    J.pre = J.post = true;
+    J.dt = dt;
+    J.st = st;
+    J.coeff = coeff;
+    jobs[q] = &J;
+  }
+  if (!ctx->s0) CK(cudaStreamCreateWithFlags(&ctx->s0, cudaStreamNonBlocking));
+  int r = run_jobs_batch(ctx, jobs, ctx->s0);
   if (r) return r;
-  std::vector<Grid*> gs(n);
-  for (int q = 0; q < n; q++) {
-    gs[q] = get_grid(ctx, grids[q]);
-    if (!gs[q]) return fail(ctx, VFS_ERR_ARG, "no such grid in the batch");
-    if (!gs[q]->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the batch");
-    if (gs[q]->m && p->restart > gs[q]->m) return fail(ctx, VFS_ERR_ARG, "restart cannot grow");
-  }
-  const bool mixed = p->precision == VFS_MIXED;
-  std::vector<Fgmres> fs(n);
-  for (int q = 0; q < n; q++) {
-    Grid& g = *gs[q];
-    r = mixed ? ensure_mg<float>(ctx, g) : ensure_mg<double>(ctx, g);
-    if (!r) r = ensure_krylov(ctx, g, p->restart, p->precision);
-    if (r) return r;
-    const size_t N = ncell(g.d);
-    CK(cudaEventRecord(g.t0, g.s));
-    CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
-    step_pre(g, dt, st, coeff);
-    fs[q] = Fgmres{&g, p};
-    const double atol = initial_atol(g, *p);
-    r = mixed ? fg_start<float>(ctx, fs[q], atol, p->warm_start != 0) : fg_start<double>(ctx, fs[q], atol, p->warm_start != 0);
-    if (r) return r;
-  }
-  // interleave the iterations of all grids, each on its own stream
-  int live = n;
-  while (live > 0) {
-    live = 0;
-    for (int q = 0; q < n; q++) {
-      if (fs[q].finished) continue;
-      r = mixed ? fg_step<float>(ctx, fs[q]) : fg_step<double>(ctx, fs[q]);
-      if (r) return r;
-      if (!fs[q].finished) live++;
-    }
-  }
   int rc = VFS_OK;
   for (int q = 0; q < n; q++) {
-    vfs_solve_info tmp{};
-    const double atol = initial_atol(*gs[q], *p);
-    r = mixed ? solve_finish_rounds<float>(ctx, *gs[q], *p, fs[q], atol, infos ? &infos[q] : &tmp)
-              : solve_finish_rounds<double>(ctx, *gs[q], *p, fs[q], atol, infos ? &infos[q] : &tmp);
-    if (r) return r;
-    step_post(*gs[q], dt, st, coeff);
-  }
-  for (int q = 0; q < n; q++) {
-    Grid& g = *gs[q];
-    double dm = 0.;
-    CK(cudaMemcpyAsync(&dm, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
-    CK(cudaStreamSynchronize(g.s));
-    if (divmax) divmax[q] = dm;
-    if (infos && !infos[q].converged) rc = VFS_ERR_NOTCONV;
+    if (js[q].rc) return fail(ctx, js[q].rc, js[q].err);
+    if (infos) infos[q] = js[q].info;
+    if (divmax) divmax[q] = js[q].divmax;
+    if (!js[q].info.converged) rc = VFS_ERR_NOTCONV;
   }
   if (rc) fail(ctx, rc, "a solve of the batch stopped at maxit above rtol");
   return rc;

@@ -49,6 +49,7 @@ struct KrylovState {
   int m;          // restart length
   int j;          // current Arnoldi column
   int done;       // 1 once converged (or broken down)
+  int epoch;      // solve round, copied to the host beside done (a stale copy is recognisable)
   int it;         // preconditioner applications so far
   int reorth;     // 1 if the second Gram-Schmidt pass is needed this column
   double rtol, atol, bnorm, beta, resid;  // converged: resid <= rtol*bnorm and (atol <= 0 or resid <= atol)
