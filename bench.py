@@ -46,7 +46,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="sphere", choices=["channel", "sphere", "terrain"])
+    ap.add_argument("--config", default="sphere", choices=["channel", "sphere", "terrain", "batch", "serve"])
+    ap.add_argument("--requests", type=int, default=400, help="serve: timed requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate, requests/s")
+    ap.add_argument("--tune", action="store_true", help="batch/serve: autotune sweeps and tiles per size class")
     ap.add_argument("--scale", type=int, default=1, help="divide each grid extent (quick runs)")
     ap.add_argument("--grid", default=None, help="NIxNJxNK override of the sphere workload (profiling sizes)")
     ap.add_argument("--rtol", type=float, default=1e-9)
@@ -81,6 +84,10 @@ WORKLOAD = {
     "channel": "channel 64x64x64, tanh beta 2.0, skew 0.05 sin(z), no body, U ~ N(0,1) per face",
     "sphere": "channel 256x128x128 + sphere r=0.3 at (pi,0,pi/2), Poiseuille + N(0,0.1^2)",
     "terrain": "terrain 512x256x256 over a Gaussian hill, log-law + N(0,0.05^2)",
+    "batch": "64 independent channel grids, extents log-uniform 32^3..192x96x96, skew U[0,0.1], beta U[1.5,3], "
+             "0-3 spheres r U[0.1,0.3], U ~ N(0,1); one graph launch per FGMRES iteration for all 64",
+    "serve": "Poisson arrivals from 16 streams, extents log-uniform 32^3..256x128x128, U* = previous + N(0,0.01^2), "
+             "warm start from the resident phi, HBM admission budget 120 GB",
 }
 
 
@@ -197,6 +204,28 @@ def run_reference(args):
     dist, rank, local, ws = dist_init()
     if rank != 0:
         return
+    if args.config in ("batch", "serve"):
+        # the oracle on a sample of the workload's own grids (its median-size ones)
+        from vfs_v3p2_gb300 import serve, synth
+        if args.config == "batch":
+            pool = synth.c4_batch(64, seed=1004)
+        else:
+            pool = [s.case for s in serve.serving_streams(16)]
+        pool.sort(key=lambda c: c.grid.nvert.size)
+        sample = pool[len(pool) // 2 - 1:len(pool) // 2 + 1]
+        rates = [cpu_baseline(c, args, steps=1)[0] for c in sample]
+        val = float(len(rates) / sum(1.0 / r for r in rates))
+        cores = os.cpu_count()
+        line = {"metric": "pressure projection steps/s (solves/s)", "value": val, "unit": "solves/s",
+                "impl": "reference", "n_gpus": args.gpus, "steps": len(sample), "warmup": 1,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded)", "config": {"workload": WORKLOAD[args.config]},
+                "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
+                                 "sample": "two median-size grids of the workload, one step each after a warm-up"},
+                "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference build unavailable (PETSc/HYPRE/MPI absent); CPU oracle restatement"}
+        print(json.dumps(line), flush=True)
+        return
     case = make_case(args)
     val, cores, r = cpu_baseline(case, args, steps=max(1, min(args.steps, 3)))
     line = {
@@ -213,10 +242,120 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def base_line(args, ws):
+    return {"n_gpus": ws, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)"}
+
+
+def main_batch(args, dist, rank, local, ws):
+    from vfs_v3p2_gb300 import autotune, capi, synth
+    sc = max(1, args.scale)
+    cases = synth.c4_batch(64, seed=1004, lo=(32 // sc, 32 // sc, 32 // sc), hi=(192 // sc, 96 // sc, 96 // sc))
+    ctx = capi.Context(local)
+    base = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400, restart=args.restart)
+    tuned = None
+    if args.tune:
+        plist, tuned = autotune.tuned_params(ctx, cases, base)
+    else:
+        plist = base
+    ids = []
+    for c in cases:
+        gid = ctx.grid_create(c.grid.coor, c.grid.nvert, c.levels, c.immersed)
+        ctx.poisson_lhs(gid)
+        ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
+        ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
+        ids.append(gid)
+    for _ in range(args.warmup):
+        ctx.projection_step_batch(ids, plist)
+    clk = Clocks(local)
+    barrier(dist)
+    n0 = capi.launch_count()
+    per, its, dms = [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        infos, dm = ctx.projection_step_batch(ids, plist)
+        per.append(time.perf_counter() - t0)
+        its += [i["iterations"] for i in infos]
+        dms.append(float(dm.max()))
+    nl = capi.launch_count() - n0
+    clocks = clk.stop()
+    barrier(dist)
+    total = allmax(dist, sum(per))
+    cells = sum(c.grid.ni * c.grid.nj * c.grid.nk for c in cases)
+    line = {"metric": "batched pressure projection steps/s (64 uneven grids, one graph launch per FGMRES iteration), "
+                      "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+            "value": ws * len(ids) * args.steps / total, "unit": "solves/s", "steps": args.steps,
+            "ms_per_step": 1e3 * total / args.steps, **base_line(args, ws),
+            "config": {"workload": WORKLOAD["batch"], "grids": len(ids), "cells_total": int(cells),
+                       "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": bool(args.tune),
+                       "timer": "host wall clock around synchronous batch calls (results on the host)",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": None, "iterations": {"mean": float(np.mean(its)), "max": int(max(its))}, "divmax": max(dms),
+            "latency_ms": {"p50": float(np.percentile(per, 50) * 1e3), "p99": float(np.percentile(per, 99) * 1e3)},
+            "clocks": clocks, "gpu_launches": int(nl)}
+    if tuned:
+        line["autotune"] = tuned
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for gid in ids:
+        ctx.grid_destroy(gid)
+    ctx.close()
+
+
+def main_serve(args, dist, rank, local, ws):
+    from vfs_v3p2_gb300 import autotune, capi, serve
+    sc = max(1, args.scale)
+    streams = serve.serving_streams(16, lo=(32 // sc,) * 3, hi=(256 // sc, 128 // sc, 128 // sc))
+    ctx = capi.Context(local, hbm_budget_bytes=120 * 10**9, max_inflight=16)
+    params = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
+                                 restart=args.restart, warm_start=1)
+    srv = serve.Server(ctx, streams, params)
+    for s in streams:  # resident hierarchies of the 16 streams (admission)
+        srv.ensure_grid(s)
+    # warm-up: every stream serves a few requests (graph capture, warm phi)
+    warm = serve.poisson_arrivals(max(48, 16 * args.warmup), args.rate, 16, seed=7)
+    srv.run(warm)
+    arr = serve.poisson_arrivals(args.requests, args.rate, 16)
+    clk = Clocks(local)
+    barrier(dist)
+    n0 = capi.launch_count()
+    recs, wall = srv.run(arr)
+    nl = capi.launch_count() - n0
+    clocks = clk.stop()
+    barrier(dist)
+    wall = allmax(dist, wall)
+    summ = serve.summarize(recs, wall)
+    cells = [streams[r["stream"]].case.grid.nvert.size for r in recs]
+    h2d = float(np.mean([24 * c for c in cells]))
+    d2h = float(np.mean([8 * c for c in cells]))
+    line = {"metric": "served pressure projection steps/s with p50/p99 latency (Poisson arrivals, continuous batching), "
+                      "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+            "value": ws * summ["solves_per_s"], "unit": "solves/s", "steps": len(recs),
+            "ms_per_step": 1e3 * wall / len(recs), **base_line(args, ws),
+            "config": {"workload": WORKLOAD["serve"], "streams": 16, "rate_req_s": args.rate,
+                       "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16, "rtol": args.rtol,
+                       "div_tol": args.div_tol, "timer": "host wall clock, first arrival to last result",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": ws * summ["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "latency_ms": summ["latency_ms"], "iterations": summ["iterations"], "divmax": summ["divmax"],
+            "failed": summ["failed"], "clocks": clocks, "gpu_launches": int(nl)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    srv.close()
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config in ("batch", "serve"):
+        dist, rank, local, ws = dist_init()
+        (main_batch if args.config == "batch" else main_serve)(args, dist, rank, local, ws)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     dist, rank, local, ws = dist_init()
     from vfs_v3p2_gb300 import capi
     case = make_case(args)

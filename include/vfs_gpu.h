@@ -59,6 +59,7 @@ typedef struct vfs_ctx vfs_ctx;
 typedef struct {
   int device;                           /* CUDA device ordinal */
   unsigned long long hbm_budget_bytes;  /* 0 = no limit; grids beyond it are refused */
+  int max_inflight;                     /* serving: requests in flight at once (0 = 16) */
 } vfs_config;
 
 typedef struct {
@@ -83,14 +84,21 @@ typedef struct {
   int orth;        /* Gram-Schmidt of the Arnoldi step: VFS_ORTH_CGS (one
                       classical pass, the reference's PETSc GMRES default) or
                       VFS_ORTH_CGS2 (classical with one re-orthogonalisation) */
+  int smooth_cols;  /* y-line smoother tile: i-columns per block, 0 (automatic: 32, fewer
+                       for long lines), 8, 16 or 32 */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every
  * row by aj, poisson.c:1560, with the RHS scaled alike).  Its residual r_s =
  * aj (b - A phi) is, cell by cell, the divergence the projection leaves
  * divided by dt st / coeff, so the solve stops when ||r_s|| <= rtol ||aj b||
- * and, when div_tol > 0, dt st / coeff * ||r_s|| <= div_tol, which bounds
- * max |div u| by div_tol. */
+ * and, when div_tol > 0, the masked max of dt st / coeff * |r_s| (the
+ * divergence the projection will leave) is at most div_tol.  A projection
+ * step then measures max |div u|; if the rounding of the flux update left it
+ * above div_tol, one more projection pass on the corrected fluxes removes the
+ * rest (at most two).  Where FP64 rounding keeps the masked max above the
+ * target (very small cells, large aj) the solve stops once another round no
+ * longer halves it and sets info.div_limited. */
 
 typedef struct {
   int iterations;  /* preconditioner applications */
@@ -98,6 +106,9 @@ typedef struct {
   double relres;   /* true ||aj (b - A phi)|| / ||aj b|| at exit */
   double bnorm;
   double time_ms;  /* device time of the solve */
+  int div_limited; /* 1: div_tol was not reachable (the masked residual max stopped
+                      falling: FP64 rounding floor of the grid) and the solve
+                      stopped at the rtol criterion */
 } vfs_solve_info;
 
 /* Context (device, streams, HBM budget). */
@@ -213,6 +224,45 @@ int vfs_mg_restrict(vfs_ctx* ctx, int grid, int level, const double* x, double* 
 int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y);
 /* One damped y-line Jacobi sweep on a level (FP64 aj-scaled operator). */
 int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x, double omega);
+
+/* ---- serving: continuous batching of projection steps ----
+ * A request is one projection step of one grid (the simulation stream's
+ * resident grid: MG hierarchy, pressure and phi stay on the device between
+ * its requests).  vfs_submit admits it at once if a slot is free, the grid
+ * has no request in flight and the grid's solver memory fits the HBM budget
+ * (it is reserved at admission); its inputs and right-hand side go to the
+ * device immediately and its iterations interleave with those of every other
+ * request in flight, each on its grid's stream.  vfs_poll advances all of
+ * them and returns finished ones.  Host buffers must stay valid until the
+ * request's result is returned; page-locked buffers (vfs_host_register) keep
+ * the copies asynchronous. */
+typedef struct {
+  int grid;
+  const double* ucont_in;   /* host AoS U* [mz][my][mx][3], or NULL: the resident U* */
+  double* ucont_out;        /* host AoS corrected fluxes, or NULL (they stay resident) */
+  const double* p_in;       /* host pressure, or NULL: the resident pressure */
+  double* p_out;            /* host pressure after the update, or NULL */
+  double dt, st, coeff;
+  vfs_solve_params params;  /* warm_start = 1: start from the grid's resident phi */
+} vfs_request;
+
+typedef struct {
+  long long ticket;
+  int status;               /* VFS_OK or the request's error code */
+  vfs_solve_info info;
+  double divmax;            /* max |div u| after the projection */
+} vfs_result;
+
+/* VFS_ERR_BUSY: no free slot or the grid is busy (retry after a poll);
+ * VFS_ERR_NOMEM: the grid's solver memory does not fit the budget now. */
+int vfs_submit(vfs_ctx* ctx, const vfs_request* req, long long* ticket);
+/* Advances every request in flight; VFS_OK with one finished result in *out,
+ * VFS_ERR_BUSY if none has finished yet (wait = 0; wait = 1 blocks until one
+ * has), VFS_ERR_STATE if nothing is in flight. */
+int vfs_poll(vfs_ctx* ctx, int wait, vfs_result* out);
+int vfs_inflight(vfs_ctx* ctx);
+/* Device memory the context holds and its budget (0 = none), in bytes. */
+int vfs_memory(vfs_ctx* ctx, unsigned long long* used, unsigned long long* budget);
 
 /* ---- batched solves (many uneven grids, one graph launch per iteration) ---- */
 /* Runs vfs_projection_step (resident U*, pressure and fluxes stay resident)

@@ -79,3 +79,31 @@ def test_batch_per_grid_parameters(gpu_ctx):
     finally:
         for gid in ids:
             gpu_ctx.grid_destroy(gid)
+
+
+def test_smoother_tile_does_not_change_results(gpu_ctx):
+    """The y-line smoother's tile (i-columns per block) only regroups
+    independent column solves: every tile gives the same bits."""
+    c = _cases()[1]
+    gid = _load(gpu_ctx, [c])[0]
+    try:
+        out = []
+        for cols in (0, 8, 16, 32):
+            _reset(gpu_ctx, gid, c)
+            info, dm = gpu_ctx.projection_step(gid, capi.default_params(rtol=1e-9, div_tol=1e-8, smooth_cols=cols))
+            out.append((info["iterations"], dm, _fields(gpu_ctx, gid, c)[0]))
+        for it, dm, phi in out[1:]:
+            assert it == out[0][0] and dm == out[0][1] and np.array_equal(phi, out[0][2])
+    finally:
+        gpu_ctx.grid_destroy(gid)
+
+
+def test_autotune_picks_a_converging_candidate(gpu_ctx):
+    from vfs_v3p2_gb300 import autotune
+    cases = _cases()[:2]
+    base = capi.default_params(rtol=1e-9, div_tol=1e-8)
+    plist, table = autotune.tuned_params(gpu_ctx, cases, base, steps=1)
+    assert len(plist) == 2 and all(autotune.size_class(c) in table for c in cases)
+    for e in table.values():
+        assert (e["nu1"], e["nu2"], e["omega"], e["smooth_cols"]) in autotune.CANDIDATES
+        assert 0 < e["ms_per_step"] < float("inf")

@@ -1,0 +1,62 @@
+"""Serving (continuous batching through vfs_submit / vfs_poll).
+
+Each request's result must be the same whether it runs alone (one request
+in flight at a time) or in the mix (all streams' requests in flight
+together, iterations interleaved on the device): same iterations, same
+max |div u| and the same pressure bit for bit, since every request's kernels
+and their order on its grid's stream are unchanged by the interleaving.
+Warm starts chain each stream's requests, so the per-stream order matters
+and the loop keeps it.  A small HBM budget forces grid eviction and
+re-admission; every request must still complete with max |div u| < 1e-8."""
+import pytest
+
+from vfs_v3p2_gb300 import capi, serve
+
+pytestmark = pytest.mark.gpu
+
+
+def _streams():
+    return serve.serving_streams(n_streams=4, lo=(16, 16, 16), hi=(48, 32, 32), seed=41)
+
+
+def _arrivals(n=14, n_streams=4):
+    # all at t = 0, streams interleaved (deterministic)
+    return [(0.0, (3 * q + q // 4) % n_streams) for q in range(n)]
+
+
+def _run(ctx, streams, arrivals):
+    params = capi.default_params(rtol=1e-9, div_tol=1e-8, warm_start=1)
+    srv = serve.Server(ctx, streams, params)
+    try:
+        recs, _ = srv.run(arrivals, keep_outputs=True)
+    finally:
+        srv.close()
+    return recs
+
+
+def test_alone_equals_mix():
+    arrivals = _arrivals()
+    with capi.Context(0, max_inflight=1) as ctx:
+        alone = _run(ctx, _streams(), arrivals)
+    with capi.Context(0, max_inflight=16) as ctx:
+        mix = _run(ctx, _streams(), arrivals)
+    # the mix really overlapped: some request was admitted before an earlier one finished
+    assert any(b["admitted"] < a["done"] for a in mix for b in mix if b is not a and b["arrival"] >= a["arrival"])
+    for q, (a, b) in enumerate(zip(alone, mix)):
+        assert a["status"] == 0 and b["status"] == 0
+        assert a["iterations"] == b["iterations"], (q, a["iterations"], b["iterations"])
+        assert a["divmax"] == b["divmax"] and a["divmax"] < 1e-8
+        assert (a["p"] == b["p"]).all(), q
+
+
+def test_budget_eviction_and_readmission():
+    streams = _streams()
+    params = capi.default_params(rtol=1e-9, div_tol=1e-8, warm_start=1)
+    with capi.Context(0) as probe:
+        srv = serve.Server(probe, streams, params)
+        need = sorted(srv._estimate(s) for s in streams)
+        srv.close()
+    budget = need[-1] + need[-2] + 1  # room for two resident grids
+    with capi.Context(0, hbm_budget_bytes=budget) as ctx:
+        recs = _run(ctx, streams, _arrivals())
+    assert all(r["status"] == 0 and r["divmax"] < 1e-8 for r in recs)

@@ -1,0 +1,107 @@
+"""Autotuner for the batched and served solves.
+
+Picks, per grid-size class, the smoothing schedule (pre/post y-line sweeps,
+damping) and the smoother's block tile (i-columns per block) by timing full
+projection steps on one representative grid of the class: each candidate is
+run once to warm up (graph capture) and then timed over a few steps with
+U* resident; the fastest candidate whose steps all converge to the requested
+max |div u| wins.  Results are cached per class in a JSON file so that a
+batch or a serving run tunes each class once.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import capi
+
+# (nu1, nu2, omega, smooth_cols); smooth_cols 0 = the kernel's own choice
+CANDIDATES = [
+    (2, 2, 0.8, 0), (3, 3, 0.9, 0), (2, 4, 0.9, 0), (4, 4, 0.9, 0), (3, 3, 0.85, 0),
+    (3, 3, 0.9, 16), (4, 4, 0.9, 16), (1, 3, 0.9, 0),
+]
+
+
+def size_class(case) -> str:
+    """log2 of the interior cell count (rounded) and whether a body is present."""
+    g = case.grid
+    cells = g.ni * g.nj * g.nk
+    body = bool((g.nvert > 0.1).any())
+    return f"c{int(round(math.log2(cells)))}{'_ib' if body else ''}"
+
+
+def _time_candidate(ctx, gid, case, params, steps):
+    shp = case.grid.nvert.shape
+    ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
+    ctx.set_field(gid, capi.FIELD_P, np.zeros(shp))
+    info, dm = ctx.projection_step(gid, params)  # warm-up: graph capture
+    if not info["converged"]:
+        return math.inf
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        info, dm = ctx.projection_step(gid, params)
+        if not info["converged"] or (params.div_tol > 0 and dm > params.div_tol):
+            return math.inf
+    return (time.perf_counter() - t0) / steps
+
+
+def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3):
+    """Best (nu1, nu2, omega, smooth_cols) for one grid and its seconds/step."""
+    g = case.grid
+    gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    try:
+        ctx.poisson_lhs(gid)
+        best, best_t = None, math.inf
+        for cand in candidates:
+            p = capi.SolveParams()
+            ctypes_copy(p, base)
+            p.nu1, p.nu2, p.omega, p.smooth_cols = cand
+            try:
+                t = _time_candidate(ctx, gid, case, p, steps)
+            except capi.VfsError:
+                t = math.inf
+            if t < best_t:
+                best, best_t = cand, t
+        return best, best_t
+    finally:
+        ctx.grid_destroy(gid)
+
+
+def ctypes_copy(dst, src):
+    for name, _ in src._fields_:
+        setattr(dst, name, getattr(src, name))
+
+
+def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = None, steps=3):
+    """Per-case SolveParams: each size class is tuned once (on its median-size
+    member) and cached in cache_path (JSON) if given."""
+    cache = {}
+    if cache_path and os.path.exists(cache_path):
+        with open(cache_path) as f:
+            cache = json.load(f)
+    classes = {}
+    for q, c in enumerate(cases):
+        classes.setdefault(size_class(c), []).append(q)
+    for key, members in classes.items():
+        if key in cache:
+            continue
+        cells = sorted(members, key=lambda q: cases[q].grid.ni * cases[q].grid.nj * cases[q].grid.nk)
+        rep = cases[cells[len(cells) // 2]]
+        cand, t = tune_case(ctx, rep, base, steps=steps)
+        cache[key] = {"nu1": cand[0], "nu2": cand[1], "omega": cand[2], "smooth_cols": cand[3],
+                      "ms_per_step": t * 1e3, "grid": rep.name}
+    if cache_path:
+        with open(cache_path, "w") as f:
+            json.dump(cache, f, indent=1, sort_keys=True)
+    out = []
+    for c in cases:
+        e = cache[size_class(c)]
+        p = capi.SolveParams()
+        ctypes_copy(p, base)
+        p.nu1, p.nu2, p.omega, p.smooth_cols = e["nu1"], e["nu2"], e["omega"], e["smooth_cols"]
+        out.append(p)
+    return out, cache

@@ -46,7 +46,7 @@ class VfsError(RuntimeError):
 
 
 class Config(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_ulonglong)]
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_ulonglong), ("max_inflight", ctypes.c_int)]
 
 
 class GridDesc(ctypes.Structure):
@@ -61,16 +61,27 @@ class SolveParams(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
                 ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
-                ("orth", ctypes.c_int)]
+                ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("relres", ctypes.c_double),
-                ("bnorm", ctypes.c_double), ("time_ms", ctypes.c_double)]
+                ("bnorm", ctypes.c_double), ("time_ms", ctypes.c_double), ("div_limited", ctypes.c_int)]
 
     def as_dict(self):
         return dict(iterations=self.iterations, converged=bool(self.converged), relres=self.relres,
-                    bnorm=self.bnorm, time_ms=self.time_ms)
+                    bnorm=self.bnorm, time_ms=self.time_ms, div_limited=bool(self.div_limited))
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_int), ("ucont_in", ctypes.c_void_p), ("ucont_out", ctypes.c_void_p),
+                ("p_in", ctypes.c_void_p), ("p_out", ctypes.c_void_p), ("dt", ctypes.c_double), ("st", ctypes.c_double),
+                ("coeff", ctypes.c_double), ("params", SolveParams)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_longlong), ("status", ctypes.c_int), ("info", SolveInfo),
+                ("divmax", ctypes.c_double)]
 
 
 # Every symbol include/vfs_gpu.h declares, with its ctypes signature.
@@ -112,6 +123,10 @@ SIGNATURES = {
     "vfs_projection_step_batch": ([_P, _I, _IP, _D, _D, _D, ctypes.POINTER(SolveParams), _I,
                                    ctypes.POINTER(SolveInfo), _DP], _I),
     "vfs_sync": ([_P], _I),
+    "vfs_submit": ([_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_longlong)], _I),
+    "vfs_poll": ([_P, _I, ctypes.POINTER(Result)], _I),
+    "vfs_inflight": ([_P], _I),
+    "vfs_memory": ([_P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)], _I),
     "vfs_probe_begin": ([_P, _I], _I),
     "vfs_probe_end": ([_P, ctypes.POINTER(ctypes.c_ulonglong), _DP, _DP], _I),
     "vfs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], _I),
@@ -177,9 +192,9 @@ def default_params(**kw) -> SolveParams:
 class Context:
     """One vfs_ctx (a device and its resident grids)."""
 
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, max_inflight: int = 0):
         self.L = load()
-        cfg = Config(device, hbm_budget_bytes)
+        cfg = Config(device, hbm_budget_bytes, max_inflight)
         h = _P()
         rc = self.L.vfs_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc:
@@ -307,6 +322,36 @@ class Context:
 
     def sync(self):
         self.check(self.L.vfs_sync(self.h))
+
+    # ---- serving ----
+    def submit(self, grid: int, params: SolveParams, ucont_in=0, ucont_out=0, p_in=0, p_out=0, dt=0.04, st=1.0,
+               coeff=1.0):
+        # Admit one projection step (host buffers as raw addresses, 0 = resident).
+        # Returns the ticket, or None when no slot is free or the grid is busy.
+        req = Request(grid, ucont_in or None, ucont_out or None, p_in or None, p_out or None, dt, st, coeff, params)
+        t = ctypes.c_longlong()
+        rc = self.L.vfs_submit(self.h, ctypes.byref(req), ctypes.byref(t))
+        if rc == VFS_ERR_BUSY:
+            return None
+        self.check(rc)
+        return t.value
+
+    def poll(self, wait: bool = False):
+        # One finished request as (ticket, status, info, divmax), or None.
+        r = Result()
+        rc = self.L.vfs_poll(self.h, 1 if wait else 0, ctypes.byref(r))
+        if rc in (VFS_ERR_BUSY, VFS_ERR_STATE):
+            return None
+        self.check(rc)
+        return r.ticket, r.status, r.info.as_dict(), r.divmax
+
+    def inflight(self) -> int:
+        return self.L.vfs_inflight(self.h)
+
+    def memory(self):
+        u, b = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        self.check(self.L.vfs_memory(self.h, ctypes.byref(u), ctypes.byref(b)))
+        return u.value, b.value
 
     def mark(self, g: int, slot: int):
         self.check(self.L.vfs_mark(self.h, g, slot))

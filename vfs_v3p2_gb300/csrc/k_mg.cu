@@ -305,15 +305,15 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
 }
 
 template <typename T>
-static int smooth_tw(int ni, int nj) {
-  int tw = VFS_SMOOTH_TWMAX;
+static int smooth_tw(int ni, int nj, int cols) {
+  int tw = cols > 0 ? cols : VFS_SMOOTH_TWMAX;
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   return tw;
 }
 
 template <typename T>
-int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
+int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -321,7 +321,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
-  const int tw = smooth_tw<T>(ni, nj);
+  const int tw = smooth_tw<T>(ni, nj, cols);
   const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
   if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
@@ -615,7 +615,7 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
 
 #define INST(T)                                                                                                        \
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
-  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t);                 \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int);            \
   template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
   template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const T*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -137,7 +138,7 @@ struct Grid {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
-  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1;
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -148,9 +149,14 @@ struct Grid {
 
 }  // namespace
 
+struct vfs_job_box;  // a serving request (defined with the solve jobs)
+
 struct vfs_ctx {
   int device = 0;
   cudaStream_t s0 = nullptr;  // batch stream (ticks of the batch graph)
+  int max_inflight = 16;      // serving slots
+  long long next_ticket = 1;
+  std::map<long long, std::unique_ptr<vfs_job_box>> inflight;  // serving requests by ticket
   std::vector<cudaEvent_t> marks;  // vfs_mark slots
   size_t budget = 0, used = 0;
   std::map<int, Grid*> grids;
@@ -285,6 +291,7 @@ int ensure_krylov(vfs_ctx* ctx, Grid& g, int m, int prec) {
 struct MGCfg {
   int nu1, nu2, ncoarse;
   double omega, omega_c;
+  int cols;  // smoother columns per block (0 = automatic)
 };
 
 int popcount(unsigned m) {
@@ -297,9 +304,10 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // A full smoothing sweep (x != 0) streams the active coefficient slots, x,
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
-void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, cudaStream_t s) {
+void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, int cols,
+                   cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
-  int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s);
+  int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s, cols);
   if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 4));
   dbg("smooth", l, rc, s);
 }
@@ -328,7 +336,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     T* cur = nullptr;
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      launch_smooth<T>(A, lf_of<T>(L), cur, b, o, (T)c.omega_c, s);
+      launch_smooth<T>(A, lf_of<T>(L), cur, b, o, (T)c.omega_c, s, c.cols);
       cur = o;
     }
     return cur;
@@ -337,7 +345,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   T* cur = nullptr;
   for (; q < c.nu1; q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, s);
+    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
   }
   Level& C = g.lev[l - 1];
@@ -353,7 +361,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   for (int r = 0; r < c.nu2; r++, q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, s);
+    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
   }
   return cur;
@@ -366,6 +374,7 @@ MGCfg mgcfg(const vfs_solve_params& p) {
   c.ncoarse = 32;
   c.omega = p.omega;
   c.omega_c = p.omega;
+  c.cols = p.smooth_cols;
   return c;
 }
 
@@ -516,7 +525,7 @@ template <typename T>
 int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphExec_t* out) {
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
-      g.ig_orth == p.orth) {
+      g.ig_orth == p.orth && g.ig_cols == p.smooth_cols) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -540,6 +549,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_nu2 = p.nu2;
   g.ig_omega = p.omega;
   g.ig_orth = p.orth;
+  g.ig_cols = p.smooth_cols;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -615,6 +625,8 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
+  if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
+    return fail(ctx, VFS_ERR_ARG, "smooth_cols must be 0 (automatic), 8, 16 or 32");
   return VFS_OK;
 }
 
@@ -650,8 +662,8 @@ struct Job {
   double* u_out = nullptr;       // host AoS corrected fluxes (with post)
   double* p_out = nullptr;       // host pressure (with post)
   double dt = 0.04, st = 1., coeff = 1.;
-  int phase = J_START, round = 0, iters = 0;
-  double atol = 0., rmax_tol = 0.;
+  int phase = J_START, round = 0, iters = 0, refine = 0;
+  double atol = 0., rmax_tol = 0., prev_rmax = 0.;
   vfs_solve_info info{};
   double divmax = 0.;
   int rc = VFS_OK;
@@ -660,6 +672,14 @@ struct Job {
   long long ticket = 0;
   bool mixed() const { return p.precision == VFS_MIXED; }
 };
+
+}  // namespace
+
+struct vfs_job_box {
+  Job job;
+};
+
+namespace {
 
 int job_fail(vfs_ctx* ctx, Job& J, int rc) {
   J.rc = rc;
@@ -687,6 +707,7 @@ int job_start(vfs_ctx* ctx, Job& J) {
     step_pre(g, J.dt, J.st, J.coeff);
   }
   J.rmax_tol = J.p.div_tol > 0. ? J.p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
+  J.prev_rmax = 0.;
   J.atol = initial_atol(g, J.p);
   J.pr = J.p;
   J.f = Fgmres{&g, &J.pr};
@@ -728,7 +749,11 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
   J.iters += h.it;
   const bool rel_ok = rn <= J.p.rtol * h.bnorm * 1.0000001 || h.bnorm == 0.;
   const bool div_ok = J.p.div_tol <= 0. || rmax <= J.rmax_tol;
-  if ((rel_ok && div_ok) || J.iters >= J.p.maxit || h.bnorm == 0. || J.round == 7) {
+  // a finish round that no longer halves the masked max has met the FP64
+  // rounding floor of this grid: the divergence target is out of reach
+  const bool floor = !div_ok && J.round > 0 && rmax > 0.5 * J.prev_rmax;
+  J.prev_rmax = rmax;
+  if ((rel_ok && (div_ok || floor)) || J.iters >= J.p.maxit || h.bnorm == 0. || J.round == 7) {
     cudaStream_t s = g.s;
     Level& F = g.lev[g.L - 1];
     const size_t N = ncell(g.d);
@@ -746,7 +771,8 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     }
     CK(cudaEventRecord(g.ev_done, s));
     J.info.iterations = J.iters;
-    J.info.converged = rel_ok && div_ok;
+    J.info.converged = rel_ok && (div_ok || floor);
+    J.info.div_limited = (!div_ok && floor) ? 1 : 0;
     J.info.bnorm = h.bnorm;
     J.info.relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
     J.phase = J_POST;
@@ -763,13 +789,32 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
   return VFS_OK;
 }
 
+// The step's outputs arrived.  The residual test bounds the divergence the
+// projection leaves up to the rounding of the flux update; when the measured
+// max |div u| still exceeds div_tol (and the grid is not at its rounding
+// floor), one more projection pass on the corrected fluxes removes the rest:
+// RHS of the corrected U, a solve from zero, pressure update and projection
+// (the pressure accumulates both passes, as one tighter solve would).
+template <typename T>
 int job_post_eval(vfs_ctx* ctx, Job& J) {
-  (void)ctx;
   Grid& g = *J.g;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, g.t0, g.t1);
   J.info.time_ms = ms;
   if (J.post) J.divmax = g.hv[2];
+  if (J.post && J.p.div_tol > 0. && J.divmax > J.p.div_tol && !J.info.div_limited && J.refine < 2 &&
+      J.iters < J.p.maxit) {
+    J.refine++;
+    step_pre(g, J.dt, J.st, J.coeff);
+    J.round = 0;
+    J.prev_rmax = 0.;
+    J.pr.maxit = J.p.maxit - J.iters;
+    const int r = fg_start<T>(ctx, J.f, J.atol, false);
+    if (r) return job_fail(ctx, J, r);
+    J.phase = J_ITER;
+    J.pending = true;
+    return VFS_OK;
+  }
   J.phase = J_DONE;
   return VFS_OK;
 }
@@ -801,7 +846,7 @@ int job_advance(vfs_ctx* ctx, Job& J) {
       const cudaError_t e = cudaEventQuery(g.ev_done);
       if (e == cudaErrorNotReady) return 0;
       if (e != cudaSuccess) return job_fail(ctx, J, cuda_fail(ctx, e, "post")), 1;
-      job_post_eval(ctx, J);
+      job_post_eval<T>(ctx, J);
       return 1;
     }
     default:
@@ -1026,6 +1071,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->warm_start = 0;
   p->div_tol = 0.;
   p->orth = VFS_ORTH_CGS;
+  p->smooth_cols = 0;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -1039,6 +1085,7 @@ int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
   vfs_ctx* ctx = new vfs_ctx();
   ctx->device = cfg ? cfg->device : 0;
   ctx->budget = cfg ? (size_t)cfg->hbm_budget_bytes : 0;
+  ctx->max_inflight = (cfg && cfg->max_inflight > 0) ? cfg->max_inflight : 16;
   if (ctx->device < 0 || ctx->device >= ndev) {
     delete ctx;
     return VFS_ERR_ARG;
@@ -1055,6 +1102,7 @@ void vfs_destroy(vfs_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   for (auto& e : ctx->marks) cudaEventDestroy(e);
+  ctx->inflight.clear();  // grid_free below waits for each grid's stream
   for (auto& kv : ctx->grids) grid_free(ctx, kv.second);
   ctx->grids.clear();
   if (ctx->s0) cudaStreamDestroy(ctx->s0);
@@ -1212,6 +1260,7 @@ int vfs_grid_destroy(vfs_ctx* ctx, int grid) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* g = get_grid(ctx, grid);
   if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (g->busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
   grid_free(ctx, g);
   ctx->grids.erase(grid);
   return VFS_OK;
@@ -1538,6 +1587,81 @@ int vfs_projection_step_batch(vfs_ctx* ctx, int n, const int* grids, double dt, 
   }
   if (rc) fail(ctx, rc, "a solve of the batch stopped at maxit above rtol");
   return rc;
+}
+
+int vfs_submit(vfs_ctx* ctx, const vfs_request* req, long long* ticket) {
+  if (!ctx || !req || !ticket) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, req->grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  Grid& g = *gp;
+  int r = check_params(ctx, &req->params);
+  if (r) return r;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before a request");
+  if (!(req->dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
+  if (g.m && req->params.restart > g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow");
+  if (g.busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
+  if ((int)ctx->inflight.size() >= ctx->max_inflight) return fail(ctx, VFS_ERR_BUSY, "all request slots are in use");
+  // admission against the HBM budget: the grid's solver memory is reserved now
+  r = req->params.precision == VFS_MIXED ? ensure_mg<float>(ctx, g) : ensure_mg<double>(ctx, g);
+  if (!r) r = ensure_krylov(ctx, g, req->params.restart, req->params.precision);
+  if (r) return r;
+  auto box = std::make_unique<vfs_job_box>();
+  Job& J = box->job;
+  J.g = &g;
+  J.p = req->params;
+  J.pre = J.post = true;
+  J.u_in = req->ucont_in;
+  J.u_out = req->ucont_out;
+  J.p_in = req->p_in;
+  J.p_out = req->p_out;
+  J.dt = req->dt;
+  J.st = req->st;
+  J.coeff = req->coeff;
+  J.ticket = ctx->next_ticket++;
+  g.busy = J.ticket;
+  job_advance_any(ctx, J);  // inputs and right-hand side go to the device now
+  *ticket = J.ticket;
+  ctx->inflight[J.ticket] = std::move(box);
+  return VFS_OK;
+}
+
+int vfs_poll(vfs_ctx* ctx, int wait, vfs_result* out) {
+  if (!ctx || !out) return VFS_ERR_ARG;
+  for (;;) {
+    for (auto it = ctx->inflight.begin(); it != ctx->inflight.end(); ++it) {
+      Job& J = it->second->job;
+      if (J.phase != J_DONE) continue;
+      out->ticket = J.ticket;
+      out->status = J.rc ? J.rc : (J.info.converged ? VFS_OK : VFS_ERR_NOTCONV);
+      out->info = J.info;
+      out->divmax = J.divmax;
+      if (J.rc) ctx->err = J.err;
+      J.g->busy = 0;
+      ctx->inflight.erase(it);
+      return VFS_OK;
+    }
+    if (ctx->inflight.empty()) return fail(ctx, VFS_ERR_STATE, "no request in flight");
+    std::vector<Job*> js;
+    for (auto& kv : ctx->inflight) js.push_back(&kv.second->job);
+    int moved = 0;
+    bool done = false;
+    for (Job* J : js) {
+      moved += job_advance_any(ctx, *J);
+      done = done || J->phase == J_DONE;
+    }
+    if (done) continue;
+    if (!wait) return VFS_ERR_BUSY;
+    if (!moved) wait_any(js);
+  }
+}
+
+int vfs_inflight(vfs_ctx* ctx) { return ctx ? (int)ctx->inflight.size() : 0; }
+
+int vfs_memory(vfs_ctx* ctx, unsigned long long* used, unsigned long long* budget) {
+  if (!ctx) return VFS_ERR_ARG;
+  if (used) *used = ctx->used;
+  if (budget) *budget = ctx->budget;
+  return VFS_OK;
 }
 
 int vfs_probe_begin(vfs_ctx* ctx, int kernel) {

@@ -41,7 +41,8 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0;
 // lf = precomputed y-line Thomas pivots 1/m_j (N of T)
 template <typename T>
-int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s);
+int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s,
+                 int cols = 0);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
 // fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc.

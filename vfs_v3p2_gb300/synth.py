@@ -293,6 +293,15 @@ def _round8(v):
     return max(8, int(round(v / 8.0)) * 8)
 
 
+def mg_levels(ni: int, nj: int, nk: int, max_levels: int = 5, min_cells: int = 4) -> int:
+    """Deepest geometric hierarchy (full coarsening) for which every axis
+    halves evenly down to the coarsest level and keeps >= min_cells cells."""
+    levels = 1
+    while levels < max_levels and all(n % (1 << levels) == 0 and n >> levels >= min_cells for n in (ni, nj, nk)):
+        levels += 1
+    return levels
+
+
 def c4_batch(count: int = 64, seed: int = 1004, lo=(32, 32, 32), hi=(192, 96, 96)):
     """Uneven batch: per-axis log-uniform extents in [lo, hi] rounded to a
     multiple of 8, skew U[0, 0.1], beta U[1.5, 3], 0-3 spheres r U[0.1, 0.3],
@@ -309,9 +318,7 @@ def c4_batch(count: int = 64, seed: int = 1004, lo=(32, 32, 32), hi=(192, 96, 96
             rad = rng.uniform(0.1, 0.3)
             sph.append((rng.uniform(1.0, 2 * math.pi - 1.0), rng.uniform(-0.5, 0.5), rng.uniform(0.6, math.pi - 0.6), rad))
         ni, nj, nk = ext
-        levels = 1
-        while levels < 5 and min(ni, nj, nk) % (1 << levels) == 0 and min(ni, nj, nk) >> levels >= 4:
-            levels += 1
+        levels = mg_levels(ni, nj, nk)
         cases.append(channel_case(ni, nj, nk, seed=1_000_000 + r, beta=beta, skew=skew, spheres=sph, levels=levels,
                                   name=f"batch{r}_{ni}x{nj}x{nk}"))
     return cases
