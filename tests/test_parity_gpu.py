@@ -176,9 +176,10 @@ def test_rhs_flux_projection_divergence(gpu_ctx, loaded):
 
 
 def test_projection_fractional_nvert_bitexact(gpu_ctx):
-    """Non-integer nvert values take the FP64 pair tests of the projection
-    (integer ones the byte path); both must reproduce the reference's
-    branch choices, so the corrected fluxes are bit-exact either way."""
+    """Non-integer nvert values take the FP64 nvert tests of the projection,
+    the IB flux balance and the divergence check (integer ones the byte
+    path); both must reproduce the reference's branch choices, so the
+    corrected fluxes and the divergence maximum are bit-exact either way."""
     case = synth.channel_case(32, 16, 16, seed=15, spheres=[(math.pi, 0.0, math.pi / 2, 0.6)], sigma=0.5, levels=3)
     g = case.grid
     nv = g.nvert * 0.35  # 0, 0.35 (IB band) and 1.4 (solid)
@@ -195,7 +196,16 @@ def test_projection_fractional_nvert_bitexact(gpu_ctx):
     gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
     gpu_ctx.L.vfs_set_field(gpu_ctx.h, gid, capi.FIELD_PHI, capi.dptr(phi))
     gpu_ctx.projection(gid)
-    assert np.array_equal(gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape), u_ref)
+    u_got = gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape)
+    assert np.array_equal(u_got, u_ref)
+    assert gpu_ctx.divergence_max(gid) == O.divergence(d, u_ref, O.metric(M, d, "aj"), nv)
+    # IB flux balance (mode 1) with fractional nvert
+    u2 = case.ucont.copy()
+    fa = O.volume_flux(d, 1, u2, nv, M)
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, case.ucont)
+    fa_g = gpu_ctx.volume_flux(gid)
+    assert np.allclose(fa_g, fa, rtol=1e-12, atol=1e-13 * abs(fa[0]))
+    assert np.abs(gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape) - u2).max() <= 1e-14 * np.abs(u2).max()
     gpu_ctx.grid_destroy(gid)
 
 

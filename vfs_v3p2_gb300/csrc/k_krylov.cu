@@ -51,6 +51,12 @@ __global__ void k_norm_finish(KrylovState* st, const double* __restrict__ parts,
   double s = 0.;
   for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[p];
   s = block_sum(s, sh);
+  if (!is_b) {  // clear the Hessenberg matrix and g with the whole block
+    const int m = st->m;
+    for (int q = threadIdx.x; q <= m; q += blockDim.x) st->g[q] = 0.;
+    for (int q = threadIdx.x; q < (m + 1) * m; q += blockDim.x) st->H[q] = 0.;
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     double nrm = sqrt(s);
     if (is_b) {
@@ -61,9 +67,7 @@ __global__ void k_norm_finish(KrylovState* st, const double* __restrict__ parts,
     } else {
       st->beta = nrm;
       st->resid = nrm;
-      for (int q = 0; q <= st->m; q++) st->g[q] = 0.;
       st->g[0] = nrm;
-      for (int q = 0; q < (st->m + 1) * st->m; q++) st->H[q] = 0.;
       st->j = 0;
       st->inv_hn = nrm > 0. ? 1. / nrm : 0.;
       st->vs[0] = 1.;  // V_0 is stored normalised

@@ -144,9 +144,13 @@ __device__ __forceinline__ double nrm3(const double* v, size_t c) {
   return sqrt(v[3 * c] * v[3 * c] + v[3 * c + 1] * v[3 * c + 1] + v[3 * c + 2] * v[3 * c + 2]);
 }
 
+// nb8 (nvert as bytes, every value an integer in [0, 127]) turns the FP64
+// interface tests into exact integer ones: nv < 0.1 <=> 0, nv > 0.1 <=> >= 1,
+// 0.1 < nv < 1.1 <=> 1.
 __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont u, const double* __restrict__ nv,
                                               const double* __restrict__ csi, const double* __restrict__ eta,
-                                              const double* __restrict__ zet, const double* __restrict__ fa, double* parts) {
+                                              const double* __restrict__ zet, const double* __restrict__ fa, double* parts,
+                                              const uint8_t* __restrict__ nb8) {
   __shared__ double sh[32];
   const double eps = 1.e-10, ibmval = 1.1;
   double flux = 0., area = 0.;
@@ -165,8 +169,15 @@ __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont
     for (int f = 0; f < 3; f++) {
       double* uu = uf[f];
       if (mode == 1) {
-        const bool plus = nv[c] < 0.1 && nv[nb[f]] > 0.1 && nv[nb[f]] < ibmval && lim1[f];
-        const bool minus = nv[c] > 0.1 && nv[c] < ibmval && nv[nb[f]] < 0.1 && lim1[f];
+        bool plus, minus;
+        if (nb8) {
+          const int a = nb8[c], b = nb8[nb[f]];
+          plus = a == 0 && b == 1 && lim1[f];
+          minus = a == 1 && b == 0 && lim1[f];
+        } else {
+          plus = nv[c] < 0.1 && nv[nb[f]] > 0.1 && nv[nb[f]] < ibmval && lim1[f];
+          minus = nv[c] > 0.1 && nv[c] < ibmval && nv[nb[f]] < 0.1 && lim1[f];
+        }
         if (!(plus || minus)) continue;
         if (phase == 0) {
           if (fabs(uu[c]) > eps) {
@@ -183,8 +194,15 @@ __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont
           area += nrm3(mt[f], c);
         }
       } else {
-        const bool plus = nv[c] < VFS_THR && nv[nb[f]] > VFS_THR && lim0[f];
-        const bool minus = nv[c] > VFS_THR && nv[nb[f]] < VFS_THR && lim0[f];
+        bool plus, minus;
+        if (nb8) {
+          const int a = nb8[c], b = nb8[nb[f]];
+          plus = a == 0 && b != 0 && lim0[f];
+          minus = a != 0 && b == 0 && lim0[f];
+        } else {
+          plus = nv[c] < VFS_THR && nv[nb[f]] > VFS_THR && lim0[f];
+          minus = nv[c] > VFS_THR && nv[nb[f]] < VFS_THR && lim0[f];
+        }
         if (!(plus || minus)) continue;
         if (phase == 1) {
           uu[c] = 0.;
@@ -203,14 +221,14 @@ __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont
   }
 }
 int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nvert, const double* M, double* parts,
-                       double* fa4, cudaStream_t s) {
+                       double* fa4, cudaStream_t s, const uint8_t* nb8) {
   const size_t N = ncell(d);
   const int nb = nblk(N, RB);
   const double *csi = M + N * MP_CSI, *eta = M + N * MP_ETA, *zet = M + N * MP_ZET;
-  k_vflux<<<nb, RB, 0, s>>>(d, mode, 0, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 0, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
   k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4); ++g_launches;
-  k_vflux<<<nb, RB, 0, s>>>(d, mode, 1, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
-  k_vflux<<<nb, RB, 0, s>>>(d, mode, 2, u, nvert, csi, eta, zet, fa4, parts); ++g_launches;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 1, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
+  k_vflux<<<nb, RB, 0, s>>>(d, mode, 2, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
   k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4 + 2); ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -536,28 +554,41 @@ int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, c
 
 // Divergence (main.c:1279-1349): max over cells of |div U| * aj, 0 where the
 // cell or a face neighbour carries nvert.
+// Cell c or one of its six face neighbours carries nvert (the reference's
+// sum > 0.1 test).  With nb8 (every nvert an integer in [0, 127]) the sum of
+// non-negative integers exceeds 0.1 exactly when one of them is nonzero, an
+// integer or of the bytes.
+__device__ __forceinline__ bool near_body(const Dims& d, const double* __restrict__ nvert,
+                                          const uint8_t* __restrict__ nb8, size_t c, int i, int j, int k) {
+  if (nb8)
+    return (nb8[c] | nb8[cidx(d, i, j, k + 1)] | nb8[cidx(d, i, j, k - 1)] | nb8[cidx(d, i, j + 1, k)] |
+            nb8[cidx(d, i, j - 1, k)] | nb8[cidx(d, i + 1, j, k)] | nb8[cidx(d, i - 1, j, k)]) != 0;
+  return nvert[c] + nvert[cidx(d, i, j, k + 1)] + nvert[cidx(d, i, j, k - 1)] + nvert[cidx(d, i, j + 1, k)] +
+             nvert[cidx(d, i, j - 1, k)] + nvert[cidx(d, i + 1, j, k)] + nvert[cidx(d, i - 1, j, k)] >
+         0.1;
+}
+
 __global__ void __launch_bounds__(RB) k_divergence(Dims d, Ucont u, const double* __restrict__ aj,
-                                                   const double* __restrict__ nvert, double* parts) {
+                                                   const double* __restrict__ nvert, double* parts,
+                                                   const uint8_t* __restrict__ nb8 = nullptr) {
   __shared__ double sh[32];
   double mxv = 0.;
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     if (!interior(d, i, j, k)) continue;
     const size_t c = _t;
-    double v = fabs((u.x[c] - u.x[cidx(d, i - 1, j, k)] + u.y[c] - u.y[cidx(d, i, j - 1, k)] + u.z[c] -
-                     u.z[cidx(d, i, j, k - 1)]) * aj[c]);
-    if (nvert[c] + nvert[cidx(d, i, j, k + 1)] + nvert[cidx(d, i, j, k - 1)] + nvert[cidx(d, i, j + 1, k)] +
-            nvert[cidx(d, i, j - 1, k)] + nvert[cidx(d, i + 1, j, k)] + nvert[cidx(d, i - 1, j, k)] > 0.1)
-      v = 0.;
+    if (near_body(d, nvert, nb8, c, i, j, k)) continue;
+    const double v = fabs((u.x[c] - u.x[cidx(d, i - 1, j, k)] + u.y[c] - u.y[cidx(d, i, j - 1, k)] + u.z[c] -
+                           u.z[cidx(d, i, j, k - 1)]) * aj[c]);
     mxv = fmax(mxv, v);
   }
   mxv = block_max(mxv, sh);
   if (threadIdx.x == 0) parts[blockIdx.x] = mxv;
 }
 int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
-                      cudaStream_t s) {
+                      cudaStream_t s, const uint8_t* nb8) {
   const int nb = nblk(ncell(d), RB);
-  k_divergence<<<nb, RB, 0, s>>>(d, u, aj, nvert, parts); ++g_launches;
+  k_divergence<<<nb, RB, 0, s>>>(d, u, aj, nvert, parts, nb8); ++g_launches;
   k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -566,24 +597,23 @@ int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const dou
 // cell and its six face neighbours free of nvert): with st = 1 the projection
 // leaves div u = dt / coeff * r there for the aj-scaled residual r.
 __global__ void __launch_bounds__(RB) k_masked_absmax(Dims d, const double* __restrict__ r, const double* __restrict__ nvert,
-                                                      double* parts) {
+                                                      double* parts, const uint8_t* __restrict__ nb8) {
   __shared__ double sh[32];
   double mxv = 0.;
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     if (!interior(d, i, j, k)) continue;
     const size_t c = _t;
-    if (nvert[c] + nvert[cidx(d, i, j, k + 1)] + nvert[cidx(d, i, j, k - 1)] + nvert[cidx(d, i, j + 1, k)] +
-            nvert[cidx(d, i, j - 1, k)] + nvert[cidx(d, i + 1, j, k)] + nvert[cidx(d, i - 1, j, k)] > 0.1)
-      continue;
+    if (near_body(d, nvert, nb8, c, i, j, k)) continue;
     mxv = fmax(mxv, fabs(r[c]));
   }
   mxv = block_max(mxv, sh);
   if (threadIdx.x == 0) parts[blockIdx.x] = mxv;
 }
-int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s) {
+int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s,
+                         const uint8_t* nb8) {
   const int nb = nblk(ncell(d), RB);
-  k_masked_absmax<<<nb, RB, 0, s>>>(d, r, nvert, parts); ++g_launches;
+  k_masked_absmax<<<nb, RB, 0, s>>>(d, r, nvert, parts, nb8); ++g_launches;
   k_finish_max<<<1, 256, 0, s>>>(parts, nb, out); ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -727,7 +727,7 @@ int job_check_enqueue(vfs_ctx* ctx, Job& J) {
   Level& F = g.lev[g.L - 1];
   dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
   dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
-  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s), s);
+  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s, g.nb8), s);
   CK(cudaMemcpyAsync(g.hk, g.st, sizeof(KrylovState), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(g.hv, g.scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(g.ev_chk, s));
@@ -1393,7 +1393,7 @@ int vfs_volume_flux(vfs_ctx* ctx, int grid, double out[4]) {
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
-  launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s);
+  launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8);
   if (out) CK(cudaMemcpyAsync(out, g.scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
   CK(cudaStreamSynchronize(g.s));
   return VFS_OK;
@@ -1482,7 +1482,7 @@ int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out) {
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
-  launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s);
+  launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8);
   CK(cudaMemcpyAsync(out, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, g.s));
   CK(cudaStreamSynchronize(g.s));
   return VFS_OK;
@@ -1499,7 +1499,7 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
   g.dt = dt;
   g.st_ = st;
   g.coeff = coeff;
-  dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s), g.s);
+  dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8), g.s);
   dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s), g.s);
 }
 // After the solve: pressure, projection, Contra2Cart, divergence.
@@ -1508,7 +1508,7 @@ void step_post(Grid& g, double dt, double st, double coeff) {
   dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
   dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
   dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
-  dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s), g.s);
+  dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8), g.s);
 }
 
 }  // namespace

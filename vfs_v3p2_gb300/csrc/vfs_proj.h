@@ -20,7 +20,8 @@ int launch_soa2aos(size_t n, const double* x, const double* y, const double* z, 
 int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, double st, double coeff, int meanfix,
                double* b, double* parts, double* sc, cudaStream_t s);
 int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nvert, const double* M, double* parts,
-                       double* fa4, cudaStream_t s);
+                       double* fa4, cudaStream_t s,
+                       const uint8_t* nb8 = nullptr);
 int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s);
 int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStream_t s);
 int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s);
@@ -37,9 +38,11 @@ int launch_inverse_metric(const Dims& d, const double* M, const double* nvert, d
 // allocation); returns 0, 1 (argument) or 2 (CUDA) and sets *why on error.
 int divergence_max_static(int device, const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* out,
                           cudaStream_t s, const char** why);
-int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s);
+int launch_masked_absmax(const Dims& d, const double* r, const double* nvert, double* parts, double* out, cudaStream_t s,
+                         const uint8_t* nb8 = nullptr);
 int launch_divergence(const Dims& d, const Ucont& u, const double* aj, const double* nvert, double* parts, double* out,
-                      cudaStream_t s);
+                      cudaStream_t s,
+                      const uint8_t* nb8 = nullptr);
 
 // ---- FGMRES device state (k_krylov.cu) ----
 // One flexible GMRES(m) solve keeps all of its scalars on the device so an
