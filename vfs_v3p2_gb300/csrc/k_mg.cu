@@ -220,6 +220,12 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_TWMAX
 #define VFS_SMOOTH_TWMAX 32  // columns per block
 #endif
+#ifndef VFS_SMOOTH_PF
+#define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off)
+#endif
+#ifndef VFS_SMOOTH_CARVE
+#define VFS_SMOOTH_CARVE -1  // preferred shared-memory carveout in percent (-1: the driver's choice)
+#endif
 
 template <unsigned MASK, typename T>
 __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
@@ -237,6 +243,38 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
   constexpr int U = VFS_SMOOTH_U;
+  // L2 prefetch of the rows a warp will stream VFS_SMOOTH_PF iterations
+  // later: the loads in flight are bounded by registers (4 bytes each), the
+  // prefetches are not, so they keep more of HBM's latency-bandwidth product
+  // busy.  One lane per 128-byte line: the 11 coefficient slots' (or MASK's)
+  // row, b, 1/m and the x rows of planes k-1, k, k+1 (a row of TW floats
+  // starting at i0 spans two lines).  Every prefetched line lies inside its
+  // array: the element offset is clamped to [0, N - 32].
+  auto prefetch_row = [&](int jrow) {
+    if (VFS_SMOOTH_PF <= 0 || jrow > d.my - 2) return;
+    const int lane = threadIdx.x & 31;
+    const int q = lane >> 1;  // stream index
+    constexpr int NS = __builtin_popcount(MASK);
+    int m = -1;
+    for (int s = 0, n = 0; s < 19; s++)
+      if (MASK & (1u << s)) {
+        if (n == q) m = s;
+        n++;
+      }
+    const T* base = nullptr;
+    int shift = 0;
+    if (m >= 0) base = A.coef + (size_t)m * N;
+    else if (q == NS) base = b;
+    else if (q == NS + 1) base = lf;
+    else if (xi && q <= NS + 4) {
+      base = xi;
+      shift = (q == NS + 3) ? -d.mx * d.my : (q == NS + 4) ? d.mx * d.my : 0;
+    }
+    if (!base) return;
+    int e = k * d.mx * d.my + jrow * d.mx + i0 + shift + (lane & 1) * 32;
+    e = max(0, min(e, N - 32));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + e));
+  };
   // Phase 1 in batches of U cells per thread: every load of the batch is
   // issued before any arithmetic (all addresses are interior cells: columns
   // past the last one are clamped onto it and discarded; non-fluid rows have
@@ -245,6 +283,8 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
   // b and only CP, SP, NP of the stencil are loaded.
   for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
+    if (VFS_SMOOTH_PF > 0 && sizeof(T) == 4 && TW == 32)
+      prefetch_row(1 + (base + VFS_SMOOTH_PF * U * VFS_SMOOTH_NT) / TW);
     T cv[U][19], xv[U][19], bb[U], inv[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -318,6 +358,10 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   if (!attr) {
     cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_smooth<MASK_ALL, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (VFS_SMOOTH_CARVE >= 0) {
+      cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
+      cudaFuncSetAttribute(k_smooth<MASK_ALL, T>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
+    }
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
