@@ -39,6 +39,7 @@ extern "C" {
 #define VFS_ERR_STATE 5    /* call order (e.g. solve before the LHS) */
 #define VFS_ERR_NUMERIC 6  /* NaN or Inf in the right-hand side or iterates */
 #define VFS_ERR_BUSY 7     /* serving: no free slot or memory right now */
+#define VFS_ERR_IO 8       /* file missing, unreadable, truncated or not a PETSc Vec */
 
 #define VFS_FP64 0   /* plain: FP64 multigrid inside FP64 FGMRES */
 #define VFS_MIXED 1  /* FP32 multigrid (FP32 coefficients) inside FP64 FGMRES */
@@ -201,6 +202,27 @@ int vfs_divergence_max_noalloc(int device, int mx, int my, int mz, int i_periodi
  * p_inout (nullable): host pressure in and out.  divmax (nullable). */
 int vfs_projection_step(vfs_ctx* ctx, int grid, double* ucont_inout, double* p_inout, double dt, double st,
                         double coeff, const vfs_solve_params* p, vfs_solve_info* info, double* divmax);
+
+/* ---- moving bodies and deforming grids ----
+ * New nvert (IB cells moved; the reference rebuilds its LHS then,
+ * poisson_hypre.c:628-648) or new node coordinates (moving or deforming
+ * grid): the coarse masks and nodes, the metrics of every level, the
+ * restriction weights and the inverse metric are rebuilt on the device
+ * from the host array ([mz][my][mx] / [mz][my][mx][3]); the grid then needs
+ * vfs_poisson_lhs again before its next solve.  Resident U*, p and phi are
+ * kept. */
+int vfs_grid_update_nvert(vfs_ctx* ctx, int grid, const double* nvert);
+int vfs_grid_update_coords(vfs_ctx* ctx, int grid, const double* coor);
+
+/* ---- PETSc binary Vec files ----
+ * The reference's field files (vfield/pfield/nvfield/ufield, VecView and
+ * VecLoad, main.c:291-330): int32 class id 1211214, int32 length n, then n
+ * IEEE doubles, all big-endian.  A DMDA vector is stored in natural ordering,
+ * which is this ABI's host layout ([mz][my][mx], Cmpnts as 3 consecutive
+ * doubles).  read: out == NULL only returns the file's length in *n_file;
+ * otherwise n must equal it.  Host only (no context, no device). */
+int vfs_petsc_vec_read(const char* path, double* out, long long n, long long* n_file);
+int vfs_petsc_vec_write(const char* path, const double* in, long long n);
 
 /* ---- test and introspection hooks (same arithmetic as the hot path) ---- */
 /* metric pack of a level: 43 * N doubles (csi eta zet aj icsi ieta izet iaj

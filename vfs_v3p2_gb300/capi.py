@@ -35,7 +35,8 @@ FIELD_UCAT = 4
 FIELD_NVERT = 5
 FIELD_USTAR = 6
 
-ERRNAMES = {1: "VFS_ERR_ARG", 2: "VFS_ERR_CUDA", 3: "VFS_ERR_NOMEM", 4: "VFS_ERR_NOTCONV", 5: "VFS_ERR_STATE",
+VFS_ERR_IO = 8
+ERRNAMES = {8: "VFS_ERR_IO", 1: "VFS_ERR_ARG", 2: "VFS_ERR_CUDA", 3: "VFS_ERR_NOMEM", 4: "VFS_ERR_NOTCONV", 5: "VFS_ERR_STATE",
             6: "VFS_ERR_NUMERIC", 7: "VFS_ERR_BUSY"}
 
 
@@ -123,6 +124,10 @@ SIGNATURES = {
     "vfs_projection_step_batch": ([_P, _I, _IP, _D, _D, _D, ctypes.POINTER(SolveParams), _I,
                                    ctypes.POINTER(SolveInfo), _DP], _I),
     "vfs_sync": ([_P], _I),
+    "vfs_grid_update_nvert": ([_P, _I, _DP], _I),
+    "vfs_grid_update_coords": ([_P, _I, _DP], _I),
+    "vfs_petsc_vec_read": ([ctypes.c_char_p, _DP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "vfs_petsc_vec_write": ([ctypes.c_char_p, _DP, ctypes.c_longlong], _I),
     "vfs_submit": ([_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_longlong)], _I),
     "vfs_poll": ([_P, _I, ctypes.POINTER(Result)], _I),
     "vfs_inflight": ([_P], _I),
@@ -380,6 +385,12 @@ class Context:
         self.L.vfs_host_unregister(a.ctypes.data_as(_P))
 
     # -- hooks --
+    def update_nvert(self, g: int, nvert: np.ndarray):
+        self.check(self.L.vfs_grid_update_nvert(self.h, g, dptr(np.ascontiguousarray(nvert, dtype=np.float64))))
+
+    def update_coords(self, g: int, coor: np.ndarray):
+        self.check(self.L.vfs_grid_update_coords(self.h, g, dptr(np.ascontiguousarray(coor, dtype=np.float64))))
+
     def metrics(self, g: int, level: int) -> np.ndarray:
         mx, my, mz = self.level_dims(g, level)
         out = np.zeros(43 * mx * my * mz)
@@ -427,3 +438,25 @@ class Context:
         self.check(self.L.vfs_mg_smooth(self.h, g, level, dptr(np.ascontiguousarray(b, dtype=np.float64)), dptr(x),
                                         omega))
         return x
+
+
+def petsc_vec_read(path: str) -> np.ndarray:
+    """A PETSc binary Vec file (the reference's field files) as a float64 array."""
+    L = load()
+    n = ctypes.c_longlong()
+    rc = L.vfs_petsc_vec_read(path.encode(), None, 0, ctypes.byref(n))
+    if rc:
+        raise VfsError(rc, f"cannot read PETSc Vec header of {path}")
+    out = np.zeros(n.value)
+    rc = L.vfs_petsc_vec_read(path.encode(), dptr(out), n.value, None)
+    if rc:
+        raise VfsError(rc, f"cannot read PETSc Vec {path}")
+    return out
+
+
+def petsc_vec_write(path: str, a: np.ndarray):
+    """Write a float64 array as a PETSc binary Vec file."""
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    rc = load().vfs_petsc_vec_write(path.encode(), dptr(a), a.size)
+    if rc:
+        raise VfsError(rc, f"cannot write PETSc Vec {path}")

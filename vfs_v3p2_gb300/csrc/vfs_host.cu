@@ -109,6 +109,8 @@ struct Grid {
   double* pd = nullptr;
   double* minv = nullptr;   // per-cell inverse metric (9, row-major), Contra2Cart
   uint8_t* nb8 = nullptr;   // nvert as bytes when all are integers in [0, 127], else null
+  uint8_t* nb8_buf = nullptr;  // storage behind nb8
+  double* mtmp = nullptr;   // metric formation scratch (9 N)
   double* u = nullptr;      // SoA Ucont: x | y | z
   double* ustar = nullptr;  // SoA resident U*
   double* p = nullptr;
@@ -1044,6 +1046,64 @@ int do_solve(vfs_ctx* ctx, Grid& g, const vfs_solve_params* p, vfs_solve_info* i
   return VFS_OK;
 }
 
+// Host-side nvert of the finest level: fluid count, the byte copy the
+// integer nvert tests use (when every value is an integer in [0, 127]), and
+// the upload.  The grid's other derived fields follow in grid_derive.
+int grid_set_nvert(vfs_ctx* ctx, Grid& g, const double* nvert) {
+  const Dims& d = g.d;
+  const size_t N = ncell(d);
+  g.nfluid = 0.;
+  for (int k = 1; k < d.mz - 1; k++)
+    for (int j = 1; j < d.my - 1; j++)
+      for (int i = 1; i < d.mx - 1; i++)
+        if (nvert[cidx(d, i, j, k)] < 0.1) g.nfluid += 1.;
+  std::vector<uint8_t> nbh(N);
+  bool integral = true;
+  for (size_t c = 0; c < N && integral; c++) {
+    const double v = nvert[c];
+    integral = v >= 0. && v <= 127. && v == (double)(int)v;
+    nbh[c] = integral ? (uint8_t)(int)v : 0;
+  }
+  Level& F = g.lev[g.L - 1];
+  CK(cudaMemcpyAsync(F.nvert, nvert, N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+  g.nb8 = nullptr;
+  if (integral) {
+    if (!g.nb8_buf) {
+      const int r = galloc(ctx, g, &g.nb8_buf, N);
+      if (r) return r;
+    }
+    CK(cudaMemcpyAsync(g.nb8_buf, nbh.data(), N, cudaMemcpyHostToDevice, g.s));
+    g.nb8 = g.nb8_buf;
+  }
+  // the host vector must outlive the copies
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
+// Everything derived from the finest coordinates and nvert: coarse nodes and
+// masks (every other node; MyNvertRestriction), the metrics of every level,
+// the restriction weights and the inverse metric.  The operator is rebuilt
+// by vfs_poisson_lhs.
+int grid_derive(vfs_ctx* ctx, Grid& g) {
+  const int L = g.L;
+  for (int l = L - 2; l >= 0; l--)
+    launch_coarsen(g.lev[l + 1].d, g.lev[l].d, g.si, g.sj, g.sk, g.lev[l + 1].coor, g.lev[l + 1].nvert, g.lev[l].coor,
+                   g.lev[l].nvert, g.s);
+  for (int l = 0; l < L; l++) launch_form_metrics(g.lev[l].d, g.lev[l].coor, g.lev[l].M, g.mtmp, g.s);
+  for (int l = 0; l < L; l++) launch_restrict_weights(g.lev[l].N, g.lev[l].nvert, g.lev[l].rw32, g.lev[l].rw64, g.s);
+  Level& F = g.lev[L - 1];
+  launch_inverse_metric(F.d, F.M, F.nvert, g.minv, g.s);
+  cudaError_t e = cudaStreamSynchronize(g.s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "grid setup");
+  // the operator and every captured iteration depend on these
+  g.lhs = false;
+  if (g.ig_exec) {
+    cudaGraphExecDestroy(g.ig_exec);
+    g.ig_exec = nullptr;
+  }
+  return VFS_OK;
+}
+
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
@@ -1220,36 +1280,13 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   GAB(g.aos, 3 * N);
   GAB(g.parts, (size_t)krylov_nblocks(N) * 72 + 4096);
   GAB(g.scal, 64);
-  for (int k = 1; k < d.mz - 1; k++)
-    for (int j = 1; j < d.my - 1; j++)
-      for (int i = 1; i < d.mx - 1; i++)
-        if (desc->nvert[cidx(d, i, j, k)] < 0.1) g.nfluid += 1.;
-  // integer nvert (the IB flags 0 / 1 / solid) lets the projection test
-  // nvert pairs with byte ors; any other value keeps the FP64 tests
-  std::vector<uint8_t> nbh(N);
-  bool integral = true;
-  for (size_t c = 0; c < N && integral; c++) {
-    const double v = desc->nvert[c];
-    integral = v >= 0. && v <= 127. && v == (double)(int)v;
-    nbh[c] = integral ? (uint8_t)(int)v : 0;
-  }
-  if (integral) {
-    GAB(g.nb8, N);
-    if (cudaMemcpyAsync(g.nb8, nbh.data(), N, cudaMemcpyHostToDevice, g.s) != cudaSuccess)
-      return bail(cuda_fail(ctx, cudaGetLastError(), "upload"));
-  }
+  g.mtmp = tmp;
   Level& F = g.lev[L - 1];
-  if (cudaMemcpyAsync(F.coor, desc->coor, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess ||
-      cudaMemcpyAsync(F.nvert, desc->nvert, N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess)
+  if (cudaMemcpyAsync(F.coor, desc->coor, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s) != cudaSuccess)
     return bail(cuda_fail(ctx, cudaGetLastError(), "upload"));
-  for (int l = L - 2; l >= 0; l--)
-    launch_coarsen(g.lev[l + 1].d, g.lev[l].d, g.si, g.sj, g.sk, g.lev[l + 1].coor, g.lev[l + 1].nvert, g.lev[l].coor,
-                   g.lev[l].nvert, g.s);
-  for (int l = 0; l < L; l++) launch_form_metrics(g.lev[l].d, g.lev[l].coor, g.lev[l].M, tmp, g.s);
-  for (int l = 0; l < L; l++) launch_restrict_weights(g.lev[l].N, g.lev[l].nvert, g.lev[l].rw32, g.lev[l].rw64, g.s);
-  launch_inverse_metric(F.d, F.M, F.nvert, g.minv, g.s);
-  cudaError_t e = cudaStreamSynchronize(g.s);
-  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "grid setup"));
+  r = grid_set_nvert(ctx, g, desc->nvert);
+  if (!r) r = grid_derive(ctx, g);
+  if (r) return bail(r);
   const int id = ctx->next_id++;
   ctx->grids[id] = gp;
   *grid_id = id;
@@ -1264,6 +1301,102 @@ int vfs_grid_destroy(vfs_ctx* ctx, int grid) {
   grid_free(ctx, g);
   ctx->grids.erase(grid);
   return VFS_OK;
+}
+
+int vfs_grid_update_nvert(vfs_ctx* ctx, int grid, const double* nvert) {
+  if (!ctx || !nvert) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (g->busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
+  CK(cudaSetDevice(ctx->device));
+  int r = grid_set_nvert(ctx, *g, nvert);
+  if (!r) r = grid_derive(ctx, *g);
+  return r;
+}
+
+int vfs_grid_update_coords(vfs_ctx* ctx, int grid, const double* coor) {
+  if (!ctx || !coor) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (g->busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
+  CK(cudaSetDevice(ctx->device));
+  Level& F = g->lev[g->L - 1];
+  CK(cudaMemcpyAsync(F.coor, coor, 3 * ncell(g->d) * sizeof(double), cudaMemcpyHostToDevice, g->s));
+  return grid_derive(ctx, *g);
+}
+
+namespace {
+constexpr int PETSC_VEC_CLASSID = 1211214;
+void put_be32(unsigned char* p, uint32_t v) {
+  for (int b = 0; b < 4; b++) p[b] = (unsigned char)(v >> (24 - 8 * b));
+}
+uint32_t get_be32(const unsigned char* p) {
+  uint32_t v = 0;
+  for (int b = 0; b < 4; b++) v = (v << 8) | p[b];
+  return v;
+}
+}  // namespace
+
+int vfs_petsc_vec_read(const char* path, double* out, long long n, long long* n_file) {
+  if (!path) return VFS_ERR_ARG;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return VFS_ERR_IO;
+  unsigned char hdr[8];
+  if (std::fread(hdr, 1, 8, f) != 8 || (int)get_be32(hdr) != PETSC_VEC_CLASSID) {
+    std::fclose(f);
+    return VFS_ERR_IO;
+  }
+  const long long len = (long long)(int32_t)get_be32(hdr + 4);
+  if (n_file) *n_file = len;
+  if (!out) {
+    std::fclose(f);
+    return len >= 0 ? VFS_OK : VFS_ERR_IO;
+  }
+  if (len != n) {
+    std::fclose(f);
+    return VFS_ERR_ARG;
+  }
+  std::vector<unsigned char> buf(1 << 20);
+  long long done = 0;
+  while (done < n) {
+    const size_t want = (size_t)std::min<long long>(n - done, (long long)(buf.size() / 8));
+    if (std::fread(buf.data(), 8, want, f) != want) {
+      std::fclose(f);
+      return VFS_ERR_IO;
+    }
+    for (size_t q = 0; q < want; q++) {
+      uint64_t v = 0;
+      for (int b = 0; b < 8; b++) v = (v << 8) | buf[8 * q + b];
+      std::memcpy(out + done + q, &v, 8);
+    }
+    done += (long long)want;
+  }
+  std::fclose(f);
+  return VFS_OK;
+}
+
+int vfs_petsc_vec_write(const char* path, const double* in, long long n) {
+  if (!path || (n > 0 && !in) || n < 0 || n > 2147483647LL) return VFS_ERR_ARG;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return VFS_ERR_IO;
+  unsigned char hdr[8];
+  put_be32(hdr, (uint32_t)PETSC_VEC_CLASSID);
+  put_be32(hdr + 4, (uint32_t)n);
+  bool ok = std::fwrite(hdr, 1, 8, f) == 8;
+  std::vector<unsigned char> buf(1 << 20);
+  long long done = 0;
+  while (ok && done < n) {
+    const size_t m = (size_t)std::min<long long>(n - done, (long long)(buf.size() / 8));
+    for (size_t q = 0; q < m; q++) {
+      uint64_t v;
+      std::memcpy(&v, in + done + q, 8);
+      for (int b = 0; b < 8; b++) buf[8 * q + b] = (unsigned char)(v >> (56 - 8 * b));
+    }
+    ok = std::fwrite(buf.data(), 8, m, f) == m;
+    done += (long long)m;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? VFS_OK : VFS_ERR_IO;
 }
 
 int vfs_grid_bytes(vfs_ctx* ctx, int grid, unsigned long long* bytes) {
@@ -1302,7 +1435,12 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
   // coarsest level: dense inverse of A + sigma e e^T when small enough
   Level& C = g.lev[0];
   const int n = (C.d.mx - 2) * (C.d.my - 2) * (C.d.mz - 2);
-  if (n <= DENSE_MAX && !C.Binv) {
+  if (g.ig_exec) {  // the slot set or the coarse solve may change
+    cudaGraphExecDestroy(g.ig_exec);
+    g.ig_exec = nullptr;
+  }
+  C.nco = 0;
+  if (n <= DENSE_MAX) {
     std::vector<double> cp(C.N);
     CK(cudaMemcpy(cp.data(), C.mcoef, C.N * sizeof(double), cudaMemcpyDeviceToHost));
     double sabs = 0.;
@@ -1320,8 +1458,8 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
       CK(cudaMalloc(&fac, (size_t)n * sizeof(double)));
       CK(cudaMalloc(&pval, sizeof(double)));
       CK(cudaMalloc(&piv, sizeof(int)));
-      int r = galloc(ctx, g, &C.Binv, (size_t)n * n);
-      if (!r) r = galloc(ctx, g, &C.Binv32, (size_t)n * n);
+      int r = C.Binv ? VFS_OK : galloc(ctx, g, &C.Binv, (size_t)n * n);
+      if (!r && !C.Binv32) r = galloc(ctx, g, &C.Binv32, (size_t)n * n);
       if (r) {
         cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv);
         return r;
