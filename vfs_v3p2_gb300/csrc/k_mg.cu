@@ -344,11 +344,17 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   }
 }
 
+// Columns per block: the requested tile (0 = automatic), narrowed while
+// three staged line arrays exceed 48 KB or the tile is twice the width of
+// the level; automatically also narrowed (down to 8) while the sweep has
+// fewer than 4 blocks per SM, so coarse levels keep the machine busy.
 template <typename T>
-static int smooth_tw(int ni, int nj, int cols) {
+static int smooth_tw(int ni, int nj, int nk, int cols) {
   int tw = cols > 0 ? cols : VFS_SMOOTH_TWMAX;
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
+  if (cols == 0)
+    while (tw > 8 && (size_t)((ni + tw - 1) / tw) * nk < 4 * 152) tw >>= 1;
   return tw;
 }
 
@@ -365,7 +371,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
-  const int tw = smooth_tw<T>(ni, nj, cols);
+  const int tw = smooth_tw<T>(ni, nj, nk, cols);
   const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
   if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
