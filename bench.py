@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--nu", type=int, default=3, help="pre- and post-smoothing sweeps")
     ap.add_argument("--nu1", type=int, default=None, help="pre-smoothing sweeps (overrides --nu)")
     ap.add_argument("--nu2", type=int, default=None, help="post-smoothing sweeps (overrides --nu)")
+    ap.add_argument("--nu-coarse", default="5,5",
+                    help="PRE,POST sweeps below the finest level of the single-grid workloads (-1,-1: as finest; "
+                         "measured 9 vs 10 iterations on the sphere workload)")
     ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
@@ -253,11 +256,6 @@ def main_batch(args, dist, rank, local, ws):
     cases = synth.c4_batch(64, seed=1004, lo=(32 // sc, 32 // sc, 32 // sc), hi=(192 // sc, 96 // sc, 96 // sc))
     ctx = capi.Context(local)
     base = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400, restart=args.restart)
-    tuned = None
-    if args.tune:
-        plist, tuned = autotune.tuned_params(ctx, cases, base)
-    else:
-        plist = base
     ids = []
     for c in cases:
         gid = ctx.grid_create(c.grid.coor, c.grid.nvert, c.levels, c.immersed)
@@ -265,6 +263,11 @@ def main_batch(args, dist, rank, local, ws):
         ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
         ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
         ids.append(gid)
+    tuned = None
+    if args.tune:
+        plist, tuned = autotune.tuned_params_batch(ctx, ids, cases, base)
+    else:
+        plist = base
     for _ in range(args.warmup):
         ctx.projection_step_batch(ids, plist)
     clk = Clocks(local)
@@ -368,10 +371,13 @@ def main():
     ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
     nu1 = args.nu if args.nu1 is None else args.nu1
     nu2 = args.nu if args.nu2 is None else args.nu2
+    nuc = [int(v) for v in args.nu_coarse.split(",")]
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
-                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega)
+                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                                nu1_coarse=nuc[0], nu2_coarse=nuc[1])
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
-                               div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega)
+                               div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                               nu1_coarse=nuc[0], nu2_coarse=nuc[1])
 
     def steps(params, K, base_slot):
         infos, divs = [], []
@@ -464,7 +470,7 @@ def main():
             "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
-                       "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2],
+                       "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
                        "restart": args.restart, "orth": args.orth, "omega": args.omega,
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,

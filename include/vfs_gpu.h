@@ -87,6 +87,11 @@ typedef struct {
                       VFS_ORTH_CGS2 (classical with one re-orthogonalisation) */
   int smooth_cols;  /* y-line smoother tile: i-columns per block, 0 (automatic: 32, fewer
                        for long lines), 8, 16 or 32 */
+  int nu1_coarse, nu2_coarse;  /* sweeps on the levels below the finest (-1, the
+                                  default: nu1 / nu2).  More coarse sweeps save
+                                  iterations on one large grid (5 / 5 on
+                                  256x128x128) but lengthen small grids' latency-
+                                  bound cycles in a batch */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

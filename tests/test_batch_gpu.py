@@ -105,5 +105,22 @@ def test_autotune_picks_a_converging_candidate(gpu_ctx):
     plist, table = autotune.tuned_params(gpu_ctx, cases, base, steps=1)
     assert len(plist) == 2 and all(autotune.size_class(c) in table for c in cases)
     for e in table.values():
-        assert (e["nu1"], e["nu2"], e["omega"], e["smooth_cols"]) in autotune.CANDIDATES
+        assert (e["nu1"], e["nu2"], e["omega"], e["smooth_cols"], e["nu_coarse"]) in autotune.CANDIDATES
         assert 0 < e["ms_per_step"] < float("inf")
+
+
+def test_autotune_batch_objective(gpu_ctx):
+    from vfs_v3p2_gb300 import autotune
+    cases = _cases()[:3]
+    ids = _load(gpu_ctx, cases)
+    try:
+        for gid, c in zip(ids, cases):
+            _reset(gpu_ctx, gid, c)
+        base = capi.default_params(rtol=1e-9, div_tol=1e-8)
+        plist, table = autotune.tuned_params_batch(gpu_ctx, ids, cases, base, steps=1)
+        assert len(plist) == 3 and all(p is not None for p in plist)
+        infos, dm = gpu_ctx.projection_step_batch(ids, plist)
+        assert all(i["converged"] for i in infos) and (dm < 1e-8).all()
+    finally:
+        for gid in ids:
+            gpu_ctx.grid_destroy(gid)

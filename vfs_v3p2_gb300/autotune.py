@@ -1,12 +1,19 @@
 """Autotuner for the batched and served solves.
 
-Picks, per grid-size class, the smoothing schedule (pre/post y-line sweeps,
-damping) and the smoother's block tile (i-columns per block) by timing full
-projection steps on one representative grid of the class: each candidate is
-run once to warm up (graph capture) and then timed over a few steps with
-U* resident; the fastest candidate whose steps all converge to the requested
-max |div u| wins.  Results are cached per class in a JSON file so that a
-batch or a serving run tunes each class once.
+Picks, per grid-size class, the smoothing schedule (pre/post y-line sweeps
+on the finest and on the coarser levels, damping) and the smoother's block
+tile (i-columns per block).  Each candidate is run once to warm up (graph
+capture) and then timed over a few steps with U* resident; the fastest
+candidate whose steps all converge to the requested max |div u| wins.
+
+Two objectives, matching how the grids will run:
+  tuned_params       one representative grid of the class alone (serving a
+                     single stream, latency);
+  tuned_params_batch all the class's grids together as one batch
+                     (vfs_projection_step_batch: throughput, where small
+                     grids' launch latencies overlap and total work counts).
+Results are cached per class in a JSON file so that a run tunes each class
+once.
 """
 from __future__ import annotations
 
@@ -19,10 +26,11 @@ import numpy as np
 
 from . import capi
 
-# (nu1, nu2, omega, smooth_cols); smooth_cols 0 = the kernel's own choice
+# (nu1, nu2, omega, smooth_cols, coarse sweeps); smooth_cols 0 = the kernel's
+# own choice; coarse sweeps -1 = as on the finest level
 CANDIDATES = [
-    (2, 2, 0.8, 0), (3, 3, 0.9, 0), (2, 4, 0.9, 0), (4, 4, 0.9, 0), (3, 3, 0.85, 0),
-    (3, 3, 0.9, 16), (4, 4, 0.9, 16), (1, 3, 0.9, 0),
+    (3, 3, 0.9, 0, 5), (3, 3, 0.9, 0, -1), (2, 2, 0.8, 0, 5), (2, 4, 0.9, 0, 5), (4, 4, 0.9, 0, 5),
+    (3, 3, 0.85, 0, 5), (3, 3, 0.9, 16, 5), (4, 4, 0.9, 16, 6), (2, 2, 0.9, 0, 4),
 ]
 
 
@@ -50,7 +58,7 @@ def _time_candidate(ctx, gid, case, params, steps):
 
 
 def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3):
-    """Best (nu1, nu2, omega, smooth_cols) for one grid and its seconds/step."""
+    """Best (nu1, nu2, omega, smooth_cols, coarse sweeps) for one grid and its seconds/step."""
     g = case.grid
     gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
     try:
@@ -59,7 +67,8 @@ def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3)
         for cand in candidates:
             p = capi.SolveParams()
             ctypes_copy(p, base)
-            p.nu1, p.nu2, p.omega, p.smooth_cols = cand
+            p.nu1, p.nu2, p.omega, p.smooth_cols = cand[:4]
+            p.nu1_coarse = p.nu2_coarse = cand[4]
             try:
                 t = _time_candidate(ctx, gid, case, p, steps)
             except capi.VfsError:
@@ -93,7 +102,7 @@ def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = No
         rep = cases[cells[len(cells) // 2]]
         cand, t = tune_case(ctx, rep, base, steps=steps)
         cache[key] = {"nu1": cand[0], "nu2": cand[1], "omega": cand[2], "smooth_cols": cand[3],
-                      "ms_per_step": t * 1e3, "grid": rep.name}
+                      "nu_coarse": cand[4], "ms_per_step": t * 1e3, "grid": rep.name}
     if cache_path:
         with open(cache_path, "w") as f:
             json.dump(cache, f, indent=1, sort_keys=True)
@@ -103,5 +112,53 @@ def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = No
         p = capi.SolveParams()
         ctypes_copy(p, base)
         p.nu1, p.nu2, p.omega, p.smooth_cols = e["nu1"], e["nu2"], e["omega"], e["smooth_cols"]
+        p.nu1_coarse = p.nu2_coarse = e["nu_coarse"]
         out.append(p)
     return out, cache
+
+
+def tuned_params_batch(ctx, ids, cases, base: capi.SolveParams, steps=2):
+    """Per-grid SolveParams for resident grids `ids` (created, LHS built,
+    U* set) that will run as one batch: each size class's grids are timed
+    together as a sub-batch for every candidate."""
+    classes = {}
+    for q, c in enumerate(cases):
+        classes.setdefault(size_class(c), []).append(q)
+    table, out = {}, [None] * len(cases)
+    for key, members in sorted(classes.items()):
+        sub = [ids[q] for q in members]
+        best, best_t = None, math.inf
+        for cand in CANDIDATES:
+            p = capi.SolveParams()
+            ctypes_copy(p, base)
+            p.nu1, p.nu2, p.omega, p.smooth_cols = cand[:4]
+            p.nu1_coarse = p.nu2_coarse = cand[4]
+            try:
+                _reset(ctx, sub, [cases[q] for q in members])
+                ctx.projection_step_batch(sub, p)  # warm-up: graph capture
+                t0 = time.perf_counter()
+                ok = True
+                for _ in range(steps):
+                    infos, dm = ctx.projection_step_batch(sub, p)
+                    ok = ok and all(i["converged"] for i in infos)
+                t = (time.perf_counter() - t0) / steps if ok else math.inf
+            except capi.VfsError:
+                t = math.inf
+            if t < best_t:
+                best, best_t = cand, t
+        table[key] = {"nu1": best[0], "nu2": best[1], "omega": best[2], "smooth_cols": best[3], "nu_coarse": best[4],
+                      "ms_per_batch_step": best_t * 1e3, "grids": len(members)}
+        for q in members:
+            p = capi.SolveParams()
+            ctypes_copy(p, base)
+            p.nu1, p.nu2, p.omega, p.smooth_cols = best[:4]
+            p.nu1_coarse = p.nu2_coarse = best[4]
+            out[q] = p
+    _reset(ctx, ids, cases)
+    return out, table
+
+
+def _reset(ctx, ids, cases):
+    for gid, c in zip(ids, cases):
+        ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
+        ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))

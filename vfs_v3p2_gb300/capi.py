@@ -62,7 +62,8 @@ class SolveParams(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("rtol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
                 ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
-                ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int)]
+                ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
+                ("nu2_coarse", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):

@@ -140,7 +140,7 @@ struct Grid {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
-  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1;
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -293,7 +293,11 @@ int ensure_krylov(vfs_ctx* ctx, Grid& g, int m, int prec) {
 struct MGCfg {
   int nu1, nu2, ncoarse;
   double omega, omega_c;
-  int cols;  // smoother columns per block (0 = automatic)
+  int cols;        // smoother columns per block (0 = automatic)
+  int nu1c, nu2c;  // sweeps on the levels below the finest
+  int top;         // index of the finest level
+  int pre(int l) const { return l == top ? nu1 : nu1c; }
+  int post(int l) const { return l == top ? nu2 : nu2c; }
 };
 
 int popcount(unsigned m) {
@@ -320,7 +324,7 @@ void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, 
 // needed to make the V-cycle's result always land in xa.
 int level_writes(const Grid& g, int l, const MGCfg& c) {
   if (l == 0) return g.lev[0].Binv ? 1 : c.ncoarse;
-  return c.nu1 + (c.nu1 == 0 ? 1 : 0) + c.nu2;
+  return c.pre(l) + (c.pre(l) == 0 ? 1 : 0) + c.post(l);
 }
 
 template <typename T>
@@ -345,7 +349,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   int q = 0;
   T* cur = nullptr;
-  for (; q < c.nu1; q++) {
+  for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
     smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
@@ -361,7 +365,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   } else {
     dbg("prolong_add", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s), s);
   }
-  for (int r = 0; r < c.nu2; r++, q++) {
+  for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
     smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
@@ -369,7 +373,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   return cur;
 }
 
-MGCfg mgcfg(const vfs_solve_params& p) {
+MGCfg mgcfg(const vfs_solve_params& p, int top) {
   MGCfg c;
   c.nu1 = p.nu1;
   c.nu2 = p.nu2;
@@ -377,6 +381,9 @@ MGCfg mgcfg(const vfs_solve_params& p) {
   c.omega = p.omega;
   c.omega_c = p.omega;
   c.cols = p.smooth_cols;
+  c.nu1c = p.nu1_coarse >= 0 ? p.nu1_coarse : p.nu1;
+  c.nu2c = p.nu2_coarse >= 0 ? p.nu2_coarse : p.nu2;
+  c.top = top;
   return c;
 }
 
@@ -388,7 +395,7 @@ int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T
   Level& F = g.lev[g.L - 1];
   T* bf = bbuf<T>(F);
   if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s), s);
-  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p), skip, s);
+  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p, g.L - 1), skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
 }
@@ -487,7 +494,7 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
-  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mgcfg(p), skip, s);
+  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mgcfg(p, g.L - 1), skip, s);
   {
     const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
     OpView<double> A{F.d, F.mcoef, F.mask, skip};
@@ -527,7 +534,7 @@ template <typename T>
 int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphExec_t* out) {
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
-      g.ig_orth == p.orth && g.ig_cols == p.smooth_cols) {
+      g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -552,6 +559,8 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_omega = p.omega;
   g.ig_orth = p.orth;
   g.ig_cols = p.smooth_cols;
+  g.ig_nu1c = p.nu1_coarse;
+  g.ig_nu2c = p.nu2_coarse;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -621,6 +630,11 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->restart < 1 || p->restart > MAXRESTART) return fail(ctx, VFS_ERR_ARG, "restart must be in [1, 64]");
   if (p->maxit < 1) return fail(ctx, VFS_ERR_ARG, "maxit must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 + p->nu2 < 1) return fail(ctx, VFS_ERR_ARG, "need at least one smoothing sweep");
+  {
+    const int a = p->nu1_coarse >= 0 ? p->nu1_coarse : p->nu1, b = p->nu2_coarse >= 0 ? p->nu2_coarse : p->nu2;
+    if (p->nu1_coarse < -1 || p->nu2_coarse < -1 || a + b < 1)
+      return fail(ctx, VFS_ERR_ARG, "nu1_coarse / nu2_coarse: -1 (as nu1 / nu2) or >= 0, at least one sweep");
+  }
   if (!(p->rtol > 0.)) return fail(ctx, VFS_ERR_ARG, "rtol must be > 0");
   if (!(p->omega > 0. && p->omega < 2.)) return fail(ctx, VFS_ERR_ARG, "omega must be in (0, 2)");
   if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
@@ -1132,6 +1146,8 @@ void vfs_default_params(vfs_solve_params* p) {
   p->div_tol = 0.;
   p->orth = VFS_ORTH_CGS;
   p->smooth_cols = 0;
+  p->nu1_coarse = -1;
+  p->nu2_coarse = -1;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
