@@ -61,6 +61,7 @@ def parse():
                     help="PRE,POST sweeps below the finest level of the single-grid workloads (-1,-1: as finest; "
                          "measured 9 vs 10 iterations on the sphere workload)")
     ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
+    ap.add_argument("--smooth-cols", type=int, default=0, help="smoother tile columns (0: automatic)")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -374,10 +375,10 @@ def main():
     nuc = [int(v) for v in args.nu_coarse.split(",")]
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
-                                nu1_coarse=nuc[0], nu2_coarse=nuc[1])
+                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
-                               nu1_coarse=nuc[0], nu2_coarse=nuc[1])
+                               nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
 
     def steps(params, K, base_slot):
         infos, divs = [], []

@@ -223,6 +223,9 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_PF
 #define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off)
 #endif
+#ifndef VFS_SMOOTH_U3
+#define VFS_SMOOTH_U3 8  // phase-3 (write) loop unroll
+#endif
 #ifndef VFS_SMOOTH_CARVE
 #define VFS_SMOOTH_CARVE -1  // preferred shared-memory carveout in percent (-1: the driver's choice)
 #endif
@@ -334,13 +337,17 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     }
   }
   __syncthreads();
+  // Phase 3, unrolled so that the old values of several cells are loaded
+  // together (columns past the last one are clamped and not stored).
+  constexpr int U3 = VFS_SMOOTH_U3;
+#pragma unroll U3
   for (int idx = threadIdx.x; idx < nt; idx += VFS_SMOOTH_NT) {
     const int il = idx % TW, jl = idx / TW;
-    const int i = i0 + il, j = 1 + jl;
-    if (i > d.mx - 2) continue;
+    const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
     const int c = k * d.mx * d.my + j * d.mx + i;
-    const T x0 = xi ? xi[c] : T(0);
-    xo[c] = x0 + omega * su[idx];
+    const T x0 = xi ? __ldg(xi + c) : T(0);
+    const T v = x0 + omega * su[idx];
+    if (i0 + il <= d.mx - 2) xo[c] = v;
   }
 }
 
