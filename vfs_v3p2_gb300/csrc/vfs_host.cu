@@ -134,6 +134,8 @@ struct Grid {
   double* hv = nullptr;     // pinned: ||r||, max |r|, max |div u|
   int epoch = 0;            // solve rounds started on this grid
   cudaEvent_t ev_chk = nullptr, ev_done = nullptr, ev_pend = nullptr;
+  cudaStream_t cs = nullptr;  // copy stream: host transfers that overlap the step
+  cudaEvent_t ev_pin = nullptr, ev_p = nullptr, ev_u = nullptr, ev_cs = nullptr;
   long long busy = 0;       // ticket of the request in flight on this grid (serving)
   cudaStream_t s = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -218,7 +220,12 @@ void grid_free(vfs_ctx* ctx, Grid* g) {
   if (g->hstat) cudaFreeHost(g->hstat);
   if (g->hk) cudaFreeHost(g->hk);
   if (g->hv) cudaFreeHost(g->hv);
-  for (cudaEvent_t e : {g->ev_chk, g->ev_done, g->ev_pend}) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : {g->ev_chk, g->ev_done, g->ev_pend, g->ev_pin, g->ev_p, g->ev_u, g->ev_cs})
+    if (e) cudaEventDestroy(e);
+  if (g->cs) {
+    cudaStreamSynchronize(g->cs);
+    cudaStreamDestroy(g->cs);
+  }
   for (auto& e : g->ev) if (e) cudaEventDestroy(e);
   if (g->t0) cudaEventDestroy(g->t0);
   if (g->t1) cudaEventDestroy(g->t1);
@@ -665,7 +672,8 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
 enum JobPhase { J_START = 0, J_ITER, J_CHECK, J_POST, J_DONE };
 
 void step_pre(Grid& g, double dt, double st, double coeff);
-void step_post(Grid& g, double dt, double st, double coeff);
+int step_post(Grid& g, double dt, double st, double coeff, double* u_out = nullptr, double* p_out = nullptr,
+              bool p_in_pending = false);
 
 struct Job {
   Grid* g = nullptr;
@@ -685,6 +693,7 @@ struct Job {
   int rc = VFS_OK;
   std::string err;
   bool pending = false;  // batch: work on the grid's stream since the last tick
+  bool p_in_pending = false;  // the pressure upload is on the copy stream
   long long ticket = 0;
   bool mixed() const { return p.precision == VFS_MIXED; }
 };
@@ -719,7 +728,11 @@ int job_start(vfs_ctx* ctx, Job& J) {
     } else {
       CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
     }
-    if (J.p_in) CK(cudaMemcpyAsync(g.p, J.p_in, N * sizeof(double), cudaMemcpyHostToDevice, g.s));
+    if (J.p_in) {  // needed only at the pressure update: upload during the solve
+      CK(cudaMemcpyAsync(g.p, J.p_in, N * sizeof(double), cudaMemcpyHostToDevice, g.cs));
+      CK(cudaEventRecord(g.ev_pin, g.cs));
+      J.p_in_pending = true;
+    }
     step_pre(g, J.dt, J.st, J.coeff);
   }
   J.rmax_tol = J.p.div_tol > 0. ? J.p.div_tol * g.coeff / (g.dt * g.st_) : 0.;
@@ -777,12 +790,9 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
     CK(cudaEventRecord(g.t1, s));
     if (J.post) {
-      step_post(g, J.dt, J.st, J.coeff);
-      if (J.u_out) {
-        launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, s);
-        CK(cudaMemcpyAsync(J.u_out, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
-      }
-      if (J.p_out) CK(cudaMemcpyAsync(J.p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+      const int rp = step_post(g, J.dt, J.st, J.coeff, J.u_out, J.p_out, J.p_in_pending);
+      J.p_in_pending = false;
+      if (rp) return job_fail(ctx, J, cuda_fail(ctx, (cudaError_t)rp, "step outputs"));
       CK(cudaMemcpyAsync(g.hv + 2, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
     }
     CK(cudaEventRecord(g.ev_done, s));
@@ -1251,6 +1261,9 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   cudaEventCreateWithFlags(&g.ev_chk, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&g.ev_done, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&g.ev_pend, cudaEventDisableTiming);
+  for (cudaEvent_t* e : {&g.ev_pin, &g.ev_p, &g.ev_u, &g.ev_cs}) cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+  if (cudaStreamCreateWithFlags(&g.cs, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(cuda_fail(ctx, cudaGetLastError(), "stream"));
   // level extents, finest = L-1
   g.lev[L - 1].d = d;
   for (int l = L - 2; l >= 0; l--) {
@@ -1657,12 +1670,40 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
   dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s), g.s);
 }
 // After the solve: pressure, projection, Contra2Cart, divergence.
-void step_post(Grid& g, double dt, double st, double coeff) {
+// Host outputs (nullable) leave on the grid's copy stream as soon as their
+// data is final: the pressure right after its update (overlapping the
+// projection), the corrected fluxes right after the projection (overlapping
+// Contra2Cart and the divergence check); the main stream then waits for the
+// copies.  p_in_pending: the pressure upload of the step (on the copy
+// stream, overlapping the solve) must land before the update.
+int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double* p_out, bool p_in_pending) {
   Level& F = g.lev[g.L - 1];
+  const size_t N = ncell(g.d);
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t r) {
+    if (r != cudaSuccess && e == cudaSuccess) e = r;
+  };
+  if (p_in_pending) ok(cudaStreamWaitEvent(g.s, g.ev_pin, 0));
   dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
+  if (p_out) {
+    ok(cudaEventRecord(g.ev_p, g.s));
+    ok(cudaStreamWaitEvent(g.cs, g.ev_p, 0));
+    ok(cudaMemcpyAsync(p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
+  }
   dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
+  if (u_out) {
+    ok(cudaEventRecord(g.ev_u, g.s));
+    ok(cudaStreamWaitEvent(g.cs, g.ev_u, 0));
+    launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, g.cs);
+    ok(cudaMemcpyAsync(u_out, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
+  }
   dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
   dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8), g.s);
+  if (p_out || u_out) {
+    ok(cudaEventRecord(g.ev_cs, g.cs));
+    ok(cudaStreamWaitEvent(g.s, g.ev_cs, 0));
+  }
+  return (int)e;
 }
 
 }  // namespace
