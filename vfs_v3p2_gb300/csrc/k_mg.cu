@@ -223,6 +223,9 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_PF
 #define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off)
 #endif
+#ifndef VFS_SMOOTH_MINBLK
+#define VFS_SMOOTH_MINBLK 152  // automatic tile: narrow while a sweep has fewer blocks (one per SM)
+#endif
 #ifndef VFS_SMOOTH_U3
 #define VFS_SMOOTH_U3 8  // phase-3 (write) loop unroll
 #endif
@@ -354,14 +357,15 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
 // Columns per block: the requested tile (0 = automatic), narrowed while
 // three staged line arrays exceed 48 KB or the tile is twice the width of
 // the level; automatically also narrowed (down to 8) while the sweep has
-// fewer than 4 blocks per SM, so coarse levels keep the machine busy.
+// fewer than VFS_SMOOTH_MINBLK blocks (one per SM), so small levels keep
+// the machine busy.
 template <typename T>
 static int smooth_tw(int ni, int nj, int nk, int cols) {
   int tw = cols > 0 ? cols : VFS_SMOOTH_TWMAX;
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   if (cols == 0)
-    while (tw > 8 && (size_t)((ni + tw - 1) / tw) * nk < 4 * 152) tw >>= 1;
+    while (tw > 8 && (size_t)((ni + tw - 1) / tw) * nk < VFS_SMOOTH_MINBLK) tw >>= 1;
   return tw;
 }
 
