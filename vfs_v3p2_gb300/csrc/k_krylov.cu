@@ -132,19 +132,21 @@ __global__ void __launch_bounds__(KB) k_multidot(const KrylovState* st, const do
 }
 
 // Sum the multi-dot partials into st->h (and accumulate the column in hacc).
+// One warp per dot (q = warp, warp + 8, ...): each lane sums a fixed stride
+// of the block partials, then the warp tree; no block barriers, and the
+// order is fixed, so the result is deterministic.
 __global__ void k_multidot_finish(KrylovState* st, const double* __restrict__ parts, int nparts, int nv, int ld, int pass) {
   if (is_done(st)) return;
   nv = nv_of(st, nv);
-  __shared__ double sh[32];
-  for (int q = 0; q < nv; q++) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int q = threadIdx.x >> 5; q < nv; q += nw) {
     double s = 0.;
-    for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[(size_t)p * ld + q];
-    s = block_sum(s, sh) * st->vs[q];
-    if (threadIdx.x == 0) {
+    for (int p = lane; p < nparts; p += 32) s += parts[(size_t)p * ld + q];
+    s = warp_sum(s) * st->vs[q];
+    if (lane == 0) {
       st->h[q] = s;
       st->hacc[q] = (pass == 1) ? s : st->hacc[q] + s;
     }
-    __syncthreads();
   }
 }
 
