@@ -62,6 +62,9 @@ def parse():
                          "measured 9 vs 10 iterations on the sphere workload)")
     ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
     ap.add_argument("--smooth-cols", type=int, default=0, help="smoother tile columns (0: automatic)")
+    ap.add_argument("--mg-half", type=int, default=1, choices=[0, 1],
+                    help="multigrid operator stored as FP16 normalised by its diagonal (1) or FP32 (0); "
+                         "FP32 arithmetic either way")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -83,6 +86,9 @@ def make_case(args):
         return synth.c3_terrain(args.scale)
     return synth.c2_sphere(args.scale)
 
+
+# storage of the FP32 multigrid's level operators (vfs_solve_params.mg_half)
+OPERATOR = {0: "fp32", 1: "fp16 diagonal-normalised, row sums kept (fp32 arithmetic)"}
 
 WORKLOAD = {
     "channel": "channel 64x64x64, tanh beta 2.0, skew 0.05 sin(z), no body, U ~ N(0,1) per face",
@@ -292,6 +298,7 @@ def main_batch(args, dist, rank, local, ws):
             "ms_per_step": 1e3 * total / args.steps, **base_line(args, ws),
             "config": {"workload": WORKLOAD["batch"], "grids": len(ids), "cells_total": int(cells),
                        "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": bool(args.tune),
+                       "mg_operator": OPERATOR[base.mg_half],
                        "timer": "host wall clock around synchronous batch calls (results on the host)",
                        "parallelism": f"replicas x{ws}"},
             "e2e": None, "iterations": {"mean": float(np.mean(its)), "max": int(max(its))}, "divmax": max(dms),
@@ -337,7 +344,8 @@ def main_serve(args, dist, rank, local, ws):
             "value": ws * summ["solves_per_s"], "unit": "solves/s", "steps": len(recs),
             "ms_per_step": 1e3 * wall / len(recs), **base_line(args, ws),
             "config": {"workload": WORKLOAD["serve"], "streams": 16, "rate_req_s": args.rate,
-                       "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16, "rtol": args.rtol,
+                       "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16,
+                       "mg_operator": OPERATOR[params.mg_half], "rtol": args.rtol,
                        "div_tol": args.div_tol, "timer": "host wall clock, first arrival to last result",
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * summ["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -375,7 +383,12 @@ def main():
     nuc = [int(v) for v in args.nu_coarse.split(",")]
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
-                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
+                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
+                                mg_half=args.mg_half)
+    other = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
+                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
+                                mg_half=1 - args.mg_half)
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
@@ -412,6 +425,15 @@ def main():
     ctx.probe_begin(capi.PROBE_SMOOTH)
     steps(mixed, min(args.steps, 5), 600)
     plaunch, pms, pbytes = ctx.probe_end()
+
+    # ---- the same mixed solve with the other multigrid operator storage ----
+    alt = None
+    if not args.no_fp64:
+        steps(other, 2, 700)
+        Ka = max(3, args.steps // 2)
+        ta, _, infa, diva = steps(other, Ka, 710)
+        alt = {"mg_operator": OPERATOR[other.mg_half], "value": ws * Ka / (allmax(dist, ta) / 1e3),
+               "iterations": statistics.mean(i["iterations"] for i in infa), "divmax": max(diva)}
 
     # ---- plain FP64 on the same grid ----
     fp64_rate, fp64_iters, fp64_div, mix_vs_fp64_err = None, None, None, None
@@ -451,8 +473,9 @@ def main():
 
     peak, peak_kind = measured_peak()
     achieved = (pbytes / plaunch) / ((pms / plaunch) / 1e3) / 1e9 if plaunch else None
-    traffic = ncu_traffic("k_smooth<float>:" + case.name)
-    roof = {"kernel": "k_smooth<float> (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
+    kname = "k_smooth<float, __half>" if args.mg_half else "k_smooth<float, float>"
+    traffic = ncu_traffic(kname + ":" + case.name)
+    roof = {"kernel": kname + " (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
             "traffic": traffic, "launches": plaunch, "avg_launch_ms": pms / plaunch if plaunch else None,
             "alg_bytes_per_launch": pbytes / plaunch if plaunch else None}
@@ -473,6 +496,7 @@ def main():
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
                        "restart": args.restart, "orth": args.orth, "omega": args.omega,
+                       "mg_operator": OPERATOR[args.mg_half],
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},
@@ -481,6 +505,7 @@ def main():
             "fp64": {"value": fp64_rate, "iterations": fp64_iters, "divmax": fp64_div,
                      "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
                      "phi_rel_l2_mixed_vs_fp64": mix_vs_fp64_err},
+            "mixed_other_operator": alt,
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl),
         }
         print(json.dumps(line), flush=True)

@@ -92,6 +92,12 @@ typedef struct {
                                   iterations on one large grid (5 / 5 on
                                   256x128x128) but lengthen small grids' latency-
                                   bound cycles in a batch */
+  int mg_half;  /* VFS_MIXED only: 1 (the default) = the multigrid levels'
+                   operator is stored as FP16 normalised by its diagonal,
+                   with an FP16 centre-slot correction that keeps every row
+                   sum (the arithmetic stays FP32; each smoothing sweep
+                   streams 38 instead of 60 bytes per cell); 0 = stored FP32.
+                   The FP64 FGMRES operator is the same either way. */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every
@@ -237,6 +243,12 @@ int vfs_get_metrics(vfs_ctx* ctx, int grid, int level, double* out);
  * operator on the finest level), 1 = aj-scaled FP64, 2 = aj-scaled FP32
  * (returned as doubles). */
 int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out);
+/* The FP16 diagonal-normalised multigrid operator of a level (mg_half):
+ * coef 19 * N values (slot m != 0: fp16(a_m / D); slot 0: the fp16 row-sum
+ * correction), lf N FP32 y-line pivots 1/m (0 on non-fluid rows), rw N FP32
+ * restriction weights max(0, 1 - nvert_f) D_f / D_c (level >= 1; zeros on
+ * level 0), all returned as doubles; any pointer may be null. */
+int vfs_get_mg_half(vfs_ctx* ctx, int grid, int level, double* coef, double* lf, double* rw);
 int vfs_get_level_dims(vfs_ctx* ctx, int grid, int level, int dims[3]);
 int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out);
 /* y = A x with the operator `which` (as vfs_get_coef) of a level; which 3 =

@@ -37,12 +37,13 @@ def _fields(ctx, gid, case):
             ctx.get_field(gid, capi.FIELD_UCONT, shp + (3,)))
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp32_operator", "fp64"])
 def test_batch_equals_one_at_a_time(gpu_ctx, precision):
     cases = _cases()
     ids = _load(gpu_ctx, cases)
     try:
-        params = capi.default_params(precision=precision, rtol=1e-9, div_tol=1e-8)
+        half = 0 if precision == "mixed_fp32_operator" else 1
+        params = capi.default_params(precision=precision.split("_")[0], rtol=1e-9, div_tol=1e-8, mg_half=half)
         for gid, c in zip(ids, cases):
             _reset(gpu_ctx, gid, c)
         infos, dm = gpu_ctx.projection_step_batch(ids, params)
@@ -81,7 +82,8 @@ def test_batch_per_grid_parameters(gpu_ctx):
             gpu_ctx.grid_destroy(gid)
 
 
-def test_smoother_tile_does_not_change_results(gpu_ctx):
+@pytest.mark.parametrize("half", [1, 0])
+def test_smoother_tile_does_not_change_results(gpu_ctx, half):
     """The y-line smoother's tile (i-columns per block) only regroups
     independent column solves: every tile gives the same bits."""
     c = _cases()[1]
@@ -90,7 +92,8 @@ def test_smoother_tile_does_not_change_results(gpu_ctx):
         out = []
         for cols in (0, 8, 16, 32):
             _reset(gpu_ctx, gid, c)
-            info, dm = gpu_ctx.projection_step(gid, capi.default_params(rtol=1e-9, div_tol=1e-8, smooth_cols=cols))
+            info, dm = gpu_ctx.projection_step(gid, capi.default_params(rtol=1e-9, div_tol=1e-8, smooth_cols=cols,
+                                                                        mg_half=half))
             out.append((info["iterations"], dm, _fields(gpu_ctx, gid, c)[0]))
         for it, dm, phi in out[1:]:
             assert it == out[0][0] and dm == out[0][1] and np.array_equal(phi, out[0][2])

@@ -63,7 +63,7 @@ class SolveParams(ctypes.Structure):
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
                 ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
                 ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
-                ("nu2_coarse", ctypes.c_int)]
+                ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -115,6 +115,7 @@ SIGNATURES = {
                              _DP], _I),
     "vfs_get_metrics": ([_P, _I, _I, _DP], _I),
     "vfs_get_coef": ([_P, _I, _I, _I, _DP], _I),
+    "vfs_get_mg_half": ([_P, _I, _I, _DP, _DP, _DP], _I),
     "vfs_get_level_dims": ([_P, _I, _I, _IP], _I),
     "vfs_get_level_nvert": ([_P, _I, _I, _DP], _I),
     "vfs_apply_op": ([_P, _I, _I, _I, _DP, _DP], _I),
@@ -403,6 +404,17 @@ class Context:
         out = np.zeros(19 * mx * my * mz)
         self.check(self.L.vfs_get_coef(self.h, g, level, which, dptr(out)))
         return out.reshape((19, mz, my, mx))
+
+    def mg_half(self, g: int, level: int):
+        """The FP16 diagonal-normalised multigrid operator of a level: the 19
+        slots (centre slot: the row-sum correction), the y-line pivots and the
+        restriction weights, as float64 arrays."""
+        mx, my, mz = self.level_dims(g, level)
+        coef = np.zeros((19, mz, my, mx))
+        lf = np.zeros((mz, my, mx))
+        rw = np.zeros((mz, my, mx))
+        self.check(self.L.vfs_get_mg_half(self.h, g, level, dptr(coef), dptr(lf), dptr(rw)))
+        return coef, lf, rw
 
     def level_nvert(self, g: int, level: int) -> np.ndarray:
         mx, my, mz = self.level_dims(g, level)

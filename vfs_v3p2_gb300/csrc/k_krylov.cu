@@ -189,9 +189,12 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
 // orthogonalised vector u = w - sum_q h_q vs_q V_q is stored unnormalised as
 // V_{j+1}, its multigrid-precision copy as the next preconditioner input, and
 // the partials of ||u||^2 go to parts (k_arnoldi_finish sets vs_{j+1}).
+// dinv (nullable): 1 / D of the FP16 normalised multigrid operator, applied
+// to the multigrid copy after its rounding to T.
 template <typename T>
 __global__ void __launch_bounds__(KB) k_cgs_update(const KrylovState* st, double* V, const double* __restrict__ w,
-                                                   T* __restrict__ out, size_t n, double* parts) {
+                                                   T* __restrict__ out, size_t n, double* parts,
+                                                   const float* __restrict__ dinv) {
   if (is_done(st)) return;
   const int nv = st->j + 1;
   __shared__ double sh[32];
@@ -205,19 +208,22 @@ __global__ void __launch_bounds__(KB) k_cgs_update(const KrylovState* st, double
 #pragma unroll 4
     for (int q = 0; q < nv; q++) a = fma(-hs[q], V[(size_t)q * n + t], a);
     vn[t] = a;
-    out[t] = (T)a;
+    out[t] = dinv ? (T)a * (T)dinv[t] : (T)a;
     s = fma(a, a, s);
   }
   s = block_sum(s, sh);
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
 }
 template <typename T>
-int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s) {
-  k_cgs_update<T><<<krylov_nblocks(n), KB, 0, s>>>(st, V, w, out, n, parts); ++g_launches;
+int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s,
+                      const float* dinv) {
+  k_cgs_update<T><<<krylov_nblocks(n), KB, 0, s>>>(st, V, w, out, n, parts, dinv); ++g_launches;
   return (int)cudaGetLastError();
 }
-template int launch_cgs_update<float>(KrylovState*, double*, const double*, float*, size_t, double*, cudaStream_t);
-template int launch_cgs_update<double>(KrylovState*, double*, const double*, double*, size_t, double*, cudaStream_t);
+template int launch_cgs_update<float>(KrylovState*, double*, const double*, float*, size_t, double*, cudaStream_t,
+                                      const float*);
+template int launch_cgs_update<double>(KrylovState*, double*, const double*, double*, size_t, double*, cudaStream_t,
+                                       const float*);
 
 // Fused CGS2 middle pass: w <- w - V h (h from the first pass), and the
 // second pass's dots V_q . w computed on the updated element while the basis
@@ -387,23 +393,27 @@ int launch_norm2(const double* v, size_t n, double* parts, double* out, cudaStre
 // vn == nullptr: the target is V + st->j * n (the column just opened).
 template <typename T>
 __global__ void __launch_bounds__(KB) k_vnext_in(const KrylovState* st, const double* __restrict__ w, double* vn,
-                                                  T* __restrict__ out, size_t n, double* V) {
+                                                  T* __restrict__ out, size_t n, double* V,
+                                                  const float* __restrict__ dinv) {
   if (is_done(st)) return;
   const double f = st->inv_hn;
   if (!vn) vn = V + (size_t)st->j * n;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     const double v = w[t] * f;
     vn[t] = v;
-    out[t] = (T)v;
+    out[t] = dinv ? (T)v * (T)dinv[t] : (T)v;
   }
 }
 template <typename T>
-int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V) {
-  k_vnext_in<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, out, n, V); ++g_launches;
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V,
+                    const float* dinv) {
+  k_vnext_in<T><<<krylov_nblocks(n) * 4, KB, 0, s>>>(st, w, vn, out, n, V, dinv); ++g_launches;
   return (int)cudaGetLastError();
 }
-template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t, double*);
-template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t, double*);
+template int launch_vnext_in<float>(KrylovState*, const double*, double*, float*, size_t, cudaStream_t, double*,
+                                    const float*);
+template int launch_vnext_in<double>(KrylovState*, const double*, double*, double*, size_t, cudaStream_t, double*,
+                                     const float*);
 
 // done and epoch (adjacent) to pinned host memory
 int launch_status_copy(const KrylovState* st, int* hst, cudaStream_t s) {

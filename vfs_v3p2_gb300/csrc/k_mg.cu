@@ -10,6 +10,8 @@
 // come back through L1/L2.  Slots that are zero on the whole level (mask bit
 // clear) are skipped with a warp-uniform branch, so a grid whose metric has
 // no i-j or j-k cross terms streams 11 coefficient arrays instead of 19.
+#include <type_traits>
+
 #include "vfs_common.cuh"
 #include "vfs_kernels.h"
 #include "vfs_proj.h"
@@ -104,6 +106,30 @@ __device__ __forceinline__ TA stencil_dot(const TC* cv, const TX_* xv) {
   for (int m = 0; m < 19; m++)
     if (MASK & (1u << m)) s = fma((TA)cv[m], to_acc<TA>(xv[m]), s);
   return s;
+}
+
+// Coefficient array of a view in storage type TC: the level's own (TC = T)
+// or its FP16 diagonal-normalised copy (TC = __half).
+template <typename TC, typename T>
+__device__ __forceinline__ const TC* coef_ptr(const OpView<T>& A) {
+  if constexpr (std::is_same<TC, __half>::value) return A.hcoef;
+  else return A.coef;
+}
+
+// Row sum of gathered slots in either storage: sum_m coef_m x_m in slot
+// order, or for the FP16 diagonal-normalised operator x_c first and then
+// the slots (the centre slot holds the row-sum correction delta).
+template <unsigned MASK, typename TA, typename TC, typename TX_>
+__device__ __forceinline__ TA row_dot(const TC* cv, const TX_* xv) {
+  if constexpr (std::is_same<TC, __half>::value) {
+    TA s = to_acc<TA>(xv[CP]);
+#pragma unroll
+    for (int m = 0; m < 19; m++)
+      if (MASK & (1u << m)) s = fma(to_acc<TA>(cv[m]), to_acc<TA>(xv[m]), s);
+    return s;
+  } else {
+    return stencil_dot<MASK, TA>(cv, xv);
+  }
 }
 
 // Stencil at (i, j, k) clamped into the interior (columns and rows past the
@@ -221,7 +247,10 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #define VFS_SMOOTH_TWMAX 32  // columns per block
 #endif
 #ifndef VFS_SMOOTH_PF
-#define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off)
+#define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off), FP32 operator
+#endif
+#ifndef VFS_SMOOTH_PF_HALF
+#define VFS_SMOOTH_PF_HALF 0  // the same for the FP16 operator (measured: the prefetches cost more than they save)
 #endif
 #ifndef VFS_SMOOTH_MINBLK
 #define VFS_SMOOTH_MINBLK 152  // automatic tile: narrow while a sweep has fewer blocks (one per SM)
@@ -233,11 +262,16 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #define VFS_SMOOTH_CARVE -1  // preferred shared-memory carveout in percent (-1: the driver's choice)
 #endif
 
-template <unsigned MASK, typename T>
+template <unsigned MASK, typename T, typename TC>
 __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
              T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
+  // NRM: the FP16 diagonal-normalised operator (b is divided by D, non-fluid
+  // rows have 1/m = 0 so their delta is 0 without a test)
+  constexpr bool NRM = std::is_same<TC, __half>::value;
+  constexpr int PF = NRM ? VFS_SMOOTH_PF_HALF : VFS_SMOOTH_PF;
+  const TC* __restrict__ coef = coef_ptr<TC>(A);
   extern __shared__ unsigned char smraw[];
   const Dims d = A.d;
   const int nj = d.my - 2;
@@ -249,15 +283,14 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
   constexpr int U = VFS_SMOOTH_U;
-  // L2 prefetch of the rows a warp will stream VFS_SMOOTH_PF iterations
-  // later: the loads in flight are bounded by registers (4 bytes each), the
+  // L2 prefetch of the rows a warp will stream PF iterations later: the loads in flight are bounded by registers (4 bytes each), the
   // prefetches are not, so they keep more of HBM's latency-bandwidth product
   // busy.  One lane per 128-byte line: the 11 coefficient slots' (or MASK's)
   // row, b, 1/m and the x rows of planes k-1, k, k+1 (a row of TW floats
   // starting at i0 spans two lines).  Every prefetched line lies inside its
   // array: the element offset is clamped to [0, N - 32].
   auto prefetch_row = [&](int jrow) {
-    if (VFS_SMOOTH_PF <= 0 || jrow > d.my - 2) return;
+    if (PF <= 0 || jrow > d.my - 2) return;
     const int lane = threadIdx.x & 31;
     const int q = lane >> 1;  // stream index
     constexpr int NS = __builtin_popcount(MASK);
@@ -267,19 +300,22 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
         if (n == q) m = s;
         n++;
       }
-    const T* base = nullptr;
+    const char* base = nullptr;
+    size_t es = sizeof(T);
     int shift = 0;
-    if (m >= 0) base = A.coef + (size_t)m * N;
-    else if (q == NS) base = b;
-    else if (q == NS + 1) base = lf;
+    if (m >= 0) {
+      base = (const char*)(coef + (size_t)m * N);
+      es = sizeof(TC);
+    } else if (q == NS) base = (const char*)b;
+    else if (q == NS + 1) base = (const char*)lf;
     else if (xi && q <= NS + 4) {
-      base = xi;
+      base = (const char*)xi;
       shift = (q == NS + 3) ? -d.mx * d.my : (q == NS + 4) ? d.mx * d.my : 0;
     }
     if (!base) return;
     int e = k * d.mx * d.my + jrow * d.mx + i0 + shift + (lane & 1) * 32;
     e = max(0, min(e, N - 32));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + e));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)e * es));
   };
   // Phase 1 in batches of U cells per thread: every load of the batch is
   // issued before any arithmetic (all addresses are interior cells: columns
@@ -289,9 +325,9 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
   // b and only CP, SP, NP of the stencil are loaded.
   for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
-    if (VFS_SMOOTH_PF > 0 && sizeof(T) == 4 && TW == 32)
-      prefetch_row(1 + (base + VFS_SMOOTH_PF * U * VFS_SMOOTH_NT) / TW);
-    T cv[U][19], xv[U][19], bb[U], inv[U];
+    if (PF > 0 && sizeof(T) == 4 && TW == 32) prefetch_row(1 + (base + PF * U * VFS_SMOOTH_NT) / TW);
+    TC cv[U][19];
+    T xv[U][19], bb[U], inv[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int idx = min(base + u * VFS_SMOOTH_NT, nt - 1);
@@ -299,11 +335,11 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
       const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
       const int c = k * d.mx * d.my + j * d.mx + i;
       if (xi) {
-        stencil_gather<MASK>(d, A.coef, xi, i, j, k, cv[u], xv[u]);
+        stencil_gather<MASK>(d, coef, xi, i, j, k, cv[u], xv[u]);
       } else {
-        cv[u][CP] = __ldg(A.coef + c);
-        cv[u][SP] = __ldg((A.coef + (size_t)SP * N) + c);
-        cv[u][NP] = __ldg((A.coef + (size_t)NP * N) + c);
+        if (!NRM) cv[u][CP] = __ldg(coef + c);
+        cv[u][SP] = __ldg((coef + (size_t)SP * N) + c);
+        cv[u][NP] = __ldg((coef + (size_t)NP * N) + c);
       }
       bb[u] = __ldg(b + c);
       inv[u] = __ldg(lf + c);
@@ -313,9 +349,9 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
       const int idx = base + u * VFS_SMOOTH_NT;
       if (idx >= nt) break;
       const int jl = idx / TW;
-      const bool live = (i0 + idx % TW <= d.mx - 2) && cv[u][CP] != T(0);
-      const T ax = xi ? stencil_dot<MASK, T>(cv[u], xv[u]) : T(0);
-      const T a = jl > 0 ? cv[u][SP] : T(0), cn = jl < nj - 1 ? cv[u][NP] : T(0);
+      const bool live = (i0 + idx % TW <= d.mx - 2) && (NRM || to_acc<T>(cv[u][CP]) != T(0));
+      const T ax = xi ? row_dot<MASK, T>(cv[u], xv[u]) : T(0);
+      const T a = jl > 0 ? to_acc<T>(cv[u][SP]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cv[u][NP]) : T(0);
       su[idx] = live ? (bb[u] - ax) * inv[u] : T(0);
       sp[idx] = live ? a * inv[u] : T(0);
       sl[idx] = live ? cn * inv[u] : T(0);
@@ -369,15 +405,22 @@ static int smooth_tw(int ni, int nj, int nk, int cols) {
   return tw;
 }
 
+template <unsigned MASK, typename T, typename TC>
+static void smooth_attrs() {
+  cudaFuncSetAttribute(k_smooth<MASK, T, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (VFS_SMOOTH_CARVE >= 0)
+    cudaFuncSetAttribute(k_smooth<MASK, T, TC>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
+}
+
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_smooth<MASK_ALL, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (VFS_SMOOTH_CARVE >= 0) {
-      cudaFuncSetAttribute(k_smooth<MASK_CH, T>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
-      cudaFuncSetAttribute(k_smooth<MASK_ALL, T>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
+    smooth_attrs<MASK_CH, T, T>();
+    smooth_attrs<MASK_ALL, T, T>();
+    if constexpr (sizeof(T) == 4) {
+      smooth_attrs<MASK_CH, T, __half>();
+      smooth_attrs<MASK_ALL, T, __half>();
     }
     attr = true;
   }
@@ -385,8 +428,19 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   const int tw = smooth_tw<T>(ni, nj, nk, cols);
   const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
-  if (fits_ch(A.mask)) k_smooth<MASK_CH, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
-  else k_smooth<MASK_ALL, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  const bool ch = fits_ch(A.mask);
+  bool done = false;
+  if constexpr (sizeof(T) == 4) {
+    if (A.hcoef) {
+      if (ch) k_smooth<MASK_CH, T, __half><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+      else k_smooth<MASK_ALL, T, __half><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+      done = true;
+    }
+  }
+  if (!done) {
+    if (ch) k_smooth<MASK_CH, T, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+    else k_smooth<MASK_ALL, T, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  }
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -426,15 +480,110 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 }
 
 // ---------------------------------------------------------------------------
+// FP16 diagonal-normalised multigrid operator (FP32 multigrid only).  Per
+// fluid row c with diagonal D = mcoef[CP][c] of the aj-scaled FP64 operator:
+// h_m = fp16(mcoef[m][c] / D) for every off-diagonal slot (round to nearest
+// even), and h_CP = fp16(delta) with delta = sum_m (mcoef[m][c] / D - h_m)
+// in FP64, slot order, so that 1 + delta + sum_m h_m equals the row sum of
+// the normalised row up to one FP16 rounding of delta.  Keeping the row sums
+// keeps the near-null space (smooth modes) of the level operator, which is
+// what the coarse-grid correction relies on.  Non-fluid rows are all zero.
+// Optional outputs: dinv = fp32(1 / D) and dval = fp32(D), 0 on non-fluid
+// rows (the finest level's input scaling, the coarsest level's dense solve).
+// ---------------------------------------------------------------------------
+__global__ void k_half_operator(size_t n, const double* __restrict__ mcoef, __half* __restrict__ h,
+                                float* __restrict__ dinv, float* __restrict__ dval) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double D = mcoef[c];
+    double delta = 0.;
+    for (int m = 1; m < 19; m++) {
+      const double a = D != 0. ? mcoef[(size_t)m * n + c] / D : 0.;
+      const __half hm = __double2half(a);
+      delta = delta + (a - (double)__half2float(hm));
+      h[(size_t)m * n + c] = hm;
+    }
+    h[c] = __double2half(delta);
+    if (dinv) dinv[c] = D != 0. ? (float)(1. / D) : 0.f;
+    if (dval) dval[c] = (float)D;
+  }
+}
+int launch_half_operator(size_t n, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s) {
+  const size_t nb = (n + 255) / 256;
+  k_half_operator<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(n, mcoef, h, dinv, dval); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Thomas pivots 1/m_j of the normalised y-line tridiagonal (a_j = h_SP,
+// b_j = 1 + h_CP, c_j = h_NP), in FP64 from the stored FP16 values, as FP32;
+// 1/m = 0 on non-fluid rows (the sweep's delta there is then 0), which act
+// as identity rows of the recurrence.
+__global__ void k_line_factors_half(Dims d, const __half* __restrict__ h, const double* __restrict__ mcoef,
+                                    float* __restrict__ lf) {
+  const size_t N = ncell(d);
+  const int ni = d.mx - 2, nk = d.mz - 2;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ni * nk; t += gridDim.x * blockDim.x) {
+    const int i = 1 + t % ni, k = 1 + t / ni;
+    double cprev = 0.;
+    for (int j = 1; j < d.my - 1; j++) {
+      const size_t c = cidx(d, i, j, k);
+      if (mcoef[c] == 0.) {
+        lf[c] = 0.f;
+        cprev = 0.;
+        continue;
+      }
+      const double a = (j > 1) ? (double)__half2float(h[(size_t)SP * N + c]) : 0.;
+      const double bb = 1. + (double)__half2float(h[c]);
+      const double cc = (j < d.my - 2) ? (double)__half2float(h[(size_t)NP * N + c]) : 0.;
+      const double inv = 1. / (bb - a * cprev);
+      cprev = cc * inv;
+      lf[c] = (float)inv;
+    }
+  }
+}
+int launch_line_factors_half(const Dims& d, const __half* h, const double* mcoef, float* lf, cudaStream_t s) {
+  const int n = (d.mx - 2) * (d.mz - 2);
+  k_line_factors_half<<<(n + 127) / 128, 128, 0, s>>>(d, h, mcoef, lf); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// Restriction weights of the normalised operator: the fine residual is
+// D_f r_n and the coarse right-hand side is divided by D_c, so the weight
+// max(0, 1 - nvert_f) becomes fp32(max(0, 1 - nvert_f) D_f / D_c) with c the
+// coarse cell the fine cell restricts into (0 when either row is non-fluid).
+__global__ void k_restrict_weights_half(Dims f, Dims c, int si, int sj, int sk, const double* __restrict__ nvf,
+                                        const double* __restrict__ mcf, const double* __restrict__ mcc,
+                                        float* __restrict__ w) {
+  const size_t n = ncell(f);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % f.mx), j = (int)((t / f.mx) % f.my), k = (int)(t / ((size_t)f.mx * f.my));
+    float v = 0.f;
+    if (i >= 1 && i <= f.mx - 2 && j >= 1 && j <= f.my - 2 && k >= 1 && k <= f.mz - 2) {
+      const int ic = si ? i : (i + 1) / 2, jc = sj ? j : (j + 1) / 2, kc = sk ? k : (k + 1) / 2;
+      const double Df = mcf[t], Dc = mcc[cidx(c, ic, jc, kc)];
+      if (Df != 0. && Dc != 0.) v = (float)(fmax(0., 1. - nvf[t]) * Df / Dc);
+    }
+    w[t] = v;
+  }
+}
+int launch_restrict_weights_half(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nvf,
+                                 const double* mcf, const double* mcc, float* w, cudaStream_t s) {
+  const size_t nb = (ncell(f) + 255) / 256;
+  k_restrict_weights_half<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(f, c, si, sj, sk, nvf, mcf, mcc, w);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Residual + restriction (MyRestriction, poisson.c:364-471), one thread per
 // coarse interior cell: bc = 0.125 * sum over the 8 children of
 // (b - A x) * max(0, 1 - nvert_f), 0 on solid coarse cells; xc = 0.
 // ---------------------------------------------------------------------------
-template <unsigned MASK, typename T>
+template <unsigned MASK, typename T, typename TC>
 __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                         const T* __restrict__ rw, Dims c, const double* __restrict__ nvc,
                                                         int si, int sj, int sk, T* __restrict__ bc, T* __restrict__ xc) {
   if (skipped(A.skip)) return;
+  const TC* __restrict__ coef = coef_ptr<TC>(A);
   const int ia = si ? 0 : 1, ja = sj ? 0 : 1, ka = sk ? 0 : 1;
   TILE_LOOP(c) {
     if (!_in) continue;
@@ -449,7 +598,13 @@ __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView
         const int fi = ih - oi[t], fj = jh - oj[t], fk = kh - ok[t];
         const size_t fc = cidx(A.d, fi, fj, fk);
         const T w = rw[fc];
-        const T ax = x ? stencil<MASK, T, T, T>(A.d, A.coef, x, fi, fj, fk) : T(0);
+        T ax = T(0);
+        if (x) {
+          TC cv[19];
+          T xv[19];
+          stencil_gather<MASK>(A.d, coef, x, fi, fj, fk, cv, xv);
+          ax = row_dot<MASK, T>(cv, xv);
+        }
         const T rr = (b[fc] - ax) * w;
         acc += (w != T(0)) ? rr : T(0);
       }
@@ -465,12 +620,13 @@ __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView
 // residuals (four each, coalesced over fine i), weight them by
 // max(0, 1 - nvert_f) into shared memory, and 128 threads sum the 2 x 2 x 2
 // children of each coarse cell in the reference's order.
-template <unsigned MASK, typename T>
+template <unsigned MASK, typename T, typename TC>
 __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpView<T> A, const T* __restrict__ x, const T* __restrict__ b,
                                                            const T* __restrict__ rw, Dims c,
                                                            const double* __restrict__ nvc, T* __restrict__ bc,
                                                            T* __restrict__ xc) {
   if (skipped(A.skip)) return;
+  const TC* __restrict__ coef = coef_ptr<TC>(A);
   __shared__ T sr[2][8][64];
   const Dims f = A.d;
   const int ci0 = 1 + blockIdx.x * 32, cj0 = 1 + blockIdx.y * 4, ck = 1 + blockIdx.z;
@@ -486,7 +642,13 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
     const size_t fc = cidx(f, fic, fjc, fk);
     const T w = rw[fc];
     const T bv = b[fc];
-    const T ax = x ? stencil_clamped<MASK, T>(f, A.coef, x, fic, fjc, fk) : T(0);
+    T ax = T(0);
+    if (x) {
+      TC cv[19];
+      T xv[19];
+      stencil_gather<MASK>(f, coef, x, fic, fjc, fk, cv, xv);
+      ax = row_dot<MASK, T>(cv, xv);
+    }
     const T rr = (bv - ax) * w;
     sr[kk][ty][ii] = (w != T(0) && fi <= f.mx - 2 && fj <= f.my - 2) ? rr : T(0);
   }
@@ -509,18 +671,31 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
   }
 }
 
-template <typename T>
-int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T* rw, const Dims& c,
-                             const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
+template <typename T, typename TC>
+static void launch_resrestrict_tc(const OpView<T>& A, const T* x, const T* b, const T* rw, const Dims& c,
+                                  const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
   const bool ch = fits_ch(A.mask);
   if (!si && !sj && !sk) {
     dim3 g((c.mx - 2 + 31) / 32, (c.my - 2 + 3) / 4, c.mz - 2);
-    if (ch) k_resrestrict_tiled<MASK_CH, T><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
-    else k_resrestrict_tiled<MASK_ALL, T><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+    if (ch) k_resrestrict_tiled<MASK_CH, T, TC><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+    else k_resrestrict_tiled<MASK_ALL, T, TC><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
   } else {
-    if (ch) k_resrestrict<MASK_CH, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
-    else k_resrestrict<MASK_ALL, T><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
+    if (ch) k_resrestrict<MASK_CH, T, TC><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
+    else k_resrestrict<MASK_ALL, T, TC><<<tile_grid(c), dim3(TX, TY), 0, s>>>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc);
   }
+}
+
+template <typename T>
+int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T* rw, const Dims& c,
+                             const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
+  bool done = false;
+  if constexpr (sizeof(T) == 4) {
+    if (A.hcoef) {
+      launch_resrestrict_tc<T, __half>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc, s);
+      done = true;
+    }
+  }
+  if (!done) launch_resrestrict_tc<T, T>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc, s);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -623,16 +798,19 @@ int launch_prolong(const Dims& f, const uint8_t* code, const Dims& c, const T* x
 // ---------------------------------------------------------------------------
 // Coarsest level: x = Binv b over the packed interior (dense, one warp per row).
 // ---------------------------------------------------------------------------
+// dsc (nullable): the level's diagonal, for a right-hand side of the
+// normalised operator (Binv inverts the unnormalised one: x = Binv (D b)).
 template <typename T>
 __global__ void __launch_bounds__(256) k_coarse_gemv(Dims d, const T* __restrict__ Binv, int n, const T* __restrict__ b,
-                                                     T* __restrict__ x, const int* skip) {
+                                                     T* __restrict__ x, const T* __restrict__ dsc, const int* skip) {
   if (skipped(skip)) return;
   extern __shared__ unsigned char smraw[];
   T* sb = (T*)smraw;
   const int ni = d.mx - 2, nj = d.my - 2;
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const int i = 1 + r % ni, j = 1 + (r / ni) % nj, k = 1 + r / (ni * nj);
-    sb[r] = b[cidx(d, i, j, k)];
+    const size_t c = cidx(d, i, j, k);
+    sb[r] = dsc ? b[c] * dsc[c] : b[c];
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -648,29 +826,35 @@ __global__ void __launch_bounds__(256) k_coarse_gemv(Dims d, const T* __restrict
   }
 }
 template <typename T>
-int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const int* skip, cudaStream_t s) {
+int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const T* dsc, const int* skip,
+                       cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_coarse_gemv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_coarse_gemv<T><<<(n + 7) / 8, 256, (size_t)n * sizeof(T), s>>>(d, Binv, n, b, x, skip); ++g_launches;
+  k_coarse_gemv<T><<<(n + 7) / 8, 256, (size_t)n * sizeof(T), s>>>(d, Binv, n, b, x, dsc, skip); ++g_launches;
   return (int)cudaGetLastError();
 }
 
+// dinv (nullable): 1 / D of the FP16 normalised operator, applied after the
+// rounding to T.
 template <typename T>
 __global__ void __launch_bounds__(TX* TY) k_scale_in(Dims d, const double* __restrict__ aj, const double* __restrict__ v,
-                                                     T* __restrict__ out, const int* skip) {
+                                                     T* __restrict__ out, const float* __restrict__ dinv,
+                                                     const int* skip) {
   if (skipped(skip)) return;
   TILE_LOOP(d) {
     if (!_in) continue;
     const size_t c = cidx(d, i, j, k);
-    out[c] = (T)(aj ? aj[c] * v[c] : v[c]);
+    const T t = (T)(aj ? aj[c] * v[c] : v[c]);
+    out[c] = dinv ? t * (T)dinv[c] : t;
   }
 }
 template <typename T>
-int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s) {
-  k_scale_in<T><<<tile_grid(d), dim3(TX, TY), 0, s>>>(d, aj, v, out, skip); ++g_launches;
+int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s,
+                    const float* dinv) {
+  k_scale_in<T><<<tile_grid(d), dim3(TX, TY), 0, s>>>(d, aj, v, out, dinv, skip); ++g_launches;
   return (int)cudaGetLastError();
 }
 
@@ -683,8 +867,9 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
   template int launch_restrict<T>(const Dims&, const T*, const double*, const Dims&, const double*, int, int, int, T*, \
                                   cudaStream_t);                                                                      \
   template int launch_prolong<T>(const Dims&, const uint8_t*, const Dims&, const T*, T*, int, const int*, cudaStream_t); \
-  template int launch_coarse_gemv<T>(const Dims&, const T*, int, const T*, T*, const int*, cudaStream_t);             \
-  template int launch_scale_in<T>(const Dims&, const double*, const double*, T*, const int*, cudaStream_t);
+  template int launch_coarse_gemv<T>(const Dims&, const T*, int, const T*, T*, const T*, const int*, cudaStream_t);  \
+  template int launch_scale_in<T>(const Dims&, const double*, const double*, T*, const int*, cudaStream_t,             \
+                                  const float*);
 INST(float)
 INST(double)
 

@@ -10,6 +10,7 @@
 // arrays [slot][cell] in the slot order of poisson.c:956-974.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -67,13 +68,20 @@ __device__ __forceinline__ void neighbours(const Dims& d, int i, int j, int k, N
   for (int m = 0; m < 19; m++) nb.c[m] = cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]);
 }
 
-// One multigrid level (or the outer operator) as seen by a kernel.
+// One multigrid level (or the outer operator) as seen by a kernel.  With
+// hcoef set (FP32 multigrid only) the kernels use the level's FP16
+// diagonal-normalised operator instead of coef: row c holds a_m / D_c in
+// every off-diagonal slot and, in the centre slot, the FP16 correction
+// delta_c that restores the row sum after rounding, so the row is
+// (1 + delta_c) x_c + sum_m h_m x_m and the level's right-hand sides are
+// divided by D_c.
 template <typename T>
 struct OpView {
   Dims d;
   const T* coef;     // [19][N]
   unsigned mask;     // bit m set if slot m is nonzero somewhere on this level
   const int* skip;   // device flag (nullable): kernels return at once when *skip != 0
+  const __half* hcoef = nullptr;  // [19][N], FP16 diagonal-normalised (nullable)
 };
 
 __device__ __forceinline__ bool skipped(const int* f) { return f && *(volatile const int*)f; }
@@ -163,6 +171,8 @@ template <typename TA, typename TX_>
 __device__ __forceinline__ TA to_acc(TX_ v) { return (TA)v; }
 template <>
 __device__ __forceinline__ double to_acc<double, float>(float v) { return widen(v); }
+template <>
+__device__ __forceinline__ float to_acc<float, __half>(__half v) { return __half2float(v); }
 
 }  // namespace vfs
 

@@ -100,6 +100,12 @@ struct Level {
   double* Binv = nullptr;
   float* Binv32 = nullptr;
   int nco = 0;
+  // FP16 diagonal-normalised operator of the FP32 multigrid (mg_half)
+  __half* hcoef = nullptr;  // [19][N]
+  float* lfh = nullptr;     // its y-line pivots (0 on non-fluid rows)
+  float* rwh = nullptr;     // its restriction weights (levels >= 1)
+  float* dinvh = nullptr;   // finest level: 1 / D (input scaling)
+  float* dvalh = nullptr;   // coarsest level: D (dense-solve scaling)
 };
 
 struct Grid {
@@ -142,7 +148,7 @@ struct Grid {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
-  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2;
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -264,6 +270,28 @@ OpView<T> mgview(Level& L, const int* skip) {
   return OpView<T>{L.d, mcoef_of<T>(L), L.mask, skip};
 }
 
+// The multigrid level data in use: the FP16 normalised operator's pivots,
+// weights and scales when half is set (FP32 multigrid only), else the
+// level's own.
+template <typename T> T* lf_sel(Level& L, bool half);
+template <> float* lf_sel<float>(Level& L, bool half) { return half ? L.lfh : L.lf32; }
+template <> double* lf_sel<double>(Level& L, bool) { return L.lf64; }
+template <typename T> T* rw_sel(Level& L, bool half);
+template <> float* rw_sel<float>(Level& L, bool half) { return half ? L.rwh : L.rw32; }
+template <> double* rw_sel<double>(Level& L, bool) { return L.rw64; }
+template <typename T> T* dsc_sel(Level& L, bool half);
+template <> float* dsc_sel<float>(Level& L, bool half) { return half ? L.dvalh : nullptr; }
+template <> double* dsc_sel<double>(Level&, bool) { return nullptr; }
+template <typename T> const float* dinv_sel(Level& L, bool half);
+template <> const float* dinv_sel<float>(Level& L, bool half) { return half ? L.dinvh : nullptr; }
+template <> const float* dinv_sel<double>(Level&, bool) { return nullptr; }
+template <typename T>
+OpView<T> mgview(Level& L, const int* skip, bool half) {
+  OpView<T> A = mgview<T>(L, skip);
+  if (sizeof(T) == 4 && half) A.hcoef = L.hcoef;
+  return A;
+}
+
 template <typename T>
 int ensure_mg(vfs_ctx* ctx, Grid& g) {
   for (int l = 0; l < g.L; l++) {
@@ -303,6 +331,7 @@ struct MGCfg {
   int cols;        // smoother columns per block (0 = automatic)
   int nu1c, nu2c;  // sweeps on the levels below the finest
   int top;         // index of the finest level
+  bool half;       // FP16 normalised operator (FP32 multigrid only)
   int pre(int l) const { return l == top ? nu1 : nu1c; }
   int post(int l) const { return l == top ? nu2 : nu2c; }
 };
@@ -317,11 +346,13 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // A full smoothing sweep (x != 0) streams the active coefficient slots, x,
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
-void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* xi, const T* b, T* xo, T omega, int cols,
+void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols,
                    cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
-  int rc = launch_smooth<T>(A, lf_of<T>(g.lev[l]), xi, b, xo, omega, s, cols);
-  if (probe) g_probe.end(s, (double)n_interior(A.d) * sizeof(T) * (popcount(A.mask) + 4));
+  int rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols);
+  // the coefficient slots (FP16 or T), x, b and 1/m read, x written
+  const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
+  if (probe) g_probe.end(s, (double)n_interior(A.d) * (slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)));
   dbg("smooth", l, rc, s);
 }
 
@@ -337,19 +368,22 @@ int level_writes(const Grid& g, int l, const MGCfg& c) {
 template <typename T>
 T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, cudaStream_t s) {
   Level& L = g.lev[l];
-  OpView<T> A = mgview<T>(L, skip);
+  const bool half = sizeof(T) == 4 && c.half;
+  OpView<T> A = mgview<T>(L, skip, half);
+  T* lf = lf_sel<T>(L, half);
   const int W = level_writes(g, l, c);
   T* bufs[2] = {xa, xb};
   if (((W - 1) & 1) == 1) std::swap(bufs[0], bufs[1]);
   if (l == 0) {
     if (binv<T>(L)) {
-      dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, bufs[0], skip, s), s);
+      dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, bufs[0], dsc_sel<T>(L, half), skip, s),
+          s);
       return bufs[0];
     }
     T* cur = nullptr;
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      launch_smooth<T>(A, lf_of<T>(L), cur, b, o, (T)c.omega_c, s, c.cols);
+      launch_smooth<T>(A, lf, cur, b, o, (T)c.omega_c, s, c.cols);
       cur = o;
     }
     return cur;
@@ -358,12 +392,14 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   T* cur = nullptr;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
   }
   Level& C = g.lev[l - 1];
   T** xc = xbuf<T>(C);
-  dbg("residual_restrict", l, launch_residual_restrict<T>(A, cur, b, rw_of<T>(L), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s), s);
+  dbg("residual_restrict", l,
+      launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s),
+      s);
   T* ec = vcycle<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, skip, s);
   if (!cur) {
     cur = bufs[q & 1];
@@ -374,7 +410,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, cur, b, o, (T)c.omega, c.cols, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, s);
     cur = o;
   }
   return cur;
@@ -391,6 +427,7 @@ MGCfg mgcfg(const vfs_solve_params& p, int top) {
   c.nu1c = p.nu1_coarse >= 0 ? p.nu1_coarse : p.nu1;
   c.nu2c = p.nu2_coarse >= 0 ? p.nu2_coarse : p.nu2;
   c.top = top;
+  c.half = p.precision == VFS_MIXED && p.mg_half != 0;
   return c;
 }
 
@@ -401,7 +438,8 @@ int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T
             cudaStream_t s, bool with_input = true) {
   Level& F = g.lev[g.L - 1];
   T* bf = bbuf<T>(F);
-  if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s), s);
+  const float* dinv = dinv_sel<T>(F, mgcfg(p, g.L - 1).half);
+  if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s, dinv), s);
   T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p, g.L - 1), skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
@@ -440,13 +478,15 @@ float* zbase<float>(Grid& g) { return g.Z32; }
 template <>
 double* zbase<double>(Grid& g) { return g.Z64; }
 
-// Opening of a cycle: v0 = r / beta and the preconditioner input T(v0).
+// Opening of a cycle: v0 = r / beta and the preconditioner input T(v0)
+// (divided by D for the FP16 normalised multigrid operator).
 template <typename T>
-void fg_open_cycle(Grid& g, cudaStream_t s) {
+void fg_open_cycle(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const size_t N = ncell(g.d);
   Level& F = g.lev[g.L - 1];
   dbg("v0", 0, launch_vec_scale_first(g.st, g.V, g.V, N, s), s);
-  dbg("scale_in", 0, launch_scale_in<T>(F.d, nullptr, g.V, bbuf<T>(F), &g.st->done, s), s);
+  dbg("scale_in", 0,
+      launch_scale_in<T>(F.d, nullptr, g.V, bbuf<T>(F), &g.st->done, s, dinv_sel<T>(F, mgcfg(p, g.L - 1).half)), s);
 }
 
 template <typename T>
@@ -482,7 +522,7 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   dbg("bnorm", 0, launch_norm_init(g.st, g.bs, N, g.parts, 1, s), s);
   dbg("residual0", 0, apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s), s);
   dbg("beta", 0, launch_norm_init(g.st, g.V, N, g.parts, 0, s), s);
-  fg_open_cycle<T>(g, s);
+  fg_open_cycle<T>(g, p, s);
   g.hstat[0] = 0;
   f.it = 0;
   f.j = 0;
@@ -501,7 +541,9 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
-  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mgcfg(p, g.L - 1), skip, s);
+  const MGCfg mc = mgcfg(p, g.L - 1);
+  const float* dinv = dinv_sel<T>(F, mc.half);
+  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mc, skip, s);
   {
     const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
     OpView<double> A{F.d, F.mcoef, F.mask, skip};
@@ -512,7 +554,7 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   dbg("multidot1", 0, launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 1, s), s);
   if (p.orth == VFS_ORTH_CGS) {
     // one pass: update, next column, next preconditioner input, norm partials
-    dbg("cgs_update", 0, launch_cgs_update<T>(g.st, g.V, g.w, bbuf<T>(F), N, g.parts, s), s);
+    dbg("cgs_update", 0, launch_cgs_update<T>(g.st, g.V, g.w, bbuf<T>(F), N, g.parts, s, dinv), s);
     dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
     launch_status_copy(g.st, g.hstat, s);
     return;
@@ -525,7 +567,7 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   }
   dbg("gs_update2", 0, launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 2, s), s);
   dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
-  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, nullptr, bbuf<T>(F), N, s, g.V), s);
+  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, nullptr, bbuf<T>(F), N, s, g.V, dinv), s);
   launch_status_copy(g.st, g.hstat, s);
 }
 
@@ -541,7 +583,8 @@ template <typename T>
 int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphExec_t* out) {
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
-      g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse) {
+      g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse &&
+      g.ig_half == p.mg_half) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -568,6 +611,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_cols = p.smooth_cols;
   g.ig_nu1c = p.nu1_coarse;
   g.ig_nu2c = p.nu2_coarse;
+  g.ig_half = p.mg_half;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -575,7 +619,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
 // Close a cycle (least squares, x update) and, unless finished, open the next
 // one from the true residual of the updated phi.
 template <typename T>
-void fg_cycle_end(Grid& g, bool last, cudaStream_t s) {
+void fg_cycle_end(Grid& g, const vfs_solve_params& p, bool last, cudaStream_t s) {
   const size_t N = ncell(g.d);
   dbg("lsq", 0, launch_lsq_update(g.st, s), s);
   dbg("x_update", 0, launch_x_update<T>(g.st, zbase<T>(g), N, g.phi, s), s);
@@ -583,7 +627,7 @@ void fg_cycle_end(Grid& g, bool last, cudaStream_t s) {
   if (last) return;
   apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s);
   launch_norm_init(g.st, g.V, N, g.parts, 0, s);
-  fg_open_cycle<T>(g, s);
+  fg_open_cycle<T>(g, p, s);
 }
 
 // Host bookkeeping after an iteration was issued on stream s: pipelined status
@@ -601,7 +645,7 @@ int fg_after(vfs_ctx* ctx, Fgmres& f, cudaStream_t s) {
   }
   if (f.observed || f.it >= p.maxit || f.j == p.restart) {
     const bool last = f.observed || f.it >= p.maxit;
-    fg_cycle_end<T>(g, last, s);
+    fg_cycle_end<T>(g, p, last, s);
     f.finished = last;
     f.j = 0;
   }
@@ -650,6 +694,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
     return fail(ctx, VFS_ERR_ARG, "smooth_cols must be 0 (automatic), 8, 16 or 32");
+  if (p->mg_half != 0 && p->mg_half != 1) return fail(ctx, VFS_ERR_ARG, "mg_half must be 0 or 1");
   return VFS_OK;
 }
 
@@ -968,7 +1013,7 @@ int batch_after_tick(vfs_ctx* ctx, Job& J, cudaEvent_t tick, bool have_prev) {
   if (f.observed || f.it >= f.p->maxit || f.j == f.p->restart) {
     const bool last = f.observed || f.it >= f.p->maxit;
     CK(cudaStreamWaitEvent(g.s, tick, 0));
-    fg_cycle_end<T>(g, last, g.s);
+    fg_cycle_end<T>(g, *f.p, last, g.s);
     J.pending = true;
     f.finished = last;
     f.j = 0;
@@ -1131,6 +1176,7 @@ int grid_derive(vfs_ctx* ctx, Grid& g) {
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
+  b += N * (19 * 2 + 4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
   return b;
@@ -1158,6 +1204,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->smooth_cols = 0;
   p->nu1_coarse = -1;
   p->nu2_coarse = -1;
+  p->mg_half = 1;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -1294,6 +1341,11 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.rw32, Lv.N);
     GAB(Lv.rw64, Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
+    GAB(Lv.hcoef, 19 * Lv.N);
+    GAB(Lv.lfh, Lv.N);
+    GAB(Lv.rwh, Lv.N);
+    if (l == L - 1) GAB(Lv.dinvh, Lv.N);
+    if (l == 0) GAB(Lv.dvalh, Lv.N);
   }
   const size_t N = ncell(d);
   GAB(tmp, 9 * N);
@@ -1455,7 +1507,14 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
     launch_line_factors<double>(Lv.d, Lv.mcoef, Lv.lf64, g.s);
+    launch_half_operator(Lv.N, Lv.mcoef, Lv.hcoef, l == g.L - 1 ? Lv.dinvh : nullptr, l == 0 ? Lv.dvalh : nullptr,
+                         g.s);
+    launch_line_factors_half(Lv.d, Lv.hcoef, Lv.mcoef, Lv.lfh, g.s);
   }
+  CK(cudaMemsetAsync(g.lev[0].rwh, 0, g.lev[0].N * sizeof(float), g.s));
+  for (int l = 1; l < g.L; l++)
+    launch_restrict_weights_half(g.lev[l].d, g.lev[l - 1].d, g.si, g.sj, g.sk, g.lev[l].nvert, g.lev[l].mcoef,
+                                 g.lev[l - 1].mcoef, g.lev[l].rwh, g.s);
   Level& F = g.lev[g.L - 1];
   launch_proj_dots(F.d, F.M, g.pd, g.s);
   CK(cudaStreamSynchronize(g.s));
@@ -1977,6 +2036,30 @@ int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out) {
     CK(cudaMemcpy(f.data(), L.mcoef32, 19 * L.N * sizeof(float), cudaMemcpyDeviceToHost));
     for (size_t q = 0; q < f.size(); q++) out[q] = f[q];
   } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1 or 2");
+  return VFS_OK;
+}
+
+int vfs_get_mg_half(vfs_ctx* ctx, int grid, int level, double* coef, double* lf, double* rw) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* g = get_grid(ctx, grid);
+  if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (!g->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  Level& L = g->lev[level];
+  CK(cudaStreamSynchronize(g->s));
+  if (coef) {
+    std::vector<__half> h(19 * L.N);
+    CK(cudaMemcpy(h.data(), L.hcoef, h.size() * sizeof(__half), cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < h.size(); q++) coef[q] = (double)__half2float(h[q]);
+  }
+  std::vector<float> f(L.N);
+  if (lf) {
+    CK(cudaMemcpy(f.data(), L.lfh, L.N * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < L.N; q++) lf[q] = f[q];
+  }
+  if (rw) {
+    CK(cudaMemcpy(f.data(), L.rwh, L.N * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < L.N; q++) rw[q] = f[q];
+  }
   return VFS_OK;
 }
 

@@ -45,6 +45,13 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
                  int cols = 0);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
+// FP16 diagonal-normalised copy of a level's aj-scaled operator (n cells), with
+// optional fp32(1 / D) and fp32(D) per cell; its y-line pivots; its restriction
+// weights max(0, 1 - nvert_f) D_f / D_c
+int launch_half_operator(size_t n, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s);
+int launch_line_factors_half(const Dims& d, const __half* h, const double* mcoef, float* lf, cudaStream_t s);
+int launch_restrict_weights_half(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nvf,
+                                 const double* mcf, const double* mcc, float* w, cudaStream_t s);
 // fine residual r = b - A x restricted to the coarse rhs bc (MyRestriction); also zeroes xc.
 // rw = the fine level's weights max(0, 1 - nvert) in T (launch_restrict_weights)
 template <typename T>
@@ -59,11 +66,13 @@ int launch_restrict(const Dims& f, const T* x, const double* nvf, const Dims& c,
 template <typename T>
 int launch_prolong(const Dims& f, const uint8_t* code, const Dims& c, const T* xc, T* xf, int add, const int* skip,
                    cudaStream_t s);
-// x = Binv b over the packed interior of the coarsest level
+// x = Binv b over the packed interior of the coarsest level (b scaled by dsc first when dsc != nullptr)
 template <typename T>
-int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const int* skip, cudaStream_t s);
-// fine-level preconditioner input: out = T(aj * v), or T(v) when aj is null
+int launch_coarse_gemv(const Dims& d, const T* Binv, int n, const T* b, T* x, const T* dsc, const int* skip,
+                       cudaStream_t s);
+// fine-level preconditioner input: out = T(aj * v), or T(v) when aj is null; times dinv when given
 template <typename T>
-int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s);
+int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, const int* skip, cudaStream_t s,
+                    const float* dinv = nullptr);
 
 }  // namespace vfs

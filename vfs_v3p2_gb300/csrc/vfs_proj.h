@@ -81,9 +81,11 @@ int launch_gs_update(KrylovState* st, const double* V, int nv, double* w, size_t
 int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, size_t n, double* parts, cudaStream_t s,
                           int cap = 32);
 template <typename T>
-int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s);
+int launch_cgs_update(KrylovState* st, double* V, const double* w, T* out, size_t n, double* parts, cudaStream_t s,
+                      const float* dinv = nullptr);
 template <typename T>
-int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V = nullptr);
+int launch_vnext_in(KrylovState* st, const double* w, double* vn, T* out, size_t n, cudaStream_t s, double* V = nullptr,
+                    const float* dinv = nullptr);
 // w = A z (aj-scaled FP64 operator, z in T) and Z[st->j] = z on the interior
 template <typename T>
 int launch_apply64_krylov(const OpView<double>& A, const T* z, T* Z, const KrylovState* st, double* w, cudaStream_t s);
