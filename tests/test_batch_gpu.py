@@ -82,8 +82,8 @@ def test_batch_per_grid_parameters(gpu_ctx):
             gpu_ctx.grid_destroy(gid)
 
 
-@pytest.mark.parametrize("half", [1, 0])
-def test_smoother_tile_does_not_change_results(gpu_ctx, half):
+@pytest.mark.parametrize("precision,half", [("mixed", 1), ("mixed", 0), ("fp64", 0)])
+def test_smoother_tile_does_not_change_results(gpu_ctx, precision, half):
     """The y-line smoother's tile (i-columns per block) only regroups
     independent column solves: every tile gives the same bits."""
     c = _cases()[1]
@@ -92,8 +92,8 @@ def test_smoother_tile_does_not_change_results(gpu_ctx, half):
         out = []
         for cols in (0, 8, 16, 32):
             _reset(gpu_ctx, gid, c)
-            info, dm = gpu_ctx.projection_step(gid, capi.default_params(rtol=1e-9, div_tol=1e-8, smooth_cols=cols,
-                                                                        mg_half=half))
+            info, dm = gpu_ctx.projection_step(gid, capi.default_params(precision=precision, rtol=1e-9, div_tol=1e-8,
+                                                                        smooth_cols=cols, mg_half=half))
             out.append((info["iterations"], dm, _fields(gpu_ctx, gid, c)[0]))
         for it, dm, phi in out[1:]:
             assert it == out[0][0] and dm == out[0][1] and np.array_equal(phi, out[0][2])

@@ -262,6 +262,56 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #define VFS_SMOOTH_CARVE -1  // preferred shared-memory carveout in percent (-1: the driver's choice)
 #endif
 
+// Phase 2 of the sweep for column il of a tile: forward substitution
+// y_j = su_j - sp_j y_{j-1}, then backward delta_j = y_j - sl_j delta_{j+1},
+// both in place in su.  The operands of 8 rows are read into registers
+// before their 8 dependent FMAs (the staged arrays share one buffer, so a
+// plain loop would order every load after the previous row's store), which
+// leaves only the FMA chain on the critical path; the arithmetic is the
+// same row by row.
+template <typename T>
+__device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int nj, int TW, int il) {
+  constexpr int B = 8;
+  T y = T(0);
+  int jl = 0;
+  for (; jl + B <= nj; jl += B) {
+    T a[B], r[B];
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      a[u] = sp[(jl + u) * TW + il];
+      r[u] = su[(jl + u) * TW + il];
+    }
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      y = fma(-a[u], y, r[u]);
+      su[(jl + u) * TW + il] = y;
+    }
+  }
+  for (; jl < nj; jl++) {
+    y = fma(-sp[jl * TW + il], y, su[jl * TW + il]);
+    su[jl * TW + il] = y;
+  }
+  T xn = T(0);
+  jl = nj - 1;
+  for (; jl - B + 1 >= 0; jl -= B) {
+    T c[B], r[B];
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      c[u] = sl[(jl - u) * TW + il];
+      r[u] = su[(jl - u) * TW + il];
+    }
+#pragma unroll
+    for (int u = 0; u < B; u++) {
+      xn = fma(-c[u], xn, r[u]);
+      su[(jl - u) * TW + il] = xn;
+    }
+  }
+  for (; jl >= 0; jl--) {
+    xn = fma(-sl[jl * TW + il], xn, su[jl * TW + il]);
+    su[jl * TW + il] = xn;
+  }
+}
+
 template <unsigned MASK, typename T, typename TC>
 __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
@@ -358,23 +408,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     }
   }
   __syncthreads();
-  if (threadIdx.x < TW) {
-    const int il = threadIdx.x;
-    T y = T(0);
-#pragma unroll 8
-    for (int jl = 0; jl < nj; jl++) {
-      const int q = jl * TW + il;
-      y = fma(-sp[q], y, su[q]);
-      su[q] = y;
-    }
-    T xn = T(0);
-#pragma unroll 8
-    for (int jl = nj - 1; jl >= 0; jl--) {
-      const int q = jl * TW + il;
-      xn = fma(-sl[q], xn, su[q]);
-      su[q] = xn;
-    }
-  }
+  if (threadIdx.x < TW) line_solve<T>(su, sp, sl, nj, TW, threadIdx.x);
   __syncthreads();
   // Phase 3, unrolled so that the old values of several cells are loaded
   // together (columns past the last one are clamped and not stored).
