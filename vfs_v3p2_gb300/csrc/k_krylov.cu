@@ -19,6 +19,7 @@
 namespace vfs {
 
 constexpr int KB = 256;
+constexpr int MAXCOL = 64;  // largest restart length
 
 int krylov_nblocks(size_t n) {
   size_t b = (n + KB * 4 - 1) / (KB * 4);
@@ -203,7 +204,26 @@ __global__ void __launch_bounds__(KB) k_cgs_update(const KrylovState* st, double
   __syncthreads();
   double* vn = V + (size_t)nv * n;
   double s = 0.;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+  // two cells per turn (their basis loads in flight together), in cell order
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; t + stride < n; t += 2 * stride) {
+    double a0 = w[t], a1 = w[t + stride];
+#pragma unroll 4
+    for (int q = 0; q < nv; q++) {
+      const double h = hs[q];
+      const double v0 = V[(size_t)q * n + t], v1 = V[(size_t)q * n + t + stride];
+      a0 = fma(-h, v0, a0);
+      a1 = fma(-h, v1, a1);
+    }
+    vn[t] = a0;
+    vn[t + stride] = a1;
+    out[t] = dinv ? (T)a0 * (T)dinv[t] : (T)a0;
+    out[t + stride] = dinv ? (T)a1 * (T)dinv[t + stride] : (T)a1;
+    s = fma(a0, a0, s);
+    s = fma(a1, a1, s);
+  }
+  if (t < n) {
     double a = w[t];
 #pragma unroll 4
     for (int q = 0; q < nv; q++) a = fma(-hs[q], V[(size_t)q * n + t], a);
@@ -289,24 +309,33 @@ int launch_gs_update_dots(KrylovState* st, const double* V, int nv, double* w, s
 
 // Close Arnoldi column j: ||w||, Hessenberg column, Givens rotation, residual
 // estimate |g[j+1]|, convergence test, 1 / h[j+1][j] for the next basis vector.
+// The column, the previous rotations and g[j] are staged in shared memory by
+// the whole block first, so that the serial rotation loop of thread 0 reads
+// no global memory.
 __global__ void k_arnoldi_finish(KrylovState* st, const double* __restrict__ parts, int nparts) {
   if (is_done(st)) return;
   __shared__ double sh[32];
+  __shared__ double hc[MAXCOL + 2], cq[MAXCOL + 1], sq[MAXCOL + 1];
   double s = 0.;
   for (int p = threadIdx.x; p < nparts; p += blockDim.x) s += parts[p];
-  s = block_sum(s, sh);
-  if (threadIdx.x != 0) return;
   const int m = st->m, j = st->j;
+  for (int q = threadIdx.x; q <= j; q += blockDim.x) hc[q] = st->hacc[q];
+  for (int q = threadIdx.x; q < j; q += blockDim.x) {
+    cq[q] = st->cs[q];
+    sq[q] = st->sn[q];
+  }
+  s = block_sum(s, sh);  // (its barriers also order the staging)
+  if (threadIdx.x != 0) return;
   const double hn = sqrt(s);
   double* Hc = st->H + (size_t)j * (m + 1);
-  for (int q = 0; q <= j; q++) Hc[q] = st->hacc[q];
-  Hc[j + 1] = hn;
+  hc[j + 1] = hn;
   for (int q = 0; q < j; q++) {
-    const double a = Hc[q], b = Hc[q + 1];
-    Hc[q] = st->cs[q] * a + st->sn[q] * b;
-    Hc[q + 1] = -st->sn[q] * a + st->cs[q] * b;
+    const double a = hc[q], b = hc[q + 1];
+    hc[q] = cq[q] * a + sq[q] * b;
+    hc[q + 1] = -sq[q] * a + cq[q] * b;
   }
-  const double a = Hc[j], b = Hc[j + 1];
+  for (int q = 0; q < j; q++) Hc[q] = hc[q];
+  const double a = hc[j], b = hc[j + 1];
   const double den = sqrt(a * a + b * b);
   const double c = den > 0. ? a / den : 1., sn = den > 0. ? b / den : 0.;
   st->cs[j] = c;
