@@ -108,6 +108,31 @@ __device__ __forceinline__ TA stencil_dot(const TC* cv, const TX_* xv) {
   return s;
 }
 
+// stencil_gather for the FP16 operator (hidx layout; x as in stencil_gather).
+template <unsigned MASK, typename TX_>
+__device__ __forceinline__ void stencil_gather_h(const Dims& d, const __half* __restrict__ h, const TX_* __restrict__ x,
+                                                 int i, int j, int k, __half* cv, TX_* xv) {
+  const int sy = d.mx, sz = d.mx * d.my;
+  const int c = k * sz + j * sy + i;
+  const size_t hs = hslot(d), hc = hidx(d, i, j, k);
+  const int oi[3] = {(i == 1 && d.ip) ? d.mx - 3 : -1, 0, (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1};
+  const int oj[3] = {((j == 1 && d.jp) ? d.my - 3 : -1) * sy, 0, ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy};
+  const int ok[3] = {((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, 0, ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz};
+#pragma unroll
+  for (int m = 0; m < 19; m++) {
+    if (MASK & (1u << m)) {
+      cv[m] = __ldg(h + (size_t)m * hs + hc);
+      xv[m] = x ? __ldg(x + (c + oi[slot_di(m) + 1] + oj[slot_dj(m) + 1] + ok[slot_dk(m) + 1])) : TX_(0);
+    }
+  }
+}
+template <unsigned MASK, typename TC, typename TX_>
+__device__ __forceinline__ void gather(const Dims& d, const TC* __restrict__ coef, const TX_* __restrict__ x, int i,
+                                       int j, int k, TC* cv, TX_* xv) {
+  if constexpr (std::is_same<TC, __half>::value) stencil_gather_h<MASK>(d, coef, x, i, j, k, cv, xv);
+  else stencil_gather<MASK>(d, coef, x, i, j, k, cv, xv);
+}
+
 // Coefficient array of a view in storage type TC: the level's own (TC = T)
 // or its FP16 diagonal-normalised copy (TC = __half).
 template <typename TC, typename T>
@@ -240,6 +265,9 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_MINB
 #define VFS_SMOOTH_MINB 4  // resident blocks per SM the register budget must allow
 #endif
+#ifndef VFS_SMOOTH_MINB_HALF
+#define VFS_SMOOTH_MINB_HALF 3  // the same for the 19-slot FP16 operator (two cells per thread: more registers)
+#endif
 #ifndef VFS_SMOOTH_U
 #define VFS_SMOOTH_U 1  // cells whose loads one thread issues together in phase 1
 #endif
@@ -261,6 +289,84 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_CARVE
 #define VFS_SMOOTH_CARVE -1  // preferred shared-memory carveout in percent (-1: the driver's choice)
 #endif
+
+// Phase 1 of the sweep on the FP16 operator, two cells per thread (see the
+// caller); writes su, sp, sl of the tile.
+template <unsigned MASK, typename T>
+__device__ __forceinline__ void smooth_pairs(const OpView<T>& A, const T* __restrict__ lf, const T* __restrict__ xi,
+                                             const T* __restrict__ b, T* su, T* sp, T* sl, int i0, int k, int TW) {
+  const Dims d = A.d;
+  const __half* __restrict__ h = A.hcoef;
+  const int nj = d.my - 2, np = TW >> 1, nitems = nj * np;
+  const int sy = d.mx, sz = d.mx * d.my;
+  const size_t hs = hslot(d);
+  const int lastodd = d.mx - 2 - ((d.mx - 1) & 1);  // largest odd column <= mx - 2
+  const int kk[3] = {(k == 1 && d.kp) ? d.mz - 2 : k - 1, k, (k == d.mz - 2 && d.kp) ? 1 : k + 1};
+  for (int it = threadIdx.x; it < nitems; it += VFS_SMOOTH_NT) {
+    const int jl = it / np, p = it - jl * np;
+    const int j = 1 + jl;
+    const int ia = i0 + 2 * p, ib = ia + 1;
+    const int ca = min(ia, d.mx - 2), cb = min(ib, d.mx - 2);
+    const int la = min(ia, lastodd);  // the aligned word holding the pair (clamped)
+    const int cL = (ca == 1 && d.ip) ? d.mx - 2 : ca - 1;
+    const int cR = (cb == d.mx - 2 && d.ip) ? 1 : cb + 1;
+    const bool sep = ca < cb;  // two distinct cells (else b is the clamped copy of a)
+    const int jm = (j == 1 && d.jp) ? nj : j - 1, jp1 = (j == nj && d.jp) ? 1 : j + 1;
+    const size_t hrow = hidx(d, la, j, k);
+    __half2 cw[19];
+    T xL[3][3], xA[3][3], xB[3][3], xR[3][3];  // [dk + 1][dj + 1]
+#pragma unroll
+    for (int m = 0; m < 19; m++)
+      if ((MASK & (1u << m)) && (xi || m == SP || m == NP)) cw[m] = __ldg((const __half2*)(h + (size_t)m * hs + hrow));
+    if (xi) {
+#pragma unroll
+      for (int dk = -1; dk <= 1; dk++)
+#pragma unroll
+        for (int dj = -1; dj <= 1; dj++) {
+          bool any = false, side = false;
+#pragma unroll
+          for (int m = 0; m < 19; m++)
+            if ((MASK & (1u << m)) && slot_dj(m) == dj && slot_dk(m) == dk) {
+              any = true;
+              if (slot_di(m) != 0) side = true;
+            }
+          if (!any) continue;
+          const int row = kk[dk + 1] * sz + (dj < 0 ? jm : (dj > 0 ? jp1 : j)) * sy;
+          xA[dk + 1][dj + 1] = __ldg(xi + row + ca);
+          xB[dk + 1][dj + 1] = __ldg(xi + row + cb);
+          if (side) {
+            xL[dk + 1][dj + 1] = __ldg(xi + row + cL);
+            xR[dk + 1][dj + 1] = __ldg(xi + row + cR);
+          }
+        }
+    }
+    const int ra = k * sz + j * sy + ca, rb = k * sz + j * sy + cb;
+    const T bba = __ldg(b + ra), bbb = __ldg(b + rb), iva = __ldg(lf + ra), ivb = __ldg(lf + rb);
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      __half cv[19];
+      T xv[19];
+#pragma unroll
+      for (int m = 0; m < 19; m++) {
+        if (!(MASK & (1u << m))) continue;
+        if (xi || m == SP || m == NP) cv[m] = e == 0 ? __low2half(cw[m]) : __high2half(cw[m]);
+        if (!xi) continue;
+        const int di = slot_di(m), dj = slot_dj(m) + 1, dk = slot_dk(m) + 1;
+        if (e == 0) xv[m] = di < 0 ? xL[dk][dj] : (di > 0 ? (sep ? xB[dk][dj] : xR[dk][dj]) : xA[dk][dj]);
+        else xv[m] = di < 0 ? (sep ? xA[dk][dj] : xL[dk][dj]) : (di > 0 ? xR[dk][dj] : xB[dk][dj]);
+      }
+      const int il = 2 * p + e;
+      const bool live = i0 + il <= d.mx - 2;
+      const T ax = xi ? row_dot<MASK, T>(cv, xv) : T(0);
+      const T a = jl > 0 ? to_acc<T>(cv[SP]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cv[NP]) : T(0);
+      const T bb = e == 0 ? bba : bbb, inv = e == 0 ? iva : ivb;
+      const int idx = jl * TW + il;
+      su[idx] = live ? (bb - ax) * inv : T(0);
+      sp[idx] = live ? a * inv : T(0);
+      sl[idx] = live ? cn * inv : T(0);
+    }
+  }
+}
 
 // Phase 2 of the sweep for column il of a tile: forward substitution
 // y_j = su_j - sp_j y_{j-1}, then backward delta_j = y_j - sl_j delta_{j+1},
@@ -313,7 +419,9 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
 }
 
 template <unsigned MASK, typename T, typename TC>
-__global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
+__global__ void __launch_bounds__(VFS_SMOOTH_NT, (std::is_same<TC, __half>::value && MASK == MASK_ALL)
+                                                     ? VFS_SMOOTH_MINB_HALF
+                                                     : VFS_SMOOTH_MINB)
     k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
              T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
@@ -333,12 +441,14 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
   constexpr int U = VFS_SMOOTH_U;
-  // L2 prefetch of the rows a warp will stream PF iterations later: the loads in flight are bounded by registers (4 bytes each), the
-  // prefetches are not, so they keep more of HBM's latency-bandwidth product
-  // busy.  One lane per 128-byte line: the 11 coefficient slots' (or MASK's)
-  // row, b, 1/m and the x rows of planes k-1, k, k+1 (a row of TW floats
-  // starting at i0 spans two lines).  Every prefetched line lies inside its
-  // array: the element offset is clamped to [0, N - 32].
+  // L2 prefetch of the rows a warp will stream PF iterations later: the
+  // loads in flight are bounded by registers (4 bytes each), the prefetches
+  // are not, so they keep more of HBM's latency-bandwidth product busy.  One
+  // lane per 128-byte line: the 11 coefficient slots' (or MASK's) row, b, 1/m
+  // and the x rows of planes k-1, k, k+1 (a row of TW floats starting at i0
+  // spans two lines).  Every prefetched line lies inside its array: the
+  // element offset is clamped to [0, N - 32].  (FP32 operator only: the FP16
+  // one measured faster without.)
   auto prefetch_row = [&](int jrow) {
     if (PF <= 0 || jrow > d.my - 2) return;
     const int lane = threadIdx.x & 31;
@@ -354,6 +464,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     size_t es = sizeof(T);
     int shift = 0;
     if (m >= 0) {
+      if constexpr (NRM) return;  // hidx layout: not this row arithmetic
       base = (const char*)(coef + (size_t)m * N);
       es = sizeof(TC);
     } else if (q == NS) base = (const char*)b;
@@ -367,44 +478,59 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
     e = max(0, min(e, N - 32));
     asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)e * es));
   };
-  // Phase 1 in batches of U cells per thread: every load of the batch is
-  // issued before any arithmetic (all addresses are interior cells: columns
-  // past the last one are clamped onto it and discarded; non-fluid rows have
-  // finite factors and are selected out).  The line factors a_j/m_j and c'_j
-  // are formed from the SP and NP coefficients the stencil loads anyway; only
-  // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
-  // b and only CP, SP, NP of the stencil are loaded.
-  for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
-    if (PF > 0 && sizeof(T) == 4 && TW == 32) prefetch_row(1 + (base + PF * U * VFS_SMOOTH_NT) / TW);
-    TC cv[U][19];
-    T xv[U][19], bb[U], inv[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int idx = min(base + u * VFS_SMOOTH_NT, nt - 1);
-      const int il = idx % TW, jl = idx / TW;
-      const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
-      const int c = k * d.mx * d.my + j * d.mx + i;
-      if (xi) {
-        stencil_gather<MASK>(d, coef, xi, i, j, k, cv[u], xv[u]);
-      } else {
-        if (!NRM) cv[u][CP] = __ldg(coef + c);
-        cv[u][SP] = __ldg((coef + (size_t)SP * N) + c);
-        cv[u][NP] = __ldg((coef + (size_t)NP * N) + c);
+  if constexpr (NRM && MASK == MASK_ALL) {
+    // 19-slot FP16 operator: one thread takes the cell pair (ia, ia + 1),
+    // ia = i0 + 2 p odd, whose coefficients of a slot are one aligned word of
+    // the hidx layout; x is read once per column (L, A, B, R = ia - 1 .. ia + 2,
+    // the periodic wraps and the clamp of the per-cell path applied) and
+    // shared by the two cells.  Per cell the arithmetic is the per-cell
+    // path's.  (Measured: faster than one cell per thread for 19 slots,
+    // slower for 11, where one cell per thread keeps 4 blocks per SM.)
+    smooth_pairs<MASK, T>(A, lf, xi, b, su, sp, sl, i0, k, TW);
+  } else {
+    // Phase 1 in batches of U cells per thread: every load of the batch is
+    // issued before any arithmetic (all addresses are interior cells: columns
+    // past the last one are clamped onto it and discarded; non-fluid rows have
+    // finite factors and are selected out).  The line factors a_j/m_j and c'_j
+    // are formed from the SP and NP coefficients the stencil loads anyway; only
+    // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
+    // b and only CP, SP, NP of the stencil are loaded.
+    for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
+      if (PF > 0 && sizeof(T) == 4 && TW == 32) prefetch_row(1 + (base + PF * U * VFS_SMOOTH_NT) / TW);
+      TC cv[U][19];
+      T xv[U][19], bb[U], inv[U];
+  #pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int idx = min(base + u * VFS_SMOOTH_NT, nt - 1);
+        const int il = idx % TW, jl = idx / TW;
+        const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
+        const int c = k * d.mx * d.my + j * d.mx + i;
+        if (xi) {
+          gather<MASK>(d, coef, xi, i, j, k, cv[u], xv[u]);
+        } else if constexpr (NRM) {
+          const size_t hc = hidx(d, i, j, k), hs = hslot(d);
+          cv[u][SP] = __ldg(coef + (size_t)SP * hs + hc);
+          cv[u][NP] = __ldg(coef + (size_t)NP * hs + hc);
+        } else {
+          cv[u][CP] = __ldg(coef + c);
+          cv[u][SP] = __ldg((coef + (size_t)SP * N) + c);
+          cv[u][NP] = __ldg((coef + (size_t)NP * N) + c);
+        }
+        bb[u] = __ldg(b + c);
+        inv[u] = __ldg(lf + c);
       }
-      bb[u] = __ldg(b + c);
-      inv[u] = __ldg(lf + c);
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int idx = base + u * VFS_SMOOTH_NT;
-      if (idx >= nt) break;
-      const int jl = idx / TW;
-      const bool live = (i0 + idx % TW <= d.mx - 2) && (NRM || to_acc<T>(cv[u][CP]) != T(0));
-      const T ax = xi ? row_dot<MASK, T>(cv[u], xv[u]) : T(0);
-      const T a = jl > 0 ? to_acc<T>(cv[u][SP]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cv[u][NP]) : T(0);
-      su[idx] = live ? (bb[u] - ax) * inv[u] : T(0);
-      sp[idx] = live ? a * inv[u] : T(0);
-      sl[idx] = live ? cn * inv[u] : T(0);
+  #pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int idx = base + u * VFS_SMOOTH_NT;
+        if (idx >= nt) break;
+        const int jl = idx / TW;
+        const bool live = (i0 + idx % TW <= d.mx - 2) && (NRM || to_acc<T>(cv[u][CP]) != T(0));
+        const T ax = xi ? row_dot<MASK, T>(cv[u], xv[u]) : T(0);
+        const T a = jl > 0 ? to_acc<T>(cv[u][SP]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cv[u][NP]) : T(0);
+        su[idx] = live ? (bb[u] - ax) * inv[u] : T(0);
+        sp[idx] = live ? a * inv[u] : T(0);
+        sl[idx] = live ? cn * inv[u] : T(0);
+      }
     }
   }
   __syncthreads();
@@ -525,25 +651,28 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // Optional outputs: dinv = fp32(1 / D) and dval = fp32(D), 0 on non-fluid
 // rows (the finest level's input scaling, the coarsest level's dense solve).
 // ---------------------------------------------------------------------------
-__global__ void k_half_operator(size_t n, const double* __restrict__ mcoef, __half* __restrict__ h,
+__global__ void k_half_operator(Dims d, const double* __restrict__ mcoef, __half* __restrict__ h,
                                 float* __restrict__ dinv, float* __restrict__ dval) {
+  const size_t n = ncell(d), hs = hslot(d);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % d.mx), j = (int)((c / d.mx) % d.my), k = (int)(c / ((size_t)d.mx * d.my));
+    const size_t hc = hidx(d, i, j, k);
     const double D = mcoef[c];
     double delta = 0.;
     for (int m = 1; m < 19; m++) {
       const double a = D != 0. ? mcoef[(size_t)m * n + c] / D : 0.;
       const __half hm = __double2half(a);
       delta = delta + (a - (double)__half2float(hm));
-      h[(size_t)m * n + c] = hm;
+      h[(size_t)m * hs + hc] = hm;
     }
-    h[c] = __double2half(delta);
+    h[hc] = __double2half(delta);
     if (dinv) dinv[c] = D != 0. ? (float)(1. / D) : 0.f;
     if (dval) dval[c] = (float)D;
   }
 }
-int launch_half_operator(size_t n, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s) {
-  const size_t nb = (n + 255) / 256;
-  k_half_operator<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(n, mcoef, h, dinv, dval); ++g_launches;
+int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s) {
+  const size_t nb = (ncell(d) + 255) / 256;
+  k_half_operator<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(d, mcoef, h, dinv, dval); ++g_launches;
   return (int)cudaGetLastError();
 }
 
@@ -553,21 +682,21 @@ int launch_half_operator(size_t n, const double* mcoef, __half* h, float* dinv, 
 // as identity rows of the recurrence.
 __global__ void k_line_factors_half(Dims d, const __half* __restrict__ h, const double* __restrict__ mcoef,
                                     float* __restrict__ lf) {
-  const size_t N = ncell(d);
+  const size_t hs = hslot(d);
   const int ni = d.mx - 2, nk = d.mz - 2;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ni * nk; t += gridDim.x * blockDim.x) {
     const int i = 1 + t % ni, k = 1 + t / ni;
     double cprev = 0.;
     for (int j = 1; j < d.my - 1; j++) {
-      const size_t c = cidx(d, i, j, k);
+      const size_t c = cidx(d, i, j, k), hc = hidx(d, i, j, k);
       if (mcoef[c] == 0.) {
         lf[c] = 0.f;
         cprev = 0.;
         continue;
       }
-      const double a = (j > 1) ? (double)__half2float(h[(size_t)SP * N + c]) : 0.;
-      const double bb = 1. + (double)__half2float(h[c]);
-      const double cc = (j < d.my - 2) ? (double)__half2float(h[(size_t)NP * N + c]) : 0.;
+      const double a = (j > 1) ? (double)__half2float(h[(size_t)SP * hs + hc]) : 0.;
+      const double bb = 1. + (double)__half2float(h[hc]);
+      const double cc = (j < d.my - 2) ? (double)__half2float(h[(size_t)NP * hs + hc]) : 0.;
       const double inv = 1. / (bb - a * cprev);
       cprev = cc * inv;
       lf[c] = (float)inv;
@@ -636,7 +765,7 @@ __global__ void __launch_bounds__(TX* TY, VFS_STENCIL_MINB) k_resrestrict(OpView
         if (x) {
           TC cv[19];
           T xv[19];
-          stencil_gather<MASK>(A.d, coef, x, fi, fj, fk, cv, xv);
+          gather<MASK>(A.d, coef, x, fi, fj, fk, cv, xv);
           ax = row_dot<MASK, T>(cv, xv);
         }
         const T rr = (b[fc] - ax) * w;
@@ -680,7 +809,7 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
     if (x) {
       TC cv[19];
       T xv[19];
-      stencil_gather<MASK>(f, coef, x, fic, fjc, fk, cv, xv);
+      gather<MASK>(f, coef, x, fic, fjc, fk, cv, xv);
       ax = row_dot<MASK, T>(cv, xv);
     }
     const T rr = (bv - ax) * w;

@@ -68,6 +68,17 @@ __device__ __forceinline__ void neighbours(const Dims& d, int i, int j, int k, N
   for (int m = 0; m < 19; m++) nb.c[m] = cidx(d, II[slot_di(m) + 1], JJ[slot_dj(m) + 1], KK[slot_dk(m) + 1]);
 }
 
+// Layout of a level's FP16 operator (OpView::hcoef): rows padded to
+// hpitch = mx + 7 rounded up to 8 halves, element (i, j, k) of slot m at
+// m * hslot + (k * my + j) * hpitch + i + 7, so that column i = 1 of every
+// row starts a 16-byte line and the coefficients of the cell pair (i, i + 1),
+// i odd, are one aligned 4-byte word.
+__host__ __device__ __forceinline__ int hpitch(const Dims& d) { return (d.mx + 14) & ~7; }
+__host__ __device__ __forceinline__ size_t hslot(const Dims& d) { return (size_t)hpitch(d) * d.my * d.mz; }
+__host__ __device__ __forceinline__ size_t hidx(const Dims& d, int i, int j, int k) {
+  return ((size_t)k * d.my + j) * hpitch(d) + i + 7;
+}
+
 // One multigrid level (or the outer operator) as seen by a kernel.  With
 // hcoef set (FP32 multigrid only) the kernels use the level's FP16
 // diagonal-normalised operator instead of coef: row c holds a_m / D_c in
@@ -81,7 +92,7 @@ struct OpView {
   const T* coef;     // [19][N]
   unsigned mask;     // bit m set if slot m is nonzero somewhere on this level
   const int* skip;   // device flag (nullable): kernels return at once when *skip != 0
-  const __half* hcoef = nullptr;  // [19][N], FP16 diagonal-normalised (nullable)
+  const __half* hcoef = nullptr;  // [19][hslot], FP16 diagonal-normalised (nullable)
 };
 
 __device__ __forceinline__ bool skipped(const int* f) { return f && *(volatile const int*)f; }

@@ -101,7 +101,7 @@ struct Level {
   float* Binv32 = nullptr;
   int nco = 0;
   // FP16 diagonal-normalised operator of the FP32 multigrid (mg_half)
-  __half* hcoef = nullptr;  // [19][N]
+  __half* hcoef = nullptr;  // [19][hslot] (hidx layout)
   float* lfh = nullptr;     // its y-line pivots (0 on non-fluid rows)
   float* rwh = nullptr;     // its restriction weights (levels >= 1)
   float* dinvh = nullptr;   // finest level: 1 / D (input scaling)
@@ -1176,7 +1176,7 @@ int grid_derive(vfs_ctx* ctx, Grid& g) {
 size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
-  b += N * (19 * 2 + 4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
+  b += 19 * 2 * hslot(d) + N * (4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
   return b;
@@ -1341,7 +1341,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.rw32, Lv.N);
     GAB(Lv.rw64, Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
-    GAB(Lv.hcoef, 19 * Lv.N);
+    GAB(Lv.hcoef, 19 * hslot(Lv.d));
     GAB(Lv.lfh, Lv.N);
     GAB(Lv.rwh, Lv.N);
     if (l == L - 1) GAB(Lv.dinvh, Lv.N);
@@ -1507,7 +1507,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
     launch_line_factors<double>(Lv.d, Lv.mcoef, Lv.lf64, g.s);
-    launch_half_operator(Lv.N, Lv.mcoef, Lv.hcoef, l == g.L - 1 ? Lv.dinvh : nullptr, l == 0 ? Lv.dvalh : nullptr,
+    launch_half_operator(Lv.d, Lv.mcoef, Lv.hcoef, l == g.L - 1 ? Lv.dinvh : nullptr, l == 0 ? Lv.dvalh : nullptr,
                          g.s);
     launch_line_factors_half(Lv.d, Lv.hcoef, Lv.mcoef, Lv.lfh, g.s);
   }
@@ -2047,9 +2047,14 @@ int vfs_get_mg_half(vfs_ctx* ctx, int grid, int level, double* coef, double* lf,
   Level& L = g->lev[level];
   CK(cudaStreamSynchronize(g->s));
   if (coef) {
-    std::vector<__half> h(19 * L.N);
+    const size_t hs = hslot(L.d);
+    std::vector<__half> h(19 * hs);
     CK(cudaMemcpy(h.data(), L.hcoef, h.size() * sizeof(__half), cudaMemcpyDeviceToHost));
-    for (size_t q = 0; q < h.size(); q++) coef[q] = (double)__half2float(h[q]);
+    for (int m = 0; m < 19; m++)
+      for (size_t c = 0; c < L.N; c++) {
+        const int i = (int)(c % L.d.mx), j = (int)((c / L.d.mx) % L.d.my), k = (int)(c / ((size_t)L.d.mx * L.d.my));
+        coef[(size_t)m * L.N + c] = (double)__half2float(h[(size_t)m * hs + hidx(L.d, i, j, k)]);
+      }
   }
   std::vector<float> f(L.N);
   if (lf) {

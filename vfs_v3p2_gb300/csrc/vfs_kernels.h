@@ -45,10 +45,10 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
                  int cols = 0);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
-// FP16 diagonal-normalised copy of a level's aj-scaled operator (n cells), with
+// FP16 diagonal-normalised copy of a level's aj-scaled operator (hidx layout), with
 // optional fp32(1 / D) and fp32(D) per cell; its y-line pivots; its restriction
 // weights max(0, 1 - nvert_f) D_f / D_c
-int launch_half_operator(size_t n, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s);
+int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s);
 int launch_line_factors_half(const Dims& d, const __half* h, const double* mcoef, float* lf, cudaStream_t s);
 int launch_restrict_weights_half(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nvf,
                                  const double* mcf, const double* mcc, float* w, cudaStream_t s);
