@@ -138,7 +138,8 @@ int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, do
 // (immersed == 1).  mode 0: VolumeFlux(lUcor), poisson.c:2634-2828 with
 // immersed == 0, which zeroes every fluid / non-fluid face.
 // phase 0: (mode 1) zero faces with |U| <= 1e-10 and sum flux, area;
-// phase 1: apply the correction flux / area; phase 2: sums again.
+// phase 1: apply the correction flux / area and sum the corrected faces again
+// (the reference's second measuring pass, fused: same values, same order).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double nrm3(const double* v, size_t c) {
   return sqrt(v[3 * c] * v[3 * c] + v[3 * c + 1] * v[3 * c + 1] + v[3 * c + 2] * v[3 * c + 2]);
@@ -184,14 +185,16 @@ __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont
             flux += plus ? uu[c] : -uu[c];
             area += nrm3(mt[f], c);
           } else uu[c] = 0.;
-        } else if (phase == 1) {
-          if (fabs(uu[c]) > eps) {
-            if (plus) uu[c] -= nrm3(mt[f], c) * corr;
-            else uu[c] += nrm3(mt[f], c) * corr;
-          }
         } else {
+          // phase 1: correct, and measure the corrected face at once (the
+          // same values and order as a separate measuring pass)
+          const double nr = nrm3(mt[f], c);
+          if (fabs(uu[c]) > eps) {
+            if (plus) uu[c] -= nr * corr;
+            else uu[c] += nr * corr;
+          }
           flux += plus ? uu[c] : -uu[c];
-          area += nrm3(mt[f], c);
+          area += nr;
         }
       } else {
         bool plus, minus;
@@ -204,12 +207,9 @@ __global__ void __launch_bounds__(RB) k_vflux(Dims d, int mode, int phase, Ucont
           minus = nv[c] > VFS_THR && nv[nb[f]] < VFS_THR && lim0[f];
         }
         if (!(plus || minus)) continue;
-        if (phase == 1) {
-          uu[c] = 0.;
-        } else {
-          flux += plus ? uu[c] : -uu[c];
-          area += nrm3(mt[f], c);
-        }
+        if (phase == 1) uu[c] = 0.;  // and measured as such
+        flux += plus ? uu[c] : -uu[c];
+        area += nrm3(mt[f], c);
       }
     }
   }
@@ -228,7 +228,6 @@ int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nv
   k_vflux<<<nb, RB, 0, s>>>(d, mode, 0, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
   k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4); ++g_launches;
   k_vflux<<<nb, RB, 0, s>>>(d, mode, 1, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
-  k_vflux<<<nb, RB, 0, s>>>(d, mode, 2, u, nvert, csi, eta, zet, fa4, parts, nb8); ++g_launches;
   k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, fa4 + 2); ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -520,7 +520,9 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
   Level& F = g.lev[g.L - 1];
   dbg("scale_rhs", 0, launch_scale_in<double>(F.d, F.M + F.N * MP_AJ, g.b, g.bs, nullptr, s), s);
   dbg("bnorm", 0, launch_norm_init(g.st, g.bs, N, g.parts, 1, s), s);
-  dbg("residual0", 0, apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s), s);
+  // r0 = aj b - A phi; from a cold start phi = 0 and r0 = aj b exactly
+  if (warm) dbg("residual0", 0, apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s), s);
+  else CK(cudaMemcpyAsync(g.V, g.bs, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
   dbg("beta", 0, launch_norm_init(g.st, g.V, N, g.parts, 0, s), s);
   fg_open_cycle<T>(g, p, s);
   g.hstat[0] = 0;
