@@ -498,8 +498,11 @@ int launch_projection(const Dims& d, const double* pd, const double* M, const do
 // solution of [csi; eta; zet] ucat = q for the cell-centred contravariant
 // fluxes q.  The reference solves each cell's 3 x 3 system by Cramer's rule
 // (three FP64 divisions); the metric is static, so its inverse (adjugate /
-// determinant, same cofactors) is formed once per grid and the step applies
-// it with nine multiply-adds.  Agrees with Cramer's rule to rounding.
+// determinant, same cofactors) is formed once per grid, with the 1/2 of the
+// face average q = (U_f- + U_f+) / 2 folded in (an exact power-of-two
+// scale), and the step applies it with three multiplies and six FMAs (this
+// unit is built without automatic contraction; the FMAs are explicit).
+// Agrees with Cramer's rule to rounding.
 __global__ void k_inverse_metric(Dims d, const double* __restrict__ M, const double* __restrict__ nvert, double* minv) {
   const size_t N = ncell(d);
   GRID_LOOP(d) {
@@ -514,7 +517,7 @@ __global__ void k_inverse_metric(Dims d, const double* __restrict__ M, const dou
     const double* B = M + N * MP_ETA + 3 * c;
     const double* E = M + N * MP_ZET + 3 * c;
     const double det = A[0] * (B[1] * E[2] - B[2] * E[1]) - A[1] * (B[0] * E[2] - B[2] * E[0]) + A[2] * (B[0] * E[1] - B[1] * E[0]);
-    const double r = 1. / det;
+    const double r = 0.5 / det;
     o[0] = (B[1] * E[2] - B[2] * E[1]) * r;
     o[1] = -(A[1] * E[2] - A[2] * E[1]) * r;
     o[2] = (A[1] * B[2] - A[2] * B[1]) * r;
@@ -538,12 +541,12 @@ __global__ void k_contra2cart(Dims d, const double* __restrict__ minv, const dou
     if (!interior(d, i, j, k) || !(nvert[_t] < 0.1)) continue;
     const size_t c = _t;
     const double* m = minv + 9 * c;
-    const double q0 = 0.5 * (u.x[cidx(d, i - 1, j, k)] + u.x[c]);
-    const double q1 = 0.5 * (u.y[cidx(d, i, j - 1, k)] + u.y[c]);
-    const double q2 = 0.5 * (u.z[cidx(d, i, j, k - 1)] + u.z[c]);
-    ucat[3 * c] = m[0] * q0 + m[1] * q1 + m[2] * q2;
-    ucat[3 * c + 1] = m[3] * q0 + m[4] * q1 + m[5] * q2;
-    ucat[3 * c + 2] = m[6] * q0 + m[7] * q1 + m[8] * q2;
+    const double q0 = u.x[cidx(d, i - 1, j, k)] + u.x[c];  // twice the face averages
+    const double q1 = u.y[cidx(d, i, j - 1, k)] + u.y[c];
+    const double q2 = u.z[cidx(d, i, j, k - 1)] + u.z[c];
+    ucat[3 * c] = fma(m[2], q2, fma(m[1], q1, m[0] * q0));
+    ucat[3 * c + 1] = fma(m[5], q2, fma(m[4], q1, m[3] * q0));
+    ucat[3 * c + 2] = fma(m[8], q2, fma(m[7], q1, m[6] * q0));
   }
 }
 int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s) {

@@ -113,7 +113,7 @@ struct Grid {
   int L = 1, si = 0, sj = 0, sk = 0, immersed = 0;
   Level lev[MAXLEV];
   double* pd = nullptr;
-  double* minv = nullptr;   // per-cell inverse metric (9, row-major), Contra2Cart
+  double* minv = nullptr;   // per-cell inverse metric / 2 (9, row-major), Contra2Cart
   uint8_t* nb8 = nullptr;   // nvert as bytes when all are integers in [0, 127], else null
   uint8_t* nb8_buf = nullptr;  // storage behind nb8
   double* mtmp = nullptr;   // metric formation scratch (9 N)
