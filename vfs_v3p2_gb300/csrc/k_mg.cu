@@ -266,10 +266,16 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #define VFS_SMOOTH_MINB 4  // resident blocks per SM the register budget must allow
 #endif
 #ifndef VFS_SMOOTH_MINB_HALF
-#define VFS_SMOOTH_MINB_HALF 3  // the same for the 19-slot FP16 operator (two cells per thread: more registers)
+#define VFS_SMOOTH_MINB_HALF 3  // the same for the two-cells-per-thread FP16 sweep (more registers)
+#endif
+#ifndef VFS_SMOOTH_PAIR_MAXN
+#define VFS_SMOOTH_PAIR_MAXN 0  // 11-slot FP16 levels up to this many cells sweep two cells per thread (measured: none faster)
 #endif
 #ifndef VFS_SMOOTH_U
-#define VFS_SMOOTH_U 1  // cells whose loads one thread issues together in phase 1
+#define VFS_SMOOTH_U 1  // cells whose loads one thread issues together in phase 1 (large levels)
+#endif
+#ifndef VFS_SMOOTH_U_SMALL
+#define VFS_SMOOTH_U_SMALL 2  // the same on levels with fewer than two blocks per SM
 #endif
 #ifndef VFS_SMOOTH_TWMAX
 #define VFS_SMOOTH_TWMAX 32  // columns per block
@@ -418,10 +424,11 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
   }
 }
 
-template <unsigned MASK, typename T, typename TC>
-__global__ void __launch_bounds__(VFS_SMOOTH_NT, (std::is_same<TC, __half>::value && MASK == MASK_ALL)
-                                                     ? VFS_SMOOTH_MINB_HALF
-                                                     : VFS_SMOOTH_MINB)
+// UU: cells whose loads one thread issues together in phase 1 (2 on levels
+// with fewer than two blocks per SM, where the looser register budget costs
+// no occupancy and halves the serial chain of round trips).
+template <unsigned MASK, typename T, typename TC, bool PAIR, int UU>
+__global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (UU > 1 ? 2 : VFS_SMOOTH_MINB))
     k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
              T* __restrict__ xo, T omega, int TW) {
   if (skipped(A.skip)) return;
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, (std::is_same<TC, __half>::valu
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
   const int nt = TW * nj;
-  constexpr int U = VFS_SMOOTH_U;
+  constexpr int U = UU;
   // L2 prefetch of the rows a warp will stream PF iterations later: the
   // loads in flight are bounded by registers (4 bytes each), the prefetches
   // are not, so they keep more of HBM's latency-bandwidth product busy.  One
@@ -478,14 +485,16 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, (std::is_same<TC, __half>::valu
     e = max(0, min(e, N - 32));
     asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)e * es));
   };
-  if constexpr (NRM && MASK == MASK_ALL) {
-    // 19-slot FP16 operator: one thread takes the cell pair (ia, ia + 1),
-    // ia = i0 + 2 p odd, whose coefficients of a slot are one aligned word of
-    // the hidx layout; x is read once per column (L, A, B, R = ia - 1 .. ia + 2,
-    // the periodic wraps and the clamp of the per-cell path applied) and
-    // shared by the two cells.  Per cell the arithmetic is the per-cell
-    // path's.  (Measured: faster than one cell per thread for 19 slots,
-    // slower for 11, where one cell per thread keeps 4 blocks per SM.)
+  static_assert(!PAIR || NRM, "the two-cells-per-thread sweep reads the FP16 layout");
+  if constexpr (PAIR) {
+    // FP16 operator, two cells per thread: one thread takes the cell pair
+    // (ia, ia + 1), ia = i0 + 2 p odd, whose coefficients of a slot are one
+    // aligned word of the hidx layout; x is read once per column (L, A, B,
+    // R = ia - 1 .. ia + 2, the periodic wraps and the clamp of the per-cell
+    // path applied) and shared by the two cells.  Per cell the arithmetic is
+    // the per-cell path's.  Chosen for the 19-slot operator and for smaller
+    // 11-slot levels (half the serial loads per thread); the large 11-slot
+    // levels measured faster one cell per thread at 4 blocks per SM.
     smooth_pairs<MASK, T>(A, lf, xi, b, su, sp, sl, i0, k, TW);
   } else {
     // Phase 1 in batches of U cells per thread: every load of the batch is
@@ -565,22 +574,40 @@ static int smooth_tw(int ni, int nj, int nk, int cols) {
   return tw;
 }
 
-template <unsigned MASK, typename T, typename TC>
-static void smooth_attrs() {
-  cudaFuncSetAttribute(k_smooth<MASK, T, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+template <unsigned MASK, typename T, typename TC, bool PAIR, int UU>
+static void smooth_attrs1() {
+  cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (VFS_SMOOTH_CARVE >= 0)
-    cudaFuncSetAttribute(k_smooth<MASK, T, TC>, cudaFuncAttributePreferredSharedMemoryCarveout, VFS_SMOOTH_CARVE);
+    cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         VFS_SMOOTH_CARVE);
+}
+template <unsigned MASK, typename T, typename TC, bool PAIR>
+static void smooth_attrs() {
+  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U>();
+  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL>();
+}
+
+// One launch of the sweep kernel with the per-level choices: U cells per
+// thread batch (small levels) and the instantiation.
+template <unsigned MASK, typename T, typename TC, bool PAIR>
+static void smooth_launch(bool small, dim3 g, size_t sm, cudaStream_t s, const OpView<T>& A, const T* lf, const T* xi,
+                          const T* b, T* xo, T omega, int tw) {
+  if (small && !PAIR)
+    k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  else k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
 }
 
 template <typename T>
-int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols) {
+int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols,
+                  bool solo) {
   static bool attr = false;
   if (!attr) {
-    smooth_attrs<MASK_CH, T, T>();
-    smooth_attrs<MASK_ALL, T, T>();
+    smooth_attrs<MASK_CH, T, T, false>();
+    smooth_attrs<MASK_ALL, T, T, false>();
     if constexpr (sizeof(T) == 4) {
-      smooth_attrs<MASK_CH, T, __half>();
-      smooth_attrs<MASK_ALL, T, __half>();
+      smooth_attrs<MASK_CH, T, __half, false>();
+      smooth_attrs<MASK_CH, T, __half, true>();
+      smooth_attrs<MASK_ALL, T, __half, true>();
     }
     attr = true;
   }
@@ -589,17 +616,23 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   const size_t sm = (size_t)3 * tw * nj * sizeof(T);
   dim3 g((ni + tw - 1) / tw, nk);
   const bool ch = fits_ch(A.mask);
+  // two-cell batches only when the sweep has the GPU to itself (one grid
+  // solving) and fewer than two blocks per SM: with other grids' kernels
+  // beside it (batch, serving) the looser register budget costs concurrency
+  const bool small = solo && (size_t)g.x * g.y < 2 * 152;
   bool done = false;
   if constexpr (sizeof(T) == 4) {
     if (A.hcoef) {
-      if (ch) k_smooth<MASK_CH, T, __half><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
-      else k_smooth<MASK_ALL, T, __half><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+      if (!ch) smooth_launch<MASK_ALL, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+      else if (ncell(A.d) <= (size_t)VFS_SMOOTH_PAIR_MAXN)
+        smooth_launch<MASK_CH, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+      else smooth_launch<MASK_CH, T, __half, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
       done = true;
     }
   }
   if (!done) {
-    if (ch) k_smooth<MASK_CH, T, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
-    else k_smooth<MASK_ALL, T, T><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+    if (ch) smooth_launch<MASK_CH, T, T, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+    else smooth_launch<MASK_ALL, T, T, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
   }
   ++g_launches;
   return (int)cudaGetLastError();
@@ -1023,7 +1056,7 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
 
 #define INST(T)                                                                                                        \
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
-  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int);            \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int, bool);            \
   template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
   template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const T*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \

@@ -147,8 +147,9 @@ struct Grid {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
+  bool solo = false;  // the grid's solve runs alone (set by the driver before it issues work)
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
-  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1;
+  int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -332,6 +333,7 @@ struct MGCfg {
   int nu1c, nu2c;  // sweeps on the levels below the finest
   int top;         // index of the finest level
   bool half;       // FP16 normalised operator (FP32 multigrid only)
+  bool solo;       // the grid's solve runs alone
   int pre(int l) const { return l == top ? nu1 : nu1c; }
   int post(int l) const { return l == top ? nu2 : nu2c; }
 };
@@ -347,9 +349,9 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
 void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols,
-                   cudaStream_t s) {
+                   bool solo, cudaStream_t s) {
   const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
-  int rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols);
+  int rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo);
   // the coefficient slots (FP16 or T), x, b and 1/m read, x written
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
   if (probe) g_probe.end(s, (double)n_interior(A.d) * (slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)));
@@ -383,7 +385,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     T* cur = nullptr;
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      launch_smooth<T>(A, lf, cur, b, o, (T)c.omega_c, s, c.cols);
+      launch_smooth<T>(A, lf, cur, b, o, (T)c.omega_c, s, c.cols, c.solo);
       cur = o;
     }
     return cur;
@@ -392,7 +394,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   T* cur = nullptr;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, c.solo, s);
     cur = o;
   }
   Level& C = g.lev[l - 1];
@@ -410,7 +412,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, c.solo, s);
     cur = o;
   }
   return cur;
@@ -428,6 +430,7 @@ MGCfg mgcfg(const vfs_solve_params& p, int top) {
   c.nu2c = p.nu2_coarse >= 0 ? p.nu2_coarse : p.nu2;
   c.top = top;
   c.half = p.precision == VFS_MIXED && p.mg_half != 0;
+  c.solo = false;
   return c;
 }
 
@@ -543,7 +546,8 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
-  const MGCfg mc = mgcfg(p, g.L - 1);
+  MGCfg mc = mgcfg(p, g.L - 1);
+  mc.solo = g.solo;
   const float* dinv = dinv_sel<T>(F, mc.half);
   vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mc, skip, s);
   {
@@ -586,7 +590,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
       g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse &&
-      g.ig_half == p.mg_half) {
+      g.ig_half == p.mg_half && g.ig_solo == (int)g.solo) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -614,6 +618,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_nu1c = p.nu1_coarse;
   g.ig_nu2c = p.nu2_coarse;
   g.ig_half = p.mg_half;
+  g.ig_solo = (int)g.solo;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -939,6 +944,7 @@ void wait_any(std::vector<Job*>& jobs) {
 // Run jobs to completion, each on its grid's stream (single solves; the
 // serving loop uses job_advance directly).
 int run_jobs_streams(vfs_ctx* ctx, std::vector<Job*>& jobs) {
+  for (Job* J : jobs) J->g->solo = jobs.size() == 1;
   for (;;) {
     int moved = 0, live = 0;
     for (Job* J : jobs) {
@@ -1025,6 +1031,7 @@ int batch_after_tick(vfs_ctx* ctx, Job& J, cudaEvent_t tick, bool have_prev) {
 }
 
 int run_jobs_batch(vfs_ctx* ctx, std::vector<Job*>& jobs, cudaStream_t s0) {
+  for (Job* J : jobs) J->g->solo = false;
   cudaEvent_t fork = nullptr, ticks[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> joins;
   BatchGraph bg;
@@ -1783,6 +1790,7 @@ int vfs_projection_step(vfs_ctx* ctx, int grid, double* ucont_inout, double* p_i
   if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
   if (g.m && p->restart > g.m) return fail(ctx, VFS_ERR_ARG, "restart length cannot grow after the first solve");
   if (g.busy) return fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight");
+  g.solo = false;  // requests share the GPU
   Job J;
   J.g = &g;
   J.p = *p;

@@ -40,9 +40,11 @@ template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s);
 // one damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi); xi == nullptr means xi = 0;
 // lf = precomputed y-line Thomas pivots 1/m_j (N of T)
+// solo: this grid's solve has the GPU to itself (allows the low-occupancy
+// variant on small levels)
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s,
-                 int cols = 0);
+                 int cols = 0, bool solo = false);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
 // FP16 diagonal-normalised copy of a level's aj-scaled operator (hidx layout), with
