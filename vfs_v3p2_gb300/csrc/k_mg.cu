@@ -619,7 +619,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   // two-cell batches only when the sweep has the GPU to itself (one grid
   // solving) and fewer than two blocks per SM: with other grids' kernels
   // beside it (batch, serving) the looser register budget costs concurrency
-  const bool small = solo && (size_t)g.x * g.y < 2 * 152;
+  const bool small = sizeof(T) == 4 && solo && (size_t)g.x * g.y < 2 * 152;  // (FP64: spills at two cells)
   bool done = false;
   if constexpr (sizeof(T) == 4) {
     if (A.hcoef) {
