@@ -121,6 +121,9 @@ typedef struct {
   int div_limited; /* 1: div_tol was not reachable (the masked residual max stopped
                       falling: FP64 rounding floor of the grid) and the solve
                       stopped at the rtol criterion */
+  int mg_half_used; /* 1: the multigrid ran on the FP16 normalised operator
+                       (mixed precision, mg_half = 1, and every normalised
+                       coefficient of the grid within 6e4; else FP32) */
 } vfs_solve_info;
 
 /* Context (device, streams, HBM budget). */

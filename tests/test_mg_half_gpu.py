@@ -123,6 +123,7 @@ def test_half_solve_matches_fp32_storage(gpu_ctx, orth):
             gpu_ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
             info, divmax = gpu_ctx.projection_step(gid, params, u, None)
             assert info["converged"] and info["relres"] < 1e-11 and divmax < 1e-8, (half, info, divmax)
+            assert info["mg_half_used"] == bool(half)
             out[half] = (info, gpu_ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape), u)
         (i0, phi0, u0), (i1, phi1, u1) = out[0], out[1]
         assert abs(i1["iterations"] - i0["iterations"]) <= 1, (i0, i1)

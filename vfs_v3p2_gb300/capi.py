@@ -68,11 +68,13 @@ class SolveParams(ctypes.Structure):
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("relres", ctypes.c_double),
-                ("bnorm", ctypes.c_double), ("time_ms", ctypes.c_double), ("div_limited", ctypes.c_int)]
+                ("bnorm", ctypes.c_double), ("time_ms", ctypes.c_double), ("div_limited", ctypes.c_int),
+                ("mg_half_used", ctypes.c_int)]
 
     def as_dict(self):
         return dict(iterations=self.iterations, converged=bool(self.converged), relres=self.relres,
-                    bnorm=self.bnorm, time_ms=self.time_ms, div_limited=bool(self.div_limited))
+                    bnorm=self.bnorm, time_ms=self.time_ms, div_limited=bool(self.div_limited),
+                    mg_half_used=bool(self.mg_half_used))
 
 
 class Request(ctypes.Structure):

@@ -683,9 +683,11 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // what the coarse-grid correction relies on.  Non-fluid rows are all zero.
 // Optional outputs: dinv = fp32(1 / D) and dval = fp32(D), 0 on non-fluid
 // rows (the finest level's input scaling, the coarsest level's dense solve).
+// A ratio or correction beyond 6e4 (near the FP16 maximum, 65504) sets
+// *range: the solver then keeps the FP32 operator for the grid.
 // ---------------------------------------------------------------------------
 __global__ void k_half_operator(Dims d, const double* __restrict__ mcoef, __half* __restrict__ h,
-                                float* __restrict__ dinv, float* __restrict__ dval) {
+                                float* __restrict__ dinv, float* __restrict__ dval, unsigned* range) {
   const size_t n = ncell(d), hs = hslot(d);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(c % d.mx), j = (int)((c / d.mx) % d.my), k = (int)(c / ((size_t)d.mx * d.my));
@@ -694,18 +696,21 @@ __global__ void k_half_operator(Dims d, const double* __restrict__ mcoef, __half
     double delta = 0.;
     for (int m = 1; m < 19; m++) {
       const double a = D != 0. ? mcoef[(size_t)m * n + c] / D : 0.;
+      if (!(fabs(a) <= 6.e4)) atomicOr(range, 1u);
       const __half hm = __double2half(a);
       delta = delta + (a - (double)__half2float(hm));
       h[(size_t)m * hs + hc] = hm;
     }
+    if (!(fabs(delta) <= 6.e4)) atomicOr(range, 1u);
     h[hc] = __double2half(delta);
     if (dinv) dinv[c] = D != 0. ? (float)(1. / D) : 0.f;
     if (dval) dval[c] = (float)D;
   }
 }
-int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s) {
+int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, unsigned* range,
+                         cudaStream_t s) {
   const size_t nb = (ncell(d) + 255) / 256;
-  k_half_operator<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(d, mcoef, h, dinv, dval); ++g_launches;
+  k_half_operator<<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, s>>>(d, mcoef, h, dinv, dval, range); ++g_launches;
   return (int)cudaGetLastError();
 }
 

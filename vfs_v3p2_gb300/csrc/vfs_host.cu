@@ -148,6 +148,7 @@ struct Grid {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   bool lhs = false;
   bool solo = false;  // the grid's solve runs alone (set by the driver before it issues work)
+  bool half_ok = true;  // the FP16 operator represents every level (else mg_half runs the FP32 one)
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
   int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
   unsigned long long ig_kernels = 0;  // kernels per replay
@@ -418,7 +419,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   return cur;
 }
 
-MGCfg mgcfg(const vfs_solve_params& p, int top) {
+MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
   MGCfg c;
   c.nu1 = p.nu1;
   c.nu2 = p.nu2;
@@ -429,7 +430,7 @@ MGCfg mgcfg(const vfs_solve_params& p, int top) {
   c.nu1c = p.nu1_coarse >= 0 ? p.nu1_coarse : p.nu1;
   c.nu2c = p.nu2_coarse >= 0 ? p.nu2_coarse : p.nu2;
   c.top = top;
-  c.half = p.precision == VFS_MIXED && p.mg_half != 0;
+  c.half = p.precision == VFS_MIXED && p.mg_half != 0 && half_ok;
   c.solo = false;
   return c;
 }
@@ -441,9 +442,9 @@ int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T
             cudaStream_t s, bool with_input = true) {
   Level& F = g.lev[g.L - 1];
   T* bf = bbuf<T>(F);
-  const float* dinv = dinv_sel<T>(F, mgcfg(p, g.L - 1).half);
+  const float* dinv = dinv_sel<T>(F, mgcfg(p, g.L - 1, g.half_ok).half);
   if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s, dinv), s);
-  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p, g.L - 1), skip, s);
+  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p, g.L - 1, g.half_ok), skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
 }
@@ -489,7 +490,7 @@ void fg_open_cycle(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   Level& F = g.lev[g.L - 1];
   dbg("v0", 0, launch_vec_scale_first(g.st, g.V, g.V, N, s), s);
   dbg("scale_in", 0,
-      launch_scale_in<T>(F.d, nullptr, g.V, bbuf<T>(F), &g.st->done, s, dinv_sel<T>(F, mgcfg(p, g.L - 1).half)), s);
+      launch_scale_in<T>(F.d, nullptr, g.V, bbuf<T>(F), &g.st->done, s, dinv_sel<T>(F, mgcfg(p, g.L - 1, g.half_ok).half)), s);
 }
 
 template <typename T>
@@ -546,7 +547,7 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
-  MGCfg mc = mgcfg(p, g.L - 1);
+  MGCfg mc = mgcfg(p, g.L - 1, g.half_ok);
   mc.solo = g.solo;
   const float* dinv = dinv_sel<T>(F, mc.half);
   vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mc, skip, s);
@@ -851,6 +852,7 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     J.info.iterations = J.iters;
     J.info.converged = rel_ok && (div_ok || floor);
     J.info.div_limited = (!div_ok && floor) ? 1 : 0;
+    J.info.mg_half_used = mgcfg(J.p, g.L - 1, g.half_ok).half ? 1 : 0;
     J.info.bnorm = h.bnorm;
     J.info.relres = h.bnorm > 0. ? rn / h.bnorm : 0.;
     J.phase = J_POST;
@@ -1507,7 +1509,8 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
   double* gt = nullptr;
   unsigned* dmask = nullptr;
   CK(cudaMalloc(&gt, 9 * N * sizeof(double)));
-  CK(cudaMalloc(&dmask, sizeof(unsigned)));
+  CK(cudaMalloc(&dmask, 2 * sizeof(unsigned)));
+  CK(cudaMemsetAsync(dmask + 1, 0, sizeof(unsigned), g.s));
   for (int l = 0; l < g.L; l++) {
     Level& Lv = g.lev[l];
     launch_gtensor(Lv.d, Lv.M, gt, g.s);
@@ -1517,7 +1520,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
     launch_line_factors<double>(Lv.d, Lv.mcoef, Lv.lf64, g.s);
     launch_half_operator(Lv.d, Lv.mcoef, Lv.hcoef, l == g.L - 1 ? Lv.dinvh : nullptr, l == 0 ? Lv.dvalh : nullptr,
-                         g.s);
+                         dmask + 1, g.s);
     launch_line_factors_half(Lv.d, Lv.hcoef, Lv.mcoef, Lv.lfh, g.s);
   }
   CK(cudaMemsetAsync(g.lev[0].rwh, 0, g.lev[0].N * sizeof(float), g.s));
@@ -1526,7 +1529,10 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
                                  g.lev[l - 1].mcoef, g.lev[l].rwh, g.s);
   Level& F = g.lev[g.L - 1];
   launch_proj_dots(F.d, F.M, g.pd, g.s);
+  unsigned range = 0;
+  CK(cudaMemcpyAsync(&range, dmask + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
   CK(cudaStreamSynchronize(g.s));
+  g.half_ok = range == 0;
   cudaFree(gt);
   cudaFree(dmask);
   // coarsest level: dense inverse of A + sigma e e^T when small enough

@@ -50,7 +50,9 @@ int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t 
 // FP16 diagonal-normalised copy of a level's aj-scaled operator (hidx layout), with
 // optional fp32(1 / D) and fp32(D) per cell; its y-line pivots; its restriction
 // weights max(0, 1 - nvert_f) D_f / D_c
-int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, cudaStream_t s);
+// (*range |= 1 when a normalised coefficient or correction exceeds 6e4)
+int launch_half_operator(const Dims& d, const double* mcoef, __half* h, float* dinv, float* dval, unsigned* range,
+                         cudaStream_t s);
 int launch_line_factors_half(const Dims& d, const __half* h, const double* mcoef, float* lf, cudaStream_t s);
 int launch_restrict_weights_half(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nvf,
                                  const double* mcf, const double* mcc, float* w, cudaStream_t s);
