@@ -303,22 +303,25 @@ __device__ __forceinline__ void smooth_pairs(const OpView<T>& A, const T* __rest
                                              const T* __restrict__ b, T* su, T* sp, T* sl, int i0, int k, int TW) {
   const Dims d = A.d;
   const __half* __restrict__ h = A.hcoef;
-  const int nj = d.my - 2, np = TW >> 1, nitems = nj * np;
+  const int nj = d.my - 2, np = TW >> 1;
   const int sy = d.mx, sz = d.mx * d.my;
   const size_t hs = hslot(d);
   const int lastodd = d.mx - 2 - ((d.mx - 1) & 1);  // largest odd column <= mx - 2
   const int kk[3] = {(k == 1 && d.kp) ? d.mz - 2 : k - 1, k, (k == d.mz - 2 && d.kp) ? 1 : k + 1};
-  for (int it = threadIdx.x; it < nitems; it += VFS_SMOOTH_NT) {
-    const int jl = it / np, p = it - jl * np;
+  // np divides the block: the thread keeps its pair p and steps rows
+  const int p = threadIdx.x % np, jstep = VFS_SMOOTH_NT / np;
+  const int ia = i0 + 2 * p, ib = ia + 1;
+  const int ca = min(ia, d.mx - 2), cb = min(ib, d.mx - 2);
+  const int la = min(ia, lastodd);  // the aligned word holding the pair (clamped)
+  const int cL = (ca == 1 && d.ip) ? d.mx - 2 : ca - 1;
+  const int cR = (cb == d.mx - 2 && d.ip) ? 1 : cb + 1;
+  const bool sep = ca < cb;  // two distinct cells (else b is the clamped copy of a)
+  const size_t hrow1 = hidx(d, la, 1, k);
+  const int hp = hpitch(d);
+  for (int jl = threadIdx.x / np; jl < nj; jl += jstep) {
     const int j = 1 + jl;
-    const int ia = i0 + 2 * p, ib = ia + 1;
-    const int ca = min(ia, d.mx - 2), cb = min(ib, d.mx - 2);
-    const int la = min(ia, lastodd);  // the aligned word holding the pair (clamped)
-    const int cL = (ca == 1 && d.ip) ? d.mx - 2 : ca - 1;
-    const int cR = (cb == d.mx - 2 && d.ip) ? 1 : cb + 1;
-    const bool sep = ca < cb;  // two distinct cells (else b is the clamped copy of a)
     const int jm = (j == 1 && d.jp) ? nj : j - 1, jp1 = (j == nj && d.jp) ? 1 : j + 1;
-    const size_t hrow = hidx(d, la, j, k);
+    const size_t hrow = hrow1 + (size_t)jl * hp;
     __half2 cw[19];
     T xL[3][3], xA[3][3], xB[3][3], xR[3][3];  // [dk + 1][dj + 1]
 #pragma unroll
@@ -427,10 +430,13 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
 // UU: cells whose loads one thread issues together in phase 1 (2 on levels
 // with fewer than two blocks per SM, where the looser register budget costs
 // no occupancy and halves the serial chain of round trips).
-template <unsigned MASK, typename T, typename TC, bool PAIR, int UU>
+// ZG: the zero-initial-guess sweep (xi == nullptr), its own instantiation so
+// that its phase 1 (four cells a batch) leaves the others' registers alone.
+template <unsigned MASK, typename T, typename TC, bool PAIR, int UU, bool ZG>
 __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (UU > 1 ? 2 : VFS_SMOOTH_MINB))
-    k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi, const T* __restrict__ b,
+    k_smooth(OpView<T> A, const T* __restrict__ lf, const T* __restrict__ xi_arg, const T* __restrict__ b,
              T* __restrict__ xo, T omega, int TW) {
+  const T* __restrict__ xi = ZG ? nullptr : xi_arg;
   if (skipped(A.skip)) return;
   // NRM: the FP16 diagonal-normalised operator (b is divided by D, non-fluid
   // rows have 1/m = 0 so their delta is 0 without a test)
@@ -446,7 +452,6 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
   const int N = (int)ncell(d);
   const int i0 = 1 + blockIdx.x * TW;
   const int k = 1 + blockIdx.y;
-  const int nt = TW * nj;
   constexpr int U = UU;
   // L2 prefetch of the rows a warp will stream PF iterations later: the
   // loads in flight are bounded by registers (4 bytes each), the prefetches
@@ -503,14 +508,108 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
     // finite factors and are selected out).  The line factors a_j/m_j and c'_j
     // are formed from the SP and NP coefficients the stencil loads anyway; only
     // 1/m_j is stored.  With xi == nullptr (zero initial guess) the residual is
-    // b and only CP, SP, NP of the stencil are loaded.
-    for (int base = threadIdx.x; base < nt; base += U * VFS_SMOOTH_NT) {
+    // b and only CP, SP, NP of the stencil are loaded, four cells a batch
+    // (few registers a cell: the serial chain of round trips is a quarter).
+    // TW divides the block: a thread keeps its column (il) and steps rows by
+    // jstep; its cell and coefficient offsets advance by one row pitch.
+    const int il = threadIdx.x % TW, jl0 = threadIdx.x / TW, jstep = VFS_SMOOTH_NT / TW;
+    const int ic = min(i0 + il, d.mx - 2);
+    const bool col_in = i0 + il <= d.mx - 2;
+    const int c1 = k * d.mx * d.my + d.mx + ic;  // cell (ic, 1, k)
+    size_t cstride, cc1;                          // coefficient slot stride and (ic, 1, k) offset
+    int crow;                                     // coefficient row pitch
+    if constexpr (NRM) {
+      cstride = hslot(d);
+      cc1 = hidx(d, ic, 1, k);
+      crow = hpitch(d);
+    } else {
+      cstride = (size_t)N;
+      cc1 = (size_t)c1;
+      crow = d.mx;
+    }
+    if constexpr (ZG) {
+      constexpr int U0 = 4;
+      for (int jb = jl0; jb < nj; jb += U0 * jstep) {
+        TC ccp[U0], csp[U0], cnp[U0];
+        T bb[U0], inv[U0];
+  #pragma unroll
+        for (int u = 0; u < U0; u++) {
+          const int jl = min(jb + u * jstep, nj - 1);
+          const int c = c1 + jl * d.mx;
+          const size_t cc = cc1 + (size_t)jl * crow;
+          if constexpr (!NRM) ccp[u] = __ldg(coef + cc);
+          csp[u] = __ldg(coef + (size_t)SP * cstride + cc);
+          cnp[u] = __ldg(coef + (size_t)NP * cstride + cc);
+          bb[u] = __ldg(b + c);
+          inv[u] = __ldg(lf + c);
+        }
+  #pragma unroll
+        for (int u = 0; u < U0; u++) {
+          const int jl = jb + u * jstep;
+          if (jl >= nj) break;
+          const int idx = jl * TW + il;
+          const bool live = col_in && (NRM || to_acc<T>(ccp[u]) != T(0));
+          const T a = jl > 0 ? to_acc<T>(csp[u]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cnp[u]) : T(0);
+          su[idx] = live ? (bb[u] - T(0)) * inv[u] : T(0);
+          sp[idx] = live ? a * inv[u] : T(0);
+          sl[idx] = live ? cn * inv[u] : T(0);
+        }
+      }
+    } else
+    if constexpr (sizeof(T) == 8) {
+      // FP64: the thread's column, i / k offsets and base addresses
+      // hoisted (fewer integer instructions, measured faster); FP32 keeps
+      // the per-cell index arithmetic, whose registers the 64-register
+      // budget rather spends on loads in flight (measured faster there).
+    {
+      // x offsets of the stencil's i and k neighbours (periodic seams
+      // folded in) are fixed for the thread; the j ones depend on the row
+      const int sz = d.mx * d.my;
+      const int oi[3] = {(ic == 1 && d.ip) ? d.mx - 3 : -1, 0, (ic == d.mx - 2 && d.ip) ? 3 - d.mx : 1};
+      const int ok[3] = {((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, 0, ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz};
+    for (int jb = jl0; jb < nj; jb += U * jstep) {
+      if (PF > 0 && sizeof(T) == 4 && TW == 32) prefetch_row(1 + jb + PF * U * jstep);
+      TC cv[U][19];
+      T xv[U][19], bb[U], inv[U];
+  #pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int jl = min(jb + u * jstep, nj - 1);
+        const int j = 1 + jl;
+        const int c = c1 + jl * d.mx;
+        const size_t cc = cc1 + (size_t)jl * crow;
+        const int oj[3] = {((j == 1 && d.jp) ? d.my - 3 : -1) * d.mx, 0, ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * d.mx};
+  #pragma unroll
+        for (int m = 0; m < 19; m++) {
+          if (MASK & (1u << m)) {
+            cv[u][m] = __ldg(coef + (size_t)m * cstride + cc);
+            xv[u][m] = __ldg(xi + (c + oi[slot_di(m) + 1] + oj[slot_dj(m) + 1] + ok[slot_dk(m) + 1]));
+          }
+        }
+        bb[u] = __ldg(b + c);
+        inv[u] = __ldg(lf + c);
+      }
+  #pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int jl = jb + u * jstep;
+        if (jl >= nj) break;
+        const int idx = jl * TW + il;
+        const bool live = col_in && (NRM || to_acc<T>(cv[u][CP]) != T(0));
+        const T ax = row_dot<MASK, T>(cv[u], xv[u]);
+        const T a = jl > 0 ? to_acc<T>(cv[u][SP]) : T(0), cn = jl < nj - 1 ? to_acc<T>(cv[u][NP]) : T(0);
+        su[idx] = live ? (bb[u] - ax) * inv[u] : T(0);
+        sp[idx] = live ? a * inv[u] : T(0);
+        sl[idx] = live ? cn * inv[u] : T(0);
+      }
+    }
+    }
+    } else {
+    for (int base = threadIdx.x; base < TW * nj; base += U * VFS_SMOOTH_NT) {
       if (PF > 0 && sizeof(T) == 4 && TW == 32) prefetch_row(1 + (base + PF * U * VFS_SMOOTH_NT) / TW);
       TC cv[U][19];
       T xv[U][19], bb[U], inv[U];
   #pragma unroll
       for (int u = 0; u < U; u++) {
-        const int idx = min(base + u * VFS_SMOOTH_NT, nt - 1);
+        const int idx = min(base + u * VFS_SMOOTH_NT, TW * nj - 1);
         const int il = idx % TW, jl = idx / TW;
         const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
         const int c = k * d.mx * d.my + j * d.mx + i;
@@ -531,7 +630,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
   #pragma unroll
       for (int u = 0; u < U; u++) {
         const int idx = base + u * VFS_SMOOTH_NT;
-        if (idx >= nt) break;
+        if (idx >= TW * nj) break;
         const int jl = idx / TW;
         const bool live = (i0 + idx % TW <= d.mx - 2) && (NRM || to_acc<T>(cv[u][CP]) != T(0));
         const T ax = xi ? row_dot<MASK, T>(cv[u], xv[u]) : T(0);
@@ -541,6 +640,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
         sl[idx] = live ? cn * inv[u] : T(0);
       }
     }
+    }
   }
   __syncthreads();
   if (threadIdx.x < TW) line_solve<T>(su, sp, sl, nj, TW, threadIdx.x);
@@ -549,7 +649,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
   // together (columns past the last one are clamped and not stored).
   constexpr int U3 = VFS_SMOOTH_U3;
 #pragma unroll U3
-  for (int idx = threadIdx.x; idx < nt; idx += VFS_SMOOTH_NT) {
+  for (int idx = threadIdx.x; idx < TW * nj; idx += VFS_SMOOTH_NT) {
     const int il = idx % TW, jl = idx / TW;
     const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
     const int c = k * d.mx * d.my + j * d.mx + i;
@@ -574,17 +674,18 @@ static int smooth_tw(int ni, int nj, int nk, int cols) {
   return tw;
 }
 
-template <unsigned MASK, typename T, typename TC, bool PAIR, int UU>
+template <unsigned MASK, typename T, typename TC, bool PAIR, int UU, bool ZG>
 static void smooth_attrs1() {
-  cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU, ZG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (VFS_SMOOTH_CARVE >= 0)
-    cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU, ZG>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          VFS_SMOOTH_CARVE);
 }
 template <unsigned MASK, typename T, typename TC, bool PAIR>
 static void smooth_attrs() {
-  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U>();
-  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL>();
+  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U, false>();
+  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL, false>();
+  smooth_attrs1<MASK, T, TC, PAIR, VFS_SMOOTH_U, true>();
 }
 
 // One launch of the sweep kernel with the per-level choices: U cells per
@@ -592,9 +693,11 @@ static void smooth_attrs() {
 template <unsigned MASK, typename T, typename TC, bool PAIR>
 static void smooth_launch(bool small, dim3 g, size_t sm, cudaStream_t s, const OpView<T>& A, const T* lf, const T* xi,
                           const T* b, T* xo, T omega, int tw) {
-  if (small && !PAIR)
-    k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
-  else k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  if (!xi)
+    k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U, true><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  else if (small && !PAIR)
+    k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U_SMALL, false><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
+  else k_smooth<MASK, T, TC, PAIR, VFS_SMOOTH_U, false><<<g, VFS_SMOOTH_NT, sm, s>>>(A, lf, xi, b, xo, omega, tw);
 }
 
 template <typename T>
