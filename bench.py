@@ -62,9 +62,9 @@ def parse():
                          "measured 9 vs 10 iterations on the sphere workload)")
     ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
     ap.add_argument("--smooth-cols", type=int, default=0, help="smoother tile columns (0: automatic)")
-    ap.add_argument("--mg-half", type=int, default=1, choices=[0, 1],
-                    help="multigrid operator stored as FP16 normalised by its diagonal (1) or FP32 (0); "
-                         "FP32 arithmetic either way")
+    ap.add_argument("--mg-half", type=int, default=0, choices=[0, 1],
+                    help="multigrid stencil coefficients stored in FP32 (0, the specified form) or as FP16 "
+                         "normalised by their diagonal (1); FP32 arithmetic either way")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")

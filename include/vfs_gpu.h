@@ -92,12 +92,14 @@ typedef struct {
                                   iterations on one large grid (5 / 5 on
                                   256x128x128) but lengthen small grids' latency-
                                   bound cycles in a batch */
-  int mg_half;  /* VFS_MIXED only: 1 (the default) = the multigrid levels'
-                   operator is stored as FP16 normalised by its diagonal,
-                   with an FP16 centre-slot correction that keeps every row
-                   sum (the arithmetic stays FP32; each smoothing sweep
-                   streams 38 instead of 60 bytes per cell); 0 = stored FP32.
-                   The FP64 FGMRES operator is the same either way. */
+  int mg_half;  /* VFS_MIXED only: 0 (the default) = the multigrid levels'
+                   stencil coefficients are stored in FP32; 1 = stored as
+                   FP16 normalised by their diagonal, with an FP16
+                   centre-slot correction that keeps every row sum (the
+                   arithmetic stays FP32; a smoothing sweep streams 38
+                   instead of 60 bytes per cell: faster on 19-slot grids,
+                   same iterations).  The FP64 FGMRES operator is the same
+                   either way. */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

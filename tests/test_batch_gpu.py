@@ -37,12 +37,12 @@ def _fields(ctx, gid, case):
             ctx.get_field(gid, capi.FIELD_UCONT, shp + (3,)))
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_fp32_operator", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp16_operator", "fp64"])
 def test_batch_equals_one_at_a_time(gpu_ctx, precision):
     cases = _cases()
     ids = _load(gpu_ctx, cases)
     try:
-        half = 0 if precision == "mixed_fp32_operator" else 1
+        half = 1 if precision == "mixed_fp16_operator" else 0
         params = capi.default_params(precision=precision.split("_")[0], rtol=1e-9, div_tol=1e-8, mg_half=half)
         for gid, c in zip(ids, cases):
             _reset(gpu_ctx, gid, c)

@@ -209,17 +209,17 @@ def test_projection_fractional_nvert_bitexact(gpu_ctx):
     gpu_ctx.grid_destroy(gid)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp32_operator"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp16_operator"])
 @pytest.mark.parametrize("orth", ["cgs", "cgs2"])
 def test_full_step_parity(gpu_ctx, loaded, precision, orth):
-    """mixed: FP32 multigrid on the FP16 diagonal-normalised operator (the
-    default); mixed_fp32_operator: on the FP32 operator."""
+    """mixed: FP32 multigrid on FP32 stencil coefficients (the default);
+    mixed_fp16_operator: on the FP16 diagonal-normalised operator."""
     case, gid, d, mg = loaded
     g = case.grid
     ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg,
                             orth=1 if orth == "cgs" else 2)
     params = capi.default_params(precision=precision.split("_")[0], rtol=1e-12, maxit=300, restart=30, orth=orth,
-                                 div_tol=1e-8, mg_half=0 if precision == "mixed_fp32_operator" else 1)
+                                 div_tol=1e-8, mg_half=1 if precision == "mixed_fp16_operator" else 0)
     u = np.ascontiguousarray(case.ucont.copy())
     p = np.zeros(g.nvert.shape)
     info, divmax = gpu_ctx.projection_step(gid, params, u, p)

@@ -1215,7 +1215,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->smooth_cols = 0;
   p->nu1_coarse = -1;
   p->nu2_coarse = -1;
-  p->mg_half = 1;
+  p->mg_half = 0;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
