@@ -143,6 +143,8 @@ SIGNATURES = {
     "vfs_elapsed": ([_P, _I, _I, _DP], _I),
     "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
     "vfs_host_unregister": ([_P], _I),
+    "vfs_host_alloc": ([ctypes.POINTER(_P), ctypes.c_ulonglong], _I),
+    "vfs_host_free": ([_P], _I),
 }
 
 PROBE_SMOOTH = 1
@@ -387,6 +389,19 @@ class Context:
 
     def host_unregister(self, a: np.ndarray):
         self.L.vfs_host_unregister(a.ctypes.data_as(_P))
+
+    def host_alloc(self, shape, dtype=np.float64) -> np.ndarray:
+        """A numpy array over page-locked memory from vfs_host_alloc; release
+        it with host_free (the array must not be used afterwards)."""
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = _P()
+        rc = self.L.vfs_host_alloc(ctypes.byref(p), n)
+        if rc:
+            raise VfsError(rc, "cudaHostAlloc failed")
+        return np.frombuffer((ctypes.c_char * n).from_address(p.value), dtype=dtype).reshape(shape)
+
+    def host_free(self, a: np.ndarray):
+        self.check(self.L.vfs_host_free(a.ctypes.data_as(_P)))
 
     # -- hooks --
     def update_nvert(self, g: int, nvert: np.ndarray):

@@ -20,6 +20,10 @@ constexpr int RB = 256;  // reduction block size
 #define GRID_LOOP(d)                                                                          \
   for (size_t _t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; _t < ncell(d);              \
        _t += (size_t)gridDim.x * blockDim.x)
+// cells [c0, c1) of the grid, grid-stride
+#define RANGE_LOOP(c0, c1)                                                                     \
+  for (size_t _t = (c0) + blockIdx.x * (size_t)blockDim.x + threadIdx.x; _t < (c1);           \
+       _t += (size_t)gridDim.x * blockDim.x)
 // 32-bit index split (grids stay below 2^31 cells)
 #define DECOMP(d, i, j, k)                          \
   const unsigned _u = (unsigned)_t;                 \
@@ -316,7 +320,8 @@ int launch_update_pressure(const Dims& d, const double* nvert, const double* phi
 __device__ __forceinline__ double div_c(double x, double coeff) { return coeff == 1.0 ? x : x / coeff; }
 
 template <bool NVI>
-__global__ void __launch_bounds__(128) k_projection(Dims d, const double* __restrict__ pd, const double* __restrict__ iaj,
+__global__ void __launch_bounds__(128) k_projection(Dims d, size_t c0, size_t c1, const double* __restrict__ pd,
+                             const double* __restrict__ iaj,
                              const double* __restrict__ jaj, const double* __restrict__ kaj, const double* __restrict__ nvert,
                              const uint8_t* __restrict__ nb8, const double* __restrict__ phi, double dt, double st,
                              double coeff, Ucont u) {
@@ -331,7 +336,7 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __rest
     if (NVI) return (nb8[a] | nb8[b]) == 0;
     return nvert[a] + nvert[b] < THR;
   };
-  GRID_LOOP(d) {
+  RANGE_LOOP(c0, c1) {
     DECOMP(d, i, j, k);
     const size_t c = _t;
 // nvert pair tests: with NVI every nvert is an integer in [0, 127] and nb8
@@ -436,9 +441,12 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, const double* __rest
   }
 }
 
-// periodic ghost sync of the flagged component (poisson.c:2398-2437)
-__global__ void k_ucont_ghosts(Dims d, Ucont u) {
-  GRID_LOOP(d) {
+// periodic ghost sync of the flagged component (poisson.c:2398-2437) on
+// cells [c0, c1).  Every source is interior in all periodic directions, so
+// the sync never reads a cell it writes; the source of a cell on an interior
+// plane k lies on plane k.
+__global__ void k_ucont_ghosts(Dims d, size_t c0, size_t c1, Ucont u) {
+  RANGE_LOOP(c0, c1) {
     DECOMP(d, i, j, k);
     int a = wrapi(i, d.mx, d.ip), b = wrapi(j, d.my, d.jp), cc = wrapi(k, d.mz, d.kp);
     if (a == i && b == j && cc == k) continue;
@@ -481,16 +489,31 @@ int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s)
 }
 
 int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const uint8_t* nb8,
-                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s) {
+                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s, int k0,
+                      int k1) {
   const size_t N = ncell(d);
-  if (nb8)
-    k_projection<true><<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, nb8, phi,
-                                                     dt, st, coeff, u);
-  else
-    k_projection<false><<<nblk(N, 128), 128, 0, s>>>(d, pd, M + N * MP_IAJ, M + N * MP_JAJ, M + N * MP_KAJ, nvert, nb8,
-                                                      phi, dt, st, coeff, u);
-  ++g_launches;
-  k_ucont_ghosts<<<nblk(N), 256, 0, s>>>(d, u); ++g_launches;
+  const size_t P = (size_t)d.mx * d.my;
+  if (k1 < 0) k1 = d.mz;
+  if (k0 < 0 || k0 >= k1 || k1 > d.mz) return (int)cudaErrorInvalidValue;
+  // planes 0 and mz-1 hold no projected face (every branch needs 0 < k < mz-1)
+  const int p0 = k0 > 1 ? k0 : 1, p1 = k1 < d.mz - 1 ? k1 : d.mz - 1;
+  if (p0 < p1) {
+    const size_t c0 = p0 * P, c1 = p1 * P;
+    if (nb8)
+      k_projection<true><<<nblk(c1 - c0, 128), 128, 0, s>>>(d, c0, c1, pd, M + N * MP_IAJ, M + N * MP_JAJ,
+                                                            M + N * MP_KAJ, nvert, nb8, phi, dt, st, coeff, u);
+    else
+      k_projection<false><<<nblk(c1 - c0, 128), 128, 0, s>>>(d, c0, c1, pd, M + N * MP_IAJ, M + N * MP_JAJ,
+                                                             M + N * MP_KAJ, nvert, nb8, phi, dt, st, coeff, u);
+    ++g_launches;
+  }
+  return launch_ucont_ghosts(d, u, k0, k1, s);
+}
+
+int launch_ucont_ghosts(const Dims& d, const Ucont& u, int k0, int k1, cudaStream_t s) {
+  const size_t P = (size_t)d.mx * d.my;
+  if (k0 < 0 || k0 >= k1 || k1 > d.mz) return (int)cudaErrorInvalidValue;
+  k_ucont_ghosts<<<nblk((k1 - k0) * P), 256, 0, s>>>(d, k0 * P, k1 * P, u); ++g_launches;
   return (int)cudaGetLastError();
 }
 

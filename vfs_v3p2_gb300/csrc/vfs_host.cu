@@ -141,7 +141,7 @@ struct Grid {
   int epoch = 0;            // solve rounds started on this grid
   cudaEvent_t ev_chk = nullptr, ev_done = nullptr, ev_pend = nullptr;
   cudaStream_t cs = nullptr;  // copy stream: host transfers that overlap the step
-  cudaEvent_t ev_pin = nullptr, ev_p = nullptr, ev_u = nullptr, ev_cs = nullptr;
+  cudaEvent_t ev_pin = nullptr, ev_p = nullptr, ev_u = nullptr, ev_cs = nullptr, ev_uin = nullptr;
   long long busy = 0;       // ticket of the request in flight on this grid (serving)
   cudaStream_t s = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -228,7 +228,7 @@ void grid_free(vfs_ctx* ctx, Grid* g) {
   if (g->hstat) cudaFreeHost(g->hstat);
   if (g->hk) cudaFreeHost(g->hk);
   if (g->hv) cudaFreeHost(g->hv);
-  for (cudaEvent_t e : {g->ev_chk, g->ev_done, g->ev_pend, g->ev_pin, g->ev_p, g->ev_u, g->ev_cs})
+  for (cudaEvent_t e : {g->ev_chk, g->ev_done, g->ev_pend, g->ev_pin, g->ev_p, g->ev_u, g->ev_cs, g->ev_uin})
     if (e) cudaEventDestroy(e);
   if (g->cs) {
     cudaStreamSynchronize(g->cs);
@@ -720,11 +720,18 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
 //          starts from the current phi with a tighter L2 target (at most 8)
 //   POST   null-space removal, phi finish, step_post and the outputs are on
 //          their way; when they arrive the job is DONE.
-// All of a job's work is ordered on its grid's stream.
+// A job's work is ordered on its grid's stream; its host transfers run on
+// the grid's copy stream, joined to the step stream by events.
 // ---------------------------------------------------------------------------
 enum JobPhase { J_START = 0, J_ITER, J_CHECK, J_POST, J_DONE };
 
 void step_pre(Grid& g, double dt, double st, double coeff);
+// Slabs of the flux upload and download: one per 4 MiB of AoS fluxes, 1 to 8.
+int transfer_slabs(size_t ncells) {
+  const size_t b = 3 * ncells * sizeof(double);
+  return (int)std::max<size_t>(1, std::min<size_t>(8, b >> 22));
+}
+
 int step_post(Grid& g, double dt, double st, double coeff, double* u_out = nullptr, double* p_out = nullptr,
               bool p_in_pending = false);
 
@@ -776,12 +783,26 @@ int job_start(vfs_ctx* ctx, Job& J) {
   CK(cudaEventRecord(g.t0, g.s));
   if (J.pre) {
     if (J.u_in) {
-      CK(cudaMemcpyAsync(g.aos, J.u_in, 3 * N * sizeof(double), cudaMemcpyHostToDevice, g.s));
-      launch_aos2soa(N, g.aos, g.u, g.u + N, g.u + 2 * N, g.s);
+      // the fluxes go up in k-plane slabs on the copy stream, each slab
+      // converted to SoA on the step stream while the next one is in flight
+      CK(cudaEventRecord(g.ev_uin, g.s));
+      CK(cudaStreamWaitEvent(g.cs, g.ev_uin, 0));
+      const int mz = g.d.mz;
+      const size_t P = (size_t)g.d.mx * g.d.my;
+      const int S = std::min(mz, transfer_slabs(N));
+      for (int q = 0; q < S; q++) {
+        const size_t c0 = (size_t)(mz * (long long)q / S) * P, c1 = (size_t)(mz * (long long)(q + 1) / S) * P;
+        CK(cudaMemcpyAsync(g.aos + 3 * c0, J.u_in + 3 * c0, 3 * (c1 - c0) * sizeof(double), cudaMemcpyHostToDevice,
+                           g.cs));
+        CK(cudaEventRecord(g.ev_uin, g.cs));
+        CK(cudaStreamWaitEvent(g.s, g.ev_uin, 0));
+        launch_aos2soa(c1 - c0, g.aos + 3 * c0, g.u + c0, g.u + N + c0, g.u + 2 * N + c0, g.s);
+      }
     } else {
       CK(cudaMemcpyAsync(g.u, g.ustar, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice, g.s));
     }
-    if (J.p_in) {  // needed only at the pressure update: upload during the solve
+    if (J.p_in) {  // needed only at the pressure update: upload during the solve,
+                   // on the copy stream after the fluxes
       CK(cudaMemcpyAsync(g.p, J.p_in, N * sizeof(double), cudaMemcpyHostToDevice, g.cs));
       CK(cudaEventRecord(g.ev_pin, g.cs));
       J.p_in_pending = true;
@@ -1319,7 +1340,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   cudaEventCreateWithFlags(&g.ev_chk, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&g.ev_done, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&g.ev_pend, cudaEventDisableTiming);
-  for (cudaEvent_t* e : {&g.ev_pin, &g.ev_p, &g.ev_u, &g.ev_cs}) cudaEventCreateWithFlags(e, cudaEventDisableTiming);
+  for (cudaEvent_t* e : {&g.ev_pin, &g.ev_p, &g.ev_u, &g.ev_cs, &g.ev_uin})
+    cudaEventCreateWithFlags(e, cudaEventDisableTiming);
   if (cudaStreamCreateWithFlags(&g.cs, cudaStreamNonBlocking) != cudaSuccess)
     return bail(cuda_fail(ctx, cudaGetLastError(), "stream"));
   // level extents, finest = L-1
@@ -1764,12 +1786,43 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     ok(cudaStreamWaitEvent(g.cs, g.ev_p, 0));
     ok(cudaMemcpyAsync(p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
   }
-  dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
-  if (u_out) {
+  if (!u_out) {
+    dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
+  } else {
+    // Interior planes in slabs: a slab is projected and converted to AoS on
+    // the step stream and goes down on the copy stream while the next one
+    // is projected; the k ghost planes (filled from planes mz-2 and 1)
+    // follow the last slab.
+    const int mz = F.d.mz;
+    const size_t P = (size_t)F.d.mx * F.d.my;
+    auto to_aos = [&](int k0, int k1) {
+      const size_t c0 = k0 * P;
+      launch_soa2aos((k1 - k0) * P, g.u + c0, g.u + N + c0, g.u + 2 * N + c0, g.aos + 3 * c0, g.s);
+    };
+    auto download = [&](int k0, int k1) {
+      const size_t c0 = k0 * P;
+      ok(cudaMemcpyAsync(u_out + 3 * c0, g.aos + 3 * c0, 3 * (k1 - k0) * P * sizeof(double), cudaMemcpyDeviceToHost,
+                         g.cs));
+    };
+    const int inner = mz - 2;
+    const int S = std::min(inner, transfer_slabs(N));
+    for (int q = 0; q < S; q++) {
+      const int k0 = 1 + (int)((long long)inner * q / S), k1 = 1 + (int)((long long)inner * (q + 1) / S);
+      dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s, k0, k1),
+          g.s);
+      to_aos(k0, k1);
+      ok(cudaEventRecord(g.ev_u, g.s));
+      ok(cudaStreamWaitEvent(g.cs, g.ev_u, 0));
+      download(k0, k1);
+    }
+    dbg("ucont_ghosts", 0, launch_ucont_ghosts(F.d, g.U(), 0, 1, g.s), g.s);
+    dbg("ucont_ghosts", 0, launch_ucont_ghosts(F.d, g.U(), mz - 1, mz, g.s), g.s);
+    to_aos(0, 1);
+    to_aos(mz - 1, mz);
     ok(cudaEventRecord(g.ev_u, g.s));
     ok(cudaStreamWaitEvent(g.cs, g.ev_u, 0));
-    launch_soa2aos(N, g.u, g.u + N, g.u + 2 * N, g.aos, g.cs);
-    ok(cudaMemcpyAsync(u_out, g.aos, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
+    download(0, 1);
+    download(mz - 1, mz);
   }
   dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
   dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8), g.s);
@@ -1979,6 +2032,22 @@ int vfs_host_register(void* ptr, unsigned long long bytes) {
 int vfs_host_unregister(void* ptr) {
   if (!ptr) return VFS_ERR_ARG;
   return cudaHostUnregister(ptr) == cudaSuccess ? VFS_OK : VFS_ERR_CUDA;
+}
+
+int vfs_host_alloc(void** ptr, unsigned long long bytes) {
+  if (!ptr || !bytes) return VFS_ERR_ARG;
+  *ptr = nullptr;
+  if (cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return VFS_ERR_NOMEM;
+  }
+  return VFS_OK;
+}
+
+int vfs_host_free(void* ptr) {
+  if (!ptr) return VFS_ERR_ARG;
+  return cudaFreeHost(ptr) == cudaSuccess ? VFS_OK : VFS_ERR_CUDA;
 }
 
 int vfs_mark(vfs_ctx* ctx, int grid, int slot) {

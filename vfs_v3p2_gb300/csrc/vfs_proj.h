@@ -27,9 +27,16 @@ int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStrea
 int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s);
 int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s);
 // nb8: nvert as bytes when every value is an integer in [0, 127] (exact
-// integer pair tests), else nullptr (FP64 tests).
+// integer pair tests), else nullptr (FP64 tests).  Projects the faces of
+// planes [k0, k1) (k1 < 0: mz) and syncs their periodic ghosts.  A plane
+// reads phi and the metrics alone, and the ghost sync of an interior plane
+// reads that plane alone, so interior slabs may go in any order; the k ghost
+// planes 0 and mz-1 (filled from planes mz-2 and 1) come after all of them.
 int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const uint8_t* nb8,
-                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s);
+                      const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s,
+                      int k0 = 0, int k1 = -1);
+// periodic ghost sync of the Ucont components on planes [k0, k1)
+int launch_ucont_ghosts(const Dims& d, const Ucont& u, int k0, int k1, cudaStream_t s);
 // minv: per-cell inverse of the metric matrix [csi; eta; zet] (9 doubles,
 // row-major), from launch_inverse_metric.
 int launch_contra2cart(const Dims& d, const double* minv, const double* nvert, const Ucont& u, double* ucat, cudaStream_t s);
