@@ -58,10 +58,14 @@ def parse():
     ap.add_argument("--nu", type=int, default=3, help="pre- and post-smoothing sweeps")
     ap.add_argument("--nu1", type=int, default=None, help="pre-smoothing sweeps (overrides --nu)")
     ap.add_argument("--nu2", type=int, default=None, help="post-smoothing sweeps (overrides --nu)")
-    ap.add_argument("--nu-coarse", default="5,5",
-                    help="PRE,POST sweeps below the finest level of the single-grid workloads (-1,-1: as finest; "
-                         "measured 9 vs 10 iterations on the sphere workload)")
-    ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping")
+    ap.add_argument("--nu-coarse", default=None,
+                    help="PRE,POST sweeps below the finest level of the single-grid workloads (-1,-1: as finest, "
+                         "the default with the Chebyshev smoother; 5,5 the default with the Jacobi one)")
+    ap.add_argument("--smoother", default="chebyshev", choices=["chebyshev", "jacobi"],
+                    help="sweep damping: Chebyshev roots on [cheb_hi / cheb_ratio, cheb_hi], or omega on every sweep")
+    ap.add_argument("--cheb-hi", type=float, default=2.0)
+    ap.add_argument("--cheb-ratio", type=float, default=6.0)
+    ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping (--smoother jacobi)")
     ap.add_argument("--smooth-cols", type=int, default=0, help="smoother tile columns (0: automatic)")
     ap.add_argument("--mg-half", type=int, default=0, choices=[0, 1],
                     help="multigrid stencil coefficients stored in FP32 (0, the specified form) or as FP16 "
@@ -293,9 +297,37 @@ def main_batch(args, dist, rank, local, ws):
     barrier(dist)
     total = allmax(dist, sum(per))
     cells = sum(c.grid.ni * c.grid.nj * c.grid.nk for c in cases)
+    value = ws * len(ids) * args.steps / total
+    fp64 = None
+    if not args.no_fp64:
+        # the same grids in plain FP64 (same smoother settings): batched, and
+        # one grid at a time through the single-grid step
+        p64 = capi.default_params(precision="fp64", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
+                                  restart=args.restart)
+        ctx.projection_step_batch(ids, p64)
+        K64 = max(2, args.steps // 2)
+        t0 = time.perf_counter()
+        its64, dm64 = [], []
+        for _ in range(K64):
+            infos, dm = ctx.projection_step_batch(ids, p64)
+            its64 += [i["iterations"] for i in infos]
+            dm64.append(float(dm.max()))
+        t_b = allmax(dist, time.perf_counter() - t0)
+        for gid in ids:
+            ctx.projection_step(gid, p64)
+        t0 = time.perf_counter()
+        dm1 = []
+        for gid in ids:
+            _, dm = ctx.projection_step(gid, p64)
+            dm1.append(dm)
+        t_1 = allmax(dist, time.perf_counter() - t0)
+        r_b, r_1 = ws * len(ids) * K64 / t_b, ws * len(ids) / t_1
+        fp64 = {"batched": {"value": r_b, "iterations_mean": float(np.mean(its64)), "divmax": max(dm64)},
+                "one_grid_at_a_time": {"value": r_1, "divmax": max(dm1)},
+                "mixed_batched_over_fp64_batched": value / r_b, "mixed_batched_over_fp64_one_at_a_time": value / r_1}
     line = {"metric": "batched pressure projection steps/s (64 uneven grids, one graph launch per FGMRES iteration), "
                       "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
-            "value": ws * len(ids) * args.steps / total, "unit": "solves/s", "steps": args.steps,
+            "value": value, "unit": "solves/s", "steps": args.steps,
             "ms_per_step": 1e3 * total / args.steps, **base_line(args, ws),
             "config": {"workload": WORKLOAD["batch"], "grids": len(ids), "cells_total": int(cells),
                        "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": bool(args.tune),
@@ -304,7 +336,7 @@ def main_batch(args, dist, rank, local, ws):
                        "parallelism": f"replicas x{ws}"},
             "e2e": None, "iterations": {"mean": float(np.mean(its)), "max": int(max(its))}, "divmax": max(dms),
             "latency_ms": {"p50": float(np.percentile(per, 50) * 1e3), "p99": float(np.percentile(per, 99) * 1e3)},
-            "clocks": clocks, "gpu_launches": int(nl)}
+            "clocks": clocks, "gpu_launches": int(nl), "fp64": fp64}
     if tuned:
         line["autotune"] = tuned
     if rank == 0:
@@ -340,6 +372,26 @@ def main_serve(args, dist, rank, local, ws):
     cells = [streams[r["stream"]].case.grid.nvert.size for r in recs]
     h2d = float(np.mean([24 * c for c in cells]))
     d2h = float(np.mean([8 * c for c in cells]))
+    fp64 = None
+    if not args.no_fp64:
+        # capacity: the same number of requests arriving at once, mixed and
+        # plain FP64 (same smoother settings); then FP64 at the offered rate
+        burst = serve.poisson_arrivals(args.requests, 1e6, 16, seed=11)
+        rb, wb = srv.run(burst)
+        cap = serve.summarize(rb, allmax(dist, wb))
+        srv.params = capi.default_params(precision="fp64", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
+                                         restart=args.restart, warm_start=1)
+        srv.run(warm)
+        rb64, wb64 = srv.run(burst)
+        cap64 = serve.summarize(rb64, allmax(dist, wb64))
+        recs64, wall64 = srv.run(arr)
+        s64 = serve.summarize(recs64, allmax(dist, wall64))
+        fp64 = {"value": ws * s64["solves_per_s"], "latency_ms": s64["latency_ms"], "divmax": s64["divmax"],
+                "failed": s64["failed"],
+                "capacity_solves_per_s": {"mixed": ws * cap["solves_per_s"], "fp64": ws * cap64["solves_per_s"],
+                                          "mixed_over_fp64": cap["solves_per_s"] / cap64["solves_per_s"],
+                                          "divmax": {"mixed": cap["divmax"], "fp64": cap64["divmax"]},
+                                          "requests": len(burst)}}
     line = {"metric": "served pressure projection steps/s with p50/p99 latency (Poisson arrivals, continuous batching), "
                       "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
             "value": ws * summ["solves_per_s"], "unit": "solves/s", "steps": len(recs),
@@ -352,11 +404,23 @@ def main_serve(args, dist, rank, local, ws):
             "e2e": {"value": ws * summ["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "latency_ms": summ["latency_ms"], "iterations": summ["iterations"], "divmax": summ["divmax"],
-            "failed": summ["failed"], "clocks": clocks, "gpu_launches": int(nl)}
+            "failed": summ["failed"], "clocks": clocks, "gpu_launches": int(nl), "fp64": fp64}
     if rank == 0:
         print(json.dumps(line), flush=True)
     srv.close()
     ctx.close()
+
+
+def nu_coarse(args) -> str:
+    if args.nu_coarse is not None:
+        return args.nu_coarse
+    return "-1,-1" if args.smoother == "chebyshev" else "5,5"
+
+
+def smoother_config(args) -> dict:
+    if args.smoother == "chebyshev":
+        return {"smoother": "chebyshev", "cheb_interval": [args.cheb_hi / args.cheb_ratio, args.cheb_hi]}
+    return {"smoother": "jacobi", "omega": args.omega}
 
 
 def main():
@@ -381,17 +445,18 @@ def main():
     ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
     nu1 = args.nu if args.nu1 is None else args.nu1
     nu2 = args.nu if args.nu2 is None else args.nu2
-    nuc = [int(v) for v in args.nu_coarse.split(",")]
+    nuc = [int(v) for v in nu_coarse(args).split(",")]
+    smooth = dict(smoother=args.smoother, cheb_hi=args.cheb_hi, cheb_ratio=args.cheb_ratio, omega=args.omega)
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
-                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                                div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
                                 mg_half=args.mg_half)
     other = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
-                                div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                                div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
                                 mg_half=1 - args.mg_half)
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
-                               div_tol=args.div_tol, maxit=400, orth=args.orth, omega=args.omega,
+                               div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
 
     def steps(params, K, base_slot):
@@ -498,7 +563,7 @@ def main():
             "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
-                       "restart": args.restart, "orth": args.orth, "omega": args.omega,
+                       "restart": args.restart, "orth": args.orth, **smoother_config(args),
                        "mg_operator": OPERATOR[args.mg_half],
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,

@@ -108,7 +108,7 @@ def test_autotune_picks_a_converging_candidate(gpu_ctx):
     plist, table = autotune.tuned_params(gpu_ctx, cases, base, steps=1)
     assert len(plist) == 2 and all(autotune.size_class(c) in table for c in cases)
     for e in table.values():
-        assert (e["nu1"], e["nu2"], e["omega"], e["smooth_cols"], e["nu_coarse"]) in autotune.CANDIDATES
+        assert autotune.entry_candidate(e) in autotune.CANDIDATES
         assert 0 < e["ms_per_step"] < float("inf")
 
 

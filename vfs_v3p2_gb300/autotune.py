@@ -1,8 +1,8 @@
 """Autotuner for the batched and served solves.
 
 Picks, per grid-size class, the smoothing schedule (pre/post y-line sweeps
-on the finest and on the coarser levels, damping) and the smoother's block
-tile (i-columns per block).  Each candidate is run once to warm up (graph
+on the finest and on the coarser levels, Chebyshev or constant damping) and
+the smoother's block tile (i-columns per block).  Each candidate is run once to warm up (graph
 capture) and then timed over a few steps with U* resident; the fastest
 candidate whose steps all converge to the requested max |div u| wins.
 
@@ -26,12 +26,31 @@ import numpy as np
 
 from . import capi
 
-# (nu1, nu2, omega, smooth_cols, coarse sweeps); smooth_cols 0 = the kernel's
-# own choice; coarse sweeps -1 = as on the finest level
+# (nu1, nu2, omega, smooth_cols, coarse sweeps, smoother); smooth_cols 0 = the
+# kernel's own choice; coarse sweeps -1 = as on the finest level; omega is the
+# damping of the "jacobi" smoother ("chebyshev" takes the roots on [1/3, 2])
 CANDIDATES = [
-    (3, 3, 0.9, 0, 5), (3, 3, 0.9, 0, -1), (2, 2, 0.8, 0, 5), (2, 4, 0.9, 0, 5), (4, 4, 0.9, 0, 5),
-    (3, 3, 0.85, 0, 5), (3, 3, 0.9, 16, 5), (4, 4, 0.9, 16, 6), (2, 2, 0.9, 0, 4),
+    (3, 3, 0.9, 0, -1, "chebyshev"), (2, 2, 0.9, 0, -1, "chebyshev"), (4, 4, 0.9, 0, -1, "chebyshev"),
+    (3, 3, 0.9, 16, -1, "chebyshev"), (3, 3, 0.9, 0, 4, "chebyshev"),
+    (3, 3, 0.9, 0, 5, "jacobi"), (3, 3, 0.9, 0, -1, "jacobi"), (2, 2, 0.8, 0, 5, "jacobi"),
+    (4, 4, 0.9, 16, 6, "jacobi"), (2, 2, 0.9, 0, 4, "jacobi"),
 ]
+SMOOTHERS = {"jacobi": capi.SMOOTH_JACOBI, "chebyshev": capi.SMOOTH_CHEBYSHEV}
+
+
+def apply_candidate(p: capi.SolveParams, cand):
+    p.nu1, p.nu2, p.omega, p.smooth_cols = cand[:4]
+    p.nu1_coarse = p.nu2_coarse = cand[4]
+    p.smoother = SMOOTHERS[cand[5]]
+
+
+def candidate_entry(cand) -> dict:
+    return {"nu1": cand[0], "nu2": cand[1], "omega": cand[2], "smooth_cols": cand[3], "nu_coarse": cand[4],
+            "smoother": cand[5]}
+
+
+def entry_candidate(e: dict):
+    return (e["nu1"], e["nu2"], e["omega"], e["smooth_cols"], e["nu_coarse"], e.get("smoother", "jacobi"))
 
 
 def size_class(case) -> str:
@@ -58,7 +77,7 @@ def _time_candidate(ctx, gid, case, params, steps):
 
 
 def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3):
-    """Best (nu1, nu2, omega, smooth_cols, coarse sweeps) for one grid and its seconds/step."""
+    """Best candidate for one grid and its seconds/step."""
     g = case.grid
     gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
     try:
@@ -67,8 +86,7 @@ def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3)
         for cand in candidates:
             p = capi.SolveParams()
             ctypes_copy(p, base)
-            p.nu1, p.nu2, p.omega, p.smooth_cols = cand[:4]
-            p.nu1_coarse = p.nu2_coarse = cand[4]
+            apply_candidate(p, cand)
             try:
                 t = _time_candidate(ctx, gid, case, p, steps)
             except capi.VfsError:
@@ -101,8 +119,7 @@ def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = No
         cells = sorted(members, key=lambda q: cases[q].grid.ni * cases[q].grid.nj * cases[q].grid.nk)
         rep = cases[cells[len(cells) // 2]]
         cand, t = tune_case(ctx, rep, base, steps=steps)
-        cache[key] = {"nu1": cand[0], "nu2": cand[1], "omega": cand[2], "smooth_cols": cand[3],
-                      "nu_coarse": cand[4], "ms_per_step": t * 1e3, "grid": rep.name}
+        cache[key] = {**candidate_entry(cand), "ms_per_step": t * 1e3, "grid": rep.name}
     if cache_path:
         with open(cache_path, "w") as f:
             json.dump(cache, f, indent=1, sort_keys=True)
@@ -111,8 +128,7 @@ def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = No
         e = cache[size_class(c)]
         p = capi.SolveParams()
         ctypes_copy(p, base)
-        p.nu1, p.nu2, p.omega, p.smooth_cols = e["nu1"], e["nu2"], e["omega"], e["smooth_cols"]
-        p.nu1_coarse = p.nu2_coarse = e["nu_coarse"]
+        apply_candidate(p, entry_candidate(e))
         out.append(p)
     return out, cache
 
@@ -131,8 +147,7 @@ def tuned_params_batch(ctx, ids, cases, base: capi.SolveParams, steps=2):
         for cand in CANDIDATES:
             p = capi.SolveParams()
             ctypes_copy(p, base)
-            p.nu1, p.nu2, p.omega, p.smooth_cols = cand[:4]
-            p.nu1_coarse = p.nu2_coarse = cand[4]
+            apply_candidate(p, cand)
             try:
                 _reset(ctx, sub, [cases[q] for q in members])
                 ctx.projection_step_batch(sub, p)  # warm-up: graph capture
@@ -146,13 +161,11 @@ def tuned_params_batch(ctx, ids, cases, base: capi.SolveParams, steps=2):
                 t = math.inf
             if t < best_t:
                 best, best_t = cand, t
-        table[key] = {"nu1": best[0], "nu2": best[1], "omega": best[2], "smooth_cols": best[3], "nu_coarse": best[4],
-                      "ms_per_batch_step": best_t * 1e3, "grids": len(members)}
+        table[key] = {**candidate_entry(best), "ms_per_batch_step": best_t * 1e3, "grids": len(members)}
         for q in members:
             p = capi.SolveParams()
             ctypes_copy(p, base)
-            p.nu1, p.nu2, p.omega, p.smooth_cols = best[:4]
-            p.nu1_coarse = p.nu2_coarse = best[4]
+            apply_candidate(p, best)
             out[q] = p
     _reset(ctx, ids, cases)
     return out, table

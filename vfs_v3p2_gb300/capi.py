@@ -26,6 +26,7 @@ VFS_ERR_BUSY = 7
 VFS_FP64 = 0
 VFS_MIXED = 1
 ORTH_CGS, ORTH_CGS2 = 1, 2
+SMOOTH_JACOBI, SMOOTH_CHEBYSHEV = 0, 1
 
 FIELD_UCONT = 0
 FIELD_P = 1
@@ -63,7 +64,8 @@ class SolveParams(ctypes.Structure):
                 ("restart", ctypes.c_int), ("nu1", ctypes.c_int), ("nu2", ctypes.c_int),
                 ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
                 ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
-                ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int)]
+                ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int), ("smoother", ctypes.c_int),
+                ("cheb_hi", ctypes.c_double), ("cheb_ratio", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -141,6 +143,7 @@ SIGNATURES = {
     "vfs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], _I),
     "vfs_mark": ([_P, _I, _I], _I),
     "vfs_elapsed": ([_P, _I, _I, _DP], _I),
+    "vfs_sweep_damping": ([ctypes.POINTER(SolveParams), _I, _I, _DP, _I], _I),
     "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
     "vfs_host_unregister": ([_P], _I),
     "vfs_host_alloc": ([ctypes.POINTER(_P), ctypes.c_ulonglong], _I),
@@ -188,6 +191,18 @@ def dptr(a: np.ndarray):
     return a.ctypes.data_as(_DP)
 
 
+def sweep_damping(params: SolveParams, finest: bool, post: bool) -> np.ndarray:
+    """Damping of each smoothing sweep the V-cycle launches under params."""
+    nu1c = params.nu1_coarse if params.nu1_coarse >= 0 else params.nu1
+    nu2c = params.nu2_coarse if params.nu2_coarse >= 0 else params.nu2
+    n = (params.nu2 if post else params.nu1) if finest else (nu2c if post else nu1c)
+    w = np.zeros(max(n, 1))
+    rc = load().vfs_sweep_damping(ctypes.byref(params), int(finest), int(post), dptr(w), n)
+    if rc:
+        raise VfsError(rc, "vfs_sweep_damping: invalid parameters")
+    return w[:n]
+
+
 def default_params(**kw) -> SolveParams:
     p = SolveParams()
     load().vfs_default_params(ctypes.byref(p))
@@ -196,6 +211,8 @@ def default_params(**kw) -> SolveParams:
             v = {"fp64": VFS_FP64, "mixed": VFS_MIXED}[v]
         if k == "orth" and isinstance(v, str):
             v = {"cgs": ORTH_CGS, "cgs2": ORTH_CGS2}[v]
+        if k == "smoother" and isinstance(v, str):
+            v = {"jacobi": SMOOTH_JACOBI, "chebyshev": SMOOTH_CHEBYSHEV}[v]
         setattr(p, k, v)
     return p
 

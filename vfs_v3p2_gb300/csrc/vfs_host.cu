@@ -151,6 +151,8 @@ struct Grid {
   bool half_ok = true;  // the FP16 operator represents every level (else mg_half runs the FP32 one)
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
   int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
+  int ig_smoother = -1;
+  double ig_cheb_hi = 0., ig_cheb_ratio = 0.;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
   double nfluid = 0.;  // fluid interior cells of the finest level
@@ -327,9 +329,14 @@ int ensure_krylov(vfs_ctx* ctx, Grid& g, int m, int prec) {
 // A_l x = b; xa / xb are the level's ping-pong buffers; returns the buffer
 // that holds the result.
 // ---------------------------------------------------------------------------
+constexpr int MAXSWEEP = 64;  // smoothing sweeps per level and side
+
 struct MGCfg {
   int nu1, nu2, ncoarse;
   double omega, omega_c;
+  double wf[2][MAXSWEEP];  // damping of the finest level's sweeps: [0] pre, [1] post
+  double wc[2][MAXSWEEP];  // of the coarser levels' sweeps
+  double w(int l, int post, int q) const { return (l == top ? wf : wc)[post][q]; }
   int cols;        // smoother columns per block (0 = automatic)
   int nu1c, nu2c;  // sweeps on the levels below the finest
   int top;         // index of the finest level
@@ -395,7 +402,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   T* cur = nullptr;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, c.solo, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s);
     cur = o;
   }
   Level& C = g.lev[l - 1];
@@ -413,10 +420,27 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega, c.cols, c.solo, s);
+    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s);
     cur = o;
   }
   return cur;
+}
+
+// Damping of n sweeps: omega each (Jacobi), or 1 / theta_k at the roots
+// theta_k = (hi + lo) / 2 + (hi - lo) / 2 cos((2k - 1) pi / (2n)), k = 1..n,
+// of the degree-n Chebyshev polynomial on [lo, hi] (descending theta, so the
+// smallest damping comes first); post-sweeps take them in reverse order.
+void sweep_damping(const vfs_solve_params& p, int n, double* pre, double* post) {
+  for (int k = 0; k < n; k++) {
+    double w = p.omega;
+    if (p.smoother == VFS_SMOOTH_CHEBYSHEV) {
+      const double hi = p.cheb_hi, lo = p.cheb_hi / p.cheb_ratio;
+      const double th = 0.5 * (hi + lo) + 0.5 * (hi - lo) * std::cos(M_PI * (2 * k + 1) / (2.0 * n));
+      w = 1.0 / th;
+    }
+    pre[k] = w;
+    post[n - 1 - k] = w;
+  }
 }
 
 MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
@@ -429,6 +453,11 @@ MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
   c.cols = p.smooth_cols;
   c.nu1c = p.nu1_coarse >= 0 ? p.nu1_coarse : p.nu1;
   c.nu2c = p.nu2_coarse >= 0 ? p.nu2_coarse : p.nu2;
+  double tmp[MAXSWEEP];
+  sweep_damping(p, c.nu1, c.wf[0], tmp);
+  sweep_damping(p, c.nu2, tmp, c.wf[1]);
+  sweep_damping(p, c.nu1c, c.wc[0], tmp);
+  sweep_damping(p, c.nu2c, tmp, c.wc[1]);
   c.top = top;
   c.half = p.precision == VFS_MIXED && p.mg_half != 0 && half_ok;
   c.solo = false;
@@ -591,7 +620,8 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   const int prec = sizeof(T) == 4 ? VFS_MIXED : VFS_FP64;
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
       g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse &&
-      g.ig_half == p.mg_half && g.ig_solo == (int)g.solo) {
+      g.ig_half == p.mg_half && g.ig_solo == (int)g.solo && g.ig_smoother == p.smoother &&
+      g.ig_cheb_hi == p.cheb_hi && g.ig_cheb_ratio == p.cheb_ratio) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -620,6 +650,9 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_nu2c = p.nu2_coarse;
   g.ig_half = p.mg_half;
   g.ig_solo = (int)g.solo;
+  g.ig_smoother = p.smoother;
+  g.ig_cheb_hi = p.cheb_hi;
+  g.ig_cheb_ratio = p.cheb_ratio;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -703,6 +736,12 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
     return fail(ctx, VFS_ERR_ARG, "smooth_cols must be 0 (automatic), 8, 16 or 32");
   if (p->mg_half != 0 && p->mg_half != 1) return fail(ctx, VFS_ERR_ARG, "mg_half must be 0 or 1");
+  if (p->nu1 > MAXSWEEP || p->nu2 > MAXSWEEP || p->nu1_coarse > MAXSWEEP || p->nu2_coarse > MAXSWEEP)
+    return fail(ctx, VFS_ERR_ARG, "at most 64 smoothing sweeps per level and side");
+  if (p->smoother != VFS_SMOOTH_JACOBI && p->smoother != VFS_SMOOTH_CHEBYSHEV)
+    return fail(ctx, VFS_ERR_ARG, "smoother must be VFS_SMOOTH_JACOBI or VFS_SMOOTH_CHEBYSHEV");
+  if (p->smoother == VFS_SMOOTH_CHEBYSHEV && !(p->cheb_hi > 0. && p->cheb_hi <= 4. && p->cheb_ratio > 1.))
+    return fail(ctx, VFS_ERR_ARG, "Chebyshev smoother: cheb_hi must be in (0, 4] and cheb_ratio > 1");
   return VFS_OK;
 }
 
@@ -1230,6 +1269,9 @@ void vfs_default_params(vfs_solve_params* p) {
   p->nu1 = 3;
   p->nu2 = 3;
   p->omega = 0.9;
+  p->smoother = VFS_SMOOTH_CHEBYSHEV;
+  p->cheb_hi = 2.0;
+  p->cheb_ratio = 6.0;
   p->warm_start = 0;
   p->div_tol = 0.;
   p->orth = VFS_ORTH_CGS;
@@ -2249,6 +2291,21 @@ int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y
   cudaFree(dx);
   cudaFree(dy);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "prolong");
+  return VFS_OK;
+}
+
+int vfs_sweep_damping(const vfs_solve_params* p, int finest, int post, double* w, int n) {
+  if (!p || !w || n < 0) return VFS_ERR_ARG;
+  if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 > MAXSWEEP || p->nu2 > MAXSWEEP || p->nu1_coarse < -1 ||
+      p->nu2_coarse < -1 || p->nu1_coarse > MAXSWEEP || p->nu2_coarse > MAXSWEEP)
+    return VFS_ERR_ARG;
+  if (p->smoother != VFS_SMOOTH_JACOBI && p->smoother != VFS_SMOOTH_CHEBYSHEV) return VFS_ERR_ARG;
+  if (p->smoother == VFS_SMOOTH_CHEBYSHEV && !(p->cheb_hi > 0. && p->cheb_hi <= 4. && p->cheb_ratio > 1.))
+    return VFS_ERR_ARG;
+  const MGCfg c = mgcfg(*p, 1);
+  const int l = finest ? 1 : 0;
+  if (n != (post ? c.post(l) : c.pre(l))) return VFS_ERR_ARG;
+  for (int q = 0; q < n; q++) w[q] = c.w(l, post ? 1 : 0, q);
   return VFS_OK;
 }
 
