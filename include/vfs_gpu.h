@@ -286,6 +286,15 @@ int vfs_mg_restrict(vfs_ctx* ctx, int grid, int level, const double* x, double* 
 int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y);
 /* One damped y-line Jacobi sweep on a level (FP64 aj-scaled operator). */
 int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x, double omega);
+/* Connected fluid regions (cells with nvert < 0.1, joined through shared
+ * faces, periodic wrap included) of the finest and the coarsest level, as
+ * found by vfs_poisson_lhs.  A grid that bodies cut apart has one constant
+ * null vector per region: the step's compatibility fix and the solution's
+ * mean removal then act per region, and the coarsest dense solve adds one
+ * sigma e_q e_q^T per region (the reference's two-region case:
+ * FullyBlocked, poisson.c:1918-1998, and PoissonNullSpaceFunction,
+ * poisson.c:819-873). */
+int vfs_grid_components(vfs_ctx* ctx, int grid, int* finest, int* coarsest);
 /* Damping of the smoothing sweeps the V-cycle launches under p (host only,
  * no device): finest != 0 for the finest level, else the coarser ones;
  * post != 0 for the post-sweeps.  n must equal that side's sweep count.

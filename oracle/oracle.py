@@ -44,6 +44,8 @@ def lib():
         dp = ctypes.POINTER(ctypes.c_double)
         D = ctypes.POINTER(Dims)
         L.orc_form_metrics.argtypes = [D, dp, dp]
+        L.orc_fluid_regions.argtypes = [D, dp, ctypes.POINTER(ctypes.c_int)]
+        L.orc_fluid_regions.restype = ctypes.c_int
         L.orc_gtensor.argtypes = [D, dp, dp]
         L.orc_gid.argtypes = [D, dp, ctypes.POINTER(ctypes.c_int)]
         L.orc_gid.restype = ctypes.c_int
@@ -180,6 +182,16 @@ def volume_flux(d: Dims, mode: int, ucont: np.ndarray, nvert, M):
     lib().orc_volume_flux(ctypes.byref(d), mode, _p(ucont), _p(np.ascontiguousarray(nvert, dtype=np.float64)), _p(M),
                           _p(out))
     return out
+
+
+def fluid_regions(d: Dims, nvert):
+    """(K, labels): connected fluid regions through shared faces, periodic
+    wrap included; labels 0..K-1 (in the order of each region's first cell),
+    -1 on other cells."""
+    lab = np.zeros(_shape(d), dtype=np.int32)
+    K = lib().orc_fluid_regions(ctypes.byref(d), _p(np.ascontiguousarray(nvert, dtype=np.float64)),
+                                lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return K, lab
 
 
 def remove_mean(d: Dims, nvert, phi):

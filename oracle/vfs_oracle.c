@@ -678,8 +678,106 @@ int orc_csr(const orc_dims* d, const double* coef, const double* nvert, int* row
 }
 
 /* ------------------------------------------------------------------------- */
+/* Connected regions of the fluid cells (interior, nvert < 0.1) through       */
+/* shared faces, periodic wrap included: label[c] = 0..K-1 in the order of    */
+/* each region's first cell (cell index order), -1 on other cells; returns    */
+/* K.  A grid that bodies cut apart has one constant null vector per region   */
+/* (the reference's two-region case: FullyBlocked, poisson.c:1918-1998, and   */
+/* the split null space of PoissonNullSpaceFunction, poisson.c:819-873).      */
+/* ------------------------------------------------------------------------- */
+static int uf_find(int* parent, int a) {
+  while (parent[a] != a) {
+    parent[a] = parent[parent[a]];
+    a = parent[a];
+  }
+  return a;
+}
+static void uf_unite(int* parent, int a, int b) {
+  a = uf_find(parent, a);
+  b = uf_find(parent, b);
+  if (a != b) {
+    if (a < b) parent[b] = a;
+    else parent[a] = b;
+  }
+}
+int orc_fluid_regions(const orc_dims* d, const double* nvert, int* label) {
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const size_t N = (size_t)mx * my * mz;
+  int* parent = (int*)malloc(N * sizeof(int));
+  int* id = (int*)malloc(N * sizeof(int));
+  for (size_t c = 0; c < N; c++) { parent[c] = -1; id[c] = -1; label[c] = -1; }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t c = ID(d, i, j, k);
+        if (nvert[c] < 0.1) parent[c] = (int)c;
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t c = ID(d, i, j, k);
+        if (parent[c] < 0) continue;
+        int in = (i == mx - 2) ? (d->ip ? 1 : -1) : i + 1;
+        int jn = (j == my - 2) ? (d->jp ? 1 : -1) : j + 1;
+        int kn = (k == mz - 2) ? (d->kp ? 1 : -1) : k + 1;
+        if (in > 0 && parent[ID(d, in, j, k)] >= 0) uf_unite(parent, (int)c, (int)ID(d, in, j, k));
+        if (jn > 0 && parent[ID(d, i, jn, k)] >= 0) uf_unite(parent, (int)c, (int)ID(d, i, jn, k));
+        if (kn > 0 && parent[ID(d, i, j, kn)] >= 0) uf_unite(parent, (int)c, (int)ID(d, i, j, kn));
+      }
+  int K = 0;
+  for (size_t c = 0; c < N; c++) {
+    if (parent[c] < 0) continue;
+    int r = uf_find(parent, (int)c);
+    if (id[r] < 0) id[r] = K++;
+    label[c] = id[r];
+  }
+  free(parent);
+  free(id);
+  return K;
+}
+
+/* Per-region fluid mean of x subtracted from the region's fluid cells; the
+ * sums run in cell loop order (k, j, i), as the single-region versions. */
+static void sub_region_means(const orc_dims* d, const double* nvert, const int* label, int K, double* x) {
+  double* sum = (double*)calloc((size_t)K, sizeof(double));
+  long* cnt = (long*)calloc((size_t)K, sizeof(long));
+  for (int k = 1; k < d->mz - 1; k++)
+    for (int j = 1; j < d->my - 1; j++)
+      for (int i = 1; i < d->mx - 1; i++) {
+        size_t c = ID(d, i, j, k);
+        if (nvert[c] < 0.1) { sum[label[c]] += x[c]; cnt[label[c]]++; }
+      }
+  for (int k = 1; k < d->mz - 1; k++)
+    for (int j = 1; j < d->my - 1; j++)
+      for (int i = 1; i < d->mx - 1; i++) {
+        size_t c = ID(d, i, j, k);
+        if (nvert[c] < 0.1) x[c] += -sum[label[c]] / (double)cnt[label[c]];
+      }
+  free(sum);
+  free(cnt);
+}
+
+/* Number of fluid regions (1 without allocating when no interior cell is
+ * non-fluid); fills *label (malloc'd, caller frees) when more than one. */
+static int regions_of(const orc_dims* d, const double* nvert, int** label) {
+  *label = NULL;
+  int solid = 0;
+  for (int k = 1; k < d->mz - 1 && !solid; k++)
+    for (int j = 1; j < d->my - 1 && !solid; j++)
+      for (int i = 1; i < d->mx - 1; i++)
+        if (!(nvert[ID(d, i, j, k)] < 0.1)) { solid = 1; break; }
+  if (!solid) return 1;
+  int* lab = (int*)malloc((size_t)d->mx * d->my * d->mz * sizeof(int));
+  int K = orc_fluid_regions(d, nvert, lab);
+  if (K > 1) *label = lab;
+  else free(lab);
+  return K;
+}
+
+/* ------------------------------------------------------------------------- */
 /* PoissonRHS2_hypre (poisson_hypre.c:342-429) + optional compatibility fix   */
-/* of PoissonRHS2 (poisson.c:1879-1903): subtract the fluid-cell mean.        */
+/* of PoissonRHS2 (poisson.c:1879-1903): subtract the fluid-cell mean (per    */
+/* connected fluid region when bodies cut the grid apart).                    */
 /* ucont is AoS [mz][my][mx][3]; b is 0 on non-fluid cells.                   */
 /* Returns the sum of b before the fix.                                       */
 /* ------------------------------------------------------------------------- */
@@ -710,7 +808,12 @@ double orc_rhs(const orc_dims* d, const double* ucont, const double* nvert, doub
         sum += val;
         count++;
       }
-  if (meanfix && count > 0) {
+  int* label = NULL;
+  const int K = (meanfix && count > 0) ? regions_of(d, nvert, &label) : 1;
+  if (K > 1) {
+    sub_region_means(d, nvert, label, K, b);
+    free(label);
+  } else if (meanfix && count > 0) {
     double v = -sum / (double)count;
     for (size_t c = 0; c < N; c++) {
       int k = (int)(c / ((size_t)mx * my)), j = (int)((c / mx) % my), i = (int)(c % mx);
@@ -849,8 +952,16 @@ void orc_volume_flux(const orc_dims* d, int mode, double* u, const double* nvert
 /* ------------------------------------------------------------------------- */
 /* Solution post-processing.                                                  */
 /* ------------------------------------------------------------------------- */
-/* Remove_Nullspace (poisson_hypre.c:207-270): subtract the fluid-cell mean. */
+/* Remove_Nullspace (poisson_hypre.c:207-270): subtract the fluid-cell mean
+ * (per connected fluid region when bodies cut the grid apart; then returns 0). */
 double orc_remove_mean(const orc_dims* d, const double* nvert, double* phi) {
+  int* label = NULL;
+  const int K = regions_of(d, nvert, &label);
+  if (K > 1) {
+    sub_region_means(d, nvert, label, K, phi);
+    free(label);
+    return 0.;
+  }
   double sum = 0; long cnt = 0;
   for (int k = 1; k < d->mz - 1; k++)
     for (int j = 1; j < d->my - 1; j++)

@@ -143,6 +143,7 @@ SIGNATURES = {
     "vfs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], _I),
     "vfs_mark": ([_P, _I, _I], _I),
     "vfs_elapsed": ([_P, _I, _I, _DP], _I),
+    "vfs_grid_components": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "vfs_sweep_damping": ([ctypes.POINTER(SolveParams), _I, _I, _DP, _I], _I),
     "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
     "vfs_host_unregister": ([_P], _I),
@@ -272,6 +273,12 @@ class Context:
         b = ctypes.c_ulonglong()
         self.check(self.L.vfs_grid_bytes(self.h, g, ctypes.byref(b)))
         return b.value
+
+    def grid_components(self, g: int):
+        """(finest, coarsest): connected fluid regions found by poisson_lhs."""
+        f, c = _I(), _I()
+        self.check(self.L.vfs_grid_components(self.h, g, ctypes.byref(f), ctypes.byref(c)))
+        return f.value, c.value
 
     def level_dims(self, g: int, level: int):
         d = (ctypes.c_int * 3)()

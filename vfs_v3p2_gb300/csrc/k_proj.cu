@@ -126,10 +126,14 @@ __global__ void k_meanfix(Dims d, const double* __restrict__ nvert, const double
   }
 }
 int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, double st, double coeff, int meanfix,
-               double* b, double* parts, double* sc, cudaStream_t s) {
+               double* b, double* parts, double* sc, cudaStream_t s, const int* comp, int ncomp) {
   const int nb = nblk(ncell(d), RB);
   k_rhs<<<nb, RB, 0, s>>>(d, u, nvert, dt, st, coeff, b, parts); ++g_launches;
   k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, sc); ++g_launches;
+  if (meanfix && comp && ncomp > 1) {
+    // one compatibility fix per connected fluid region (sums in sc[2..3])
+    return launch_remove_mean(d, nvert, b, parts, sc + 2, s, comp, ncomp);
+  }
   if (meanfix) {
     k_meanfix<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, sc, b);
     ++g_launches;
@@ -238,14 +242,18 @@ int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nv
 
 // ---------------------------------------------------------------------------
 // Remove_Nullspace (poisson_hypre.c:207-270): subtract the fluid mean of phi.
+// With comp (labels of the connected fluid regions), only region q: a grid
+// cut apart by bodies has one constant null vector per region, as in the
+// reference's two-region split of PoissonNullSpaceFunction
+// (poisson.c:819-873, regions from FullyBlocked, poisson.c:1918-1998).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RB) k_fluid_sum(Dims d, const double* __restrict__ nvert, const double* __restrict__ x,
-                                                  double* parts) {
+                                                  double* parts, const int* __restrict__ comp, int q) {
   __shared__ double sh[32];
   double s = 0., n = 0.;
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
-    if (interior(d, i, j, k) && nvert[_t] < 0.1) {
+    if (interior(d, i, j, k) && nvert[_t] < 0.1 && (!comp || comp[_t] == q)) {
       s += x[_t];
       n += 1.;
     }
@@ -257,18 +265,24 @@ __global__ void __launch_bounds__(RB) k_fluid_sum(Dims d, const double* __restri
     parts[2 * blockIdx.x + 1] = n;
   }
 }
-__global__ void k_sub_mean(Dims d, const double* __restrict__ nvert, const double* __restrict__ sc, double* x) {
+__global__ void k_sub_mean(Dims d, const double* __restrict__ nvert, const double* __restrict__ sc, double* x,
+                           const int* __restrict__ comp, int q) {
   const double v = (sc[1] > 0.) ? -sc[0] / sc[1] : 0.;
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
-    if (interior(d, i, j, k) && nvert[_t] < 0.1) x[_t] += v;
+    if (interior(d, i, j, k) && nvert[_t] < 0.1 && (!comp || comp[_t] == q)) x[_t] += v;
   }
 }
-int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s) {
+int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s,
+                       const int* comp, int ncomp) {
   const int nb = nblk(ncell(d), RB);
-  k_fluid_sum<<<nb, RB, 0, s>>>(d, nvert, x, parts); ++g_launches;
-  k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, sc); ++g_launches;
-  k_sub_mean<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, sc, x); ++g_launches;
+  const int nq = (comp && ncomp > 1) ? ncomp : 1;
+  const int* cm = nq > 1 ? comp : nullptr;
+  for (int q = 0; q < nq; q++) {
+    k_fluid_sum<<<nb, RB, 0, s>>>(d, nvert, x, parts, cm, q); ++g_launches;
+    k_finish_sums<<<1, 256, 0, s>>>(parts, nb, 2, sc); ++g_launches;
+    k_sub_mean<<<nblk(ncell(d)), 256, 0, s>>>(d, nvert, sc, x, cm, q); ++g_launches;
+  }
   return (int)cudaGetLastError();
 }
 

@@ -609,12 +609,16 @@ __global__ void k_prolong_codes(Dims f, Dims c, int si, int sj, int sk, const do
 // ---------------------------------------------------------------------------
 // Dense inverse of the coarsest operator.  B = A + sigma * e e^T over the
 // fluid cells (e = fluid indicator; identity on non-fluid cells), so that
-// B^{-1} r is the mean-zero solution of A x = r for compatible r.  Unknowns
+// B^{-1} r is the mean-zero solution of A x = r for compatible r.  With
+// ccomp (labels of the level's connected fluid regions) the term is
+// sigma * sum_q e_q e_q^T, one per region, so B stays nonsingular when
+// bodies cut the level apart.  Unknowns
 // are the interior cells packed as ((k-1)*nj + (j-1))*ni + (i-1).  Work
 // matrix W = [B | I], n x 2n, row-major FP64; Gauss-Jordan with partial
 // pivoting, one pivot per launch sequence.
 // ---------------------------------------------------------------------------
-__global__ void k_dense_build(Dims d, const double* __restrict__ mcoef, double sigma, double* W, int n) {
+__global__ void k_dense_build(Dims d, const double* __restrict__ mcoef, double sigma, double* W, int n,
+                              const int* __restrict__ ccomp) {
   const size_t N = ncell(d);
   const int ni = d.mx - 2, nj = d.my - 2;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)n * 2 * n; t += (size_t)gridDim.x * blockDim.x) {
@@ -630,7 +634,7 @@ __global__ void k_dense_build(Dims d, const double* __restrict__ mcoef, double s
       bool fc = mcoef[c2] != 0.;
       if (!fr) v = (col == r) ? 1. : 0.;
       else {
-        if (fc) v = sigma;
+        if (fc && (!ccomp || ccomp[c] == ccomp[c2])) v = sigma;
         // add the stencil entries whose wrapped column is c2
         int II[3] = {wrapi(i - 1, d.mx, d.ip), i, wrapi(i + 1, d.mx, d.ip)};
         int JJ[3] = {wrapi(j - 1, d.my, d.jp), j, wrapi(j + 1, d.my, d.jp)};
@@ -760,9 +764,9 @@ int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, c
 
 // fac: n doubles; piv: 1 int; pval: 1 double (device scratch).
 int launch_dense_inverse(const Dims& d, const double* mcoef, double sigma, double* W, double* fac, int* piv, double* pval,
-                         double* Binv, float* Binv32, int n, cudaStream_t s) {
+                         double* Binv, float* Binv32, int n, cudaStream_t s, const int* ccomp) {
   const size_t w = 2 * (size_t)n;
-  k_dense_build<<<nblk((size_t)n * w), 256, 0, s>>>(d, mcoef, sigma, W, n); ++g_launches;
+  k_dense_build<<<nblk((size_t)n * w), 256, 0, s>>>(d, mcoef, sigma, W, n, ccomp); ++g_launches;
   for (int p = 0; p < n; p++) {
     k_gj_pivot<<<1, 256, 0, s>>>(W, n, p, piv, pval); ++g_launches;
     k_gj_swap_scale<<<nblk(w), 256, 0, s>>>(W, n, p, piv, pval); ++g_launches;

@@ -149,6 +149,9 @@ struct Grid {
   bool lhs = false;
   bool solo = false;  // the grid's solve runs alone (set by the driver before it issues work)
   bool half_ok = true;  // the FP16 operator represents every level (else mg_half runs the FP32 one)
+  int ncomp = 1;         // connected fluid regions of the finest level
+  int ncomp_c = 1;       // of the coarsest level
+  int* comp = nullptr;   // finest-level region labels (device), when ncomp > 1
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
   int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
   int ig_smoother = -1;
@@ -192,6 +195,54 @@ int cuda_fail(vfs_ctx* c, cudaError_t e, const char* where) {
     cudaError_t _e = (cudaError_t)(expr);                    \
     if (_e != cudaSuccess) return cuda_fail(ctx, _e, #expr); \
   } while (0)
+
+// Connected regions of the fluid cells through shared faces, periodic wrap
+// included: labels 0..K-1 in the order of each region's first cell (cell
+// index order), -1 on other cells; returns K.  A grid that bodies cut
+// apart has one constant null vector per region; the reference finds the
+// two-region case of a k-blocked grid with FullyBlocked (poisson.c:1918-1998)
+// and splits its null space at the first blocked k of each column
+// (poisson.c:819-873).
+int fluid_regions(const Dims& d, const std::vector<char>& fluid, std::vector<int>& label) {
+  const size_t N = ncell(d);
+  std::vector<int> parent(N, -1);
+  auto find = [&](int a) {
+    while (parent[a] != a) {
+      parent[a] = parent[parent[a]];
+      a = parent[a];
+    }
+    return a;
+  };
+  auto unite = [&](int a, int b) {
+    a = find(a);
+    b = find(b);
+    if (a != b) parent[std::max(a, b)] = std::min(a, b);
+  };
+  for (size_t c = 0; c < N; c++)
+    if (fluid[c]) parent[c] = (int)c;
+  for (int k = 1; k < d.mz - 1; k++)
+    for (int j = 1; j < d.my - 1; j++)
+      for (int i = 1; i < d.mx - 1; i++) {
+        const size_t c = cidx(d, i, j, k);
+        if (!fluid[c]) continue;
+        const int in = (i == d.mx - 2) ? (d.ip ? 1 : -1) : i + 1;
+        const int jn = (j == d.my - 2) ? (d.jp ? 1 : -1) : j + 1;
+        const int kn = (k == d.mz - 2) ? (d.kp ? 1 : -1) : k + 1;
+        if (in > 0 && fluid[cidx(d, in, j, k)]) unite((int)c, (int)cidx(d, in, j, k));
+        if (jn > 0 && fluid[cidx(d, i, jn, k)]) unite((int)c, (int)cidx(d, i, jn, k));
+        if (kn > 0 && fluid[cidx(d, i, j, kn)]) unite((int)c, (int)cidx(d, i, j, kn));
+      }
+  label.assign(N, -1);
+  std::vector<int> id(N, -1);
+  int K = 0;
+  for (size_t c = 0; c < N; c++) {
+    if (parent[c] < 0) continue;
+    const int r = find((int)c);
+    if (id[r] < 0) id[r] = K++;
+    label[c] = id[r];
+  }
+  return K;
+}
 
 template <typename T>
 int galloc(vfs_ctx* ctx, Grid& g, T** out, size_t count) {
@@ -899,7 +950,7 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     cudaStream_t s = g.s;
     Level& F = g.lev[g.L - 1];
     const size_t N = ncell(g.d);
-    dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s), s);
+    dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s, g.comp, g.ncomp), s);
     dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
     CK(cudaEventRecord(g.t1, s));
     if (J.post) {
@@ -1599,6 +1650,29 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
   g.half_ok = range == 0;
   cudaFree(gt);
   cudaFree(dmask);
+  // connected fluid regions of the finest level: one null vector each
+  {
+    std::vector<double> nv(N);
+    CK(cudaMemcpy(nv.data(), F.nvert, N * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<char> fl(N, 0);
+    bool solid = false;
+    for (int k = 1; k < F.d.mz - 1; k++)
+      for (int j = 1; j < F.d.my - 1; j++)
+        for (int i = 1; i < F.d.mx - 1; i++) {
+          const size_t c = cidx(F.d, i, j, k);
+          fl[c] = nv[c] < 0.1;
+          solid = solid || !fl[c];
+        }
+    std::vector<int> lab;
+    g.ncomp = solid ? fluid_regions(F.d, fl, lab) : 1;
+    if (g.ncomp > 1) {
+      if (!g.comp) {
+        const int r = galloc(ctx, g, &g.comp, N);
+        if (r) return r;
+      }
+      CK(cudaMemcpy(g.comp, lab.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
   // coarsest level: dense inverse of A + sigma e e^T when small enough
   Level& C = g.lev[0];
   const int n = (C.d.mx - 2) * (C.d.my - 2) * (C.d.mz - 2);
@@ -1617,6 +1691,21 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
         sabs += std::fabs(cp[c]);
         nf++;
       }
+    g.ncomp_c = 1;
+    int* ccomp = nullptr;
+    if (nf > 0) {
+      // the level's fluid rows (nonzero centre coefficient) and their regions
+      std::vector<char> fl(C.N, 0);
+      for (int k = 1; k < C.d.mz - 1; k++)
+        for (int j = 1; j < C.d.my - 1; j++)
+          for (int i = 1; i < C.d.mx - 1; i++) fl[cidx(C.d, i, j, k)] = cp[cidx(C.d, i, j, k)] != 0.;
+      std::vector<int> lab;
+      g.ncomp_c = fluid_regions(C.d, fl, lab);
+      if (g.ncomp_c > 1) {
+        CK(cudaMalloc(&ccomp, C.N * sizeof(int)));
+        CK(cudaMemcpy(ccomp, lab.data(), C.N * sizeof(int), cudaMemcpyHostToDevice));
+      }
+    }
     if (nf > 0) {
       const double sigma = -(sabs / nf) / (double)nf;
       double *W = nullptr, *fac = nullptr, *pval = nullptr;
@@ -1628,12 +1717,12 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
       int r = C.Binv ? VFS_OK : galloc(ctx, g, &C.Binv, (size_t)n * n);
       if (!r && !C.Binv32) r = galloc(ctx, g, &C.Binv32, (size_t)n * n);
       if (r) {
-        cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv);
+        cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv); cudaFree(ccomp);
         return r;
       }
-      launch_dense_inverse(C.d, C.mcoef, sigma, W, fac, piv, pval, C.Binv, C.Binv32, n, g.s);
+      launch_dense_inverse(C.d, C.mcoef, sigma, W, fac, piv, pval, C.Binv, C.Binv32, n, g.s, ccomp);
       cudaError_t e = cudaStreamSynchronize(g.s);
-      cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv);
+      cudaFree(W); cudaFree(fac); cudaFree(pval); cudaFree(piv); cudaFree(ccomp);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "coarse inverse");
       C.nco = n;
     }
@@ -1714,7 +1803,7 @@ int vfs_poisson_rhs(vfs_ctx* ctx, int grid, double dt, double st, double coeff, 
   g.dt = dt;
   g.st_ = st;
   g.coeff = coeff;
-  launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, meanfix, g.b, g.parts, g.scal + 4, g.s);
+  launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, meanfix, g.b, g.parts, g.scal + 4, g.s, g.comp, g.ncomp);
   double sc[2];
   CK(cudaMemcpyAsync(sc, g.scal + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
   CK(cudaStreamSynchronize(g.s));
@@ -1805,7 +1894,7 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
   g.st_ = st;
   g.coeff = coeff;
   dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8), g.s);
-  dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s), g.s);
+  dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s, g.comp, g.ncomp), g.s);
 }
 // After the solve: pressure, projection, Contra2Cart, divergence.
 // Host outputs (nullable) leave on the grid's copy stream as soon as their
@@ -2291,6 +2380,16 @@ int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y
   cudaFree(dx);
   cudaFree(dy);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "prolong");
+  return VFS_OK;
+}
+
+int vfs_grid_components(vfs_ctx* ctx, int grid, int* finest, int* coarsest) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (!gp->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run first");
+  if (finest) *finest = gp->ncomp;
+  if (coarsest) *coarsest = gp->ncomp_c;
   return VFS_OK;
 }
 

@@ -28,8 +28,10 @@ int launch_coarsen(const Dims& f, const Dims& c, int si, int sj, int sk, const d
                    double* coor_c, double* nv_c, cudaStream_t s);
 int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nv_f, const double* nv_c,
                          uint8_t* code, cudaStream_t s);
+// ccomp (nullable): labels of the level's connected fluid regions, one
+// sigma e_q e_q^T term per region
 int launch_dense_inverse(const Dims& d, const double* mcoef, double sigma, double* W, double* fac, int* piv, double* pval,
-                         double* Binv, float* Binv32, int n, cudaStream_t s);
+                         double* Binv, float* Binv32, int n, cudaStream_t s, const int* ccomp = nullptr);
 
 // ---- stencils and multigrid (k_mg.cu) ----
 // y = A x (FP64 accumulate; x FP64 or FP32); r = b - A x when b != nullptr.

@@ -17,12 +17,16 @@ int partial_blocks(const Dims& d);
 int launch_finish_sums(const double* parts, int nparts, int nq, double* out, cudaStream_t s);
 int launch_aos2soa(size_t n, const double* aos, double* x, double* y, double* z, cudaStream_t s);
 int launch_soa2aos(size_t n, const double* x, const double* y, const double* z, double* aos, cudaStream_t s);
+// comp / ncomp: labels 0..ncomp-1 of the connected fluid regions (nullptr
+// when the fluid is one region): the compatibility fix and the mean removal
+// then act per region.  sc holds 4 doubles for launch_rhs.
 int launch_rhs(const Dims& d, const Ucont& u, const double* nvert, double dt, double st, double coeff, int meanfix,
-               double* b, double* parts, double* sc, cudaStream_t s);
+               double* b, double* parts, double* sc, cudaStream_t s, const int* comp = nullptr, int ncomp = 1);
 int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nvert, const double* M, double* parts,
                        double* fa4, cudaStream_t s,
                        const uint8_t* nb8 = nullptr);
-int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s);
+int launch_remove_mean(const Dims& d, const double* nvert, double* x, double* parts, double* sc, cudaStream_t s,
+                       const int* comp = nullptr, int ncomp = 1);
 int launch_phi_finish(const Dims& d, const double* nvert, double* phi, cudaStream_t s);
 int launch_update_pressure(const Dims& d, const double* nvert, const double* phi, double* p, cudaStream_t s);
 int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s);
