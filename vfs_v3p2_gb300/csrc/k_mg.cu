@@ -289,6 +289,9 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 #ifndef VFS_SMOOTH_MINBLK
 #define VFS_SMOOTH_MINBLK 152  // automatic tile: narrow while a sweep has fewer blocks (one per SM)
 #endif
+#ifndef VFS_SMOOTH_TWMIN
+#define VFS_SMOOTH_TWMIN 8  // automatic tile: narrowest width
+#endif
 #ifndef VFS_SMOOTH_U3
 #define VFS_SMOOTH_U3 8  // phase-3 (write) loop unroll
 #endif
@@ -670,7 +673,7 @@ static int smooth_tw(int ni, int nj, int nk, int cols) {
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
   if (cols == 0)
-    while (tw > 8 && (size_t)((ni + tw - 1) / tw) * nk < VFS_SMOOTH_MINBLK) tw >>= 1;
+    while (tw > VFS_SMOOTH_TWMIN && (size_t)((ni + tw - 1) / tw) * nk < VFS_SMOOTH_MINBLK) tw >>= 1;
   return tw;
 }
 
