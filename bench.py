@@ -411,6 +411,23 @@ def main_serve(args, dist, rank, local, ws):
     ctx.close()
 
 
+def kernel_table(recs, top):
+    """Per kernel (finest level / coarser levels): launches, device ms,
+    algorithmic GB and achieved GB/s, largest time first."""
+    agg = {}
+    for name, lv, ms, by in recs:
+        key = (name, "finest" if lv == top else "coarser levels")
+        a = agg.setdefault(key, [0, 0.0, 0.0])
+        a[0] += 1
+        a[1] += ms
+        a[2] += by
+    out = []
+    for (name, where), (n, ms, by) in sorted(agg.items(), key=lambda kv: -kv[1][1]):
+        out.append({"kernel": name, "levels": where, "launches": n, "ms": ms, "alg_gb": by / 1e9,
+                    "achieved_gbs": (by / (ms / 1e3) / 1e9) if ms > 0 else 0.0})
+    return out
+
+
 def nu_coarse(args) -> str:
     if args.nu_coarse is not None:
         return args.nu_coarse
@@ -491,6 +508,13 @@ def main():
     ctx.probe_begin(capi.PROBE_SMOOTH)
     steps(mixed, min(args.steps, 5), 600)
     plaunch, pms, pbytes = ctx.probe_end()
+    # every instrumented kernel of the step, likewise, for the per-kernel
+    # achieved GB/s and the step's algorithmic bytes
+    KP = 3
+    ctx.probe_begin(capi.PROBE_ALL)
+    steps(mixed, KP, 650)
+    n_all, _, bytes_all = ctx.probe_end()
+    per_kernel = kernel_table(ctx.probe_records(n_all), case.levels - 1)
 
     # ---- the same mixed solve with the other multigrid operator storage ----
     alt = None
@@ -548,6 +572,13 @@ def main():
             "traffic": traffic, "launches": plaunch, "avg_launch_ms": pms / plaunch if plaunch else None,
             "alg_bytes_per_launch": pbytes / plaunch if plaunch else None}
 
+    step_bytes = bytes_all / KP
+    solve_hbm = {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (tmax / args.steps / 1e3) / 1e9,
+                 "unit": "GB/s", "peak": peak, "frac": step_bytes / (tmax / args.steps / 1e3) / 1e9 / peak,
+                 "note": "algorithmic bytes of every instrumented launch of a step (probed run) over the unprobed "
+                         "device time of a step"}
+    kernels = [dict(k, frac=k["achieved_gbs"] / peak) for k in per_kernel]
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cval, cores, _ = cpu_baseline(case, args, steps=2)
@@ -574,7 +605,8 @@ def main():
                      "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
                      "phi_rel_l2_mixed_vs_fp64": mix_vs_fp64_err},
             "mixed_other_operator": alt,
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl),
+            "roofline": roof, "solve_hbm": solve_hbm, "kernels": kernels,
+            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl),
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -355,11 +355,17 @@ int vfs_sync(vfs_ctx* ctx);
 /* ---- measurement ---- */
 #define VFS_PROBE_SMOOTH 1   /* full y-line sweeps of the finest multigrid level */
 #define VFS_PROBE_APPLY64 2  /* FP64 outer operator apply (w = A z) */
+#define VFS_PROBE_ALL 3      /* every instrumented launch of the step (per record: kernel, level) */
 /* Record a CUDA event pair around every launch of one kernel (on the stream
  * it runs on) until vfs_probe_end, which returns the launch count, their
- * summed device time and their summed algorithmic bytes. */
+ * summed device time and their summed algorithmic bytes (the compulsory HBM
+ * reads and writes of each launch).  Iteration graphs are not used while a
+ * probe is open, and the host checks convergence after every iteration. */
 int vfs_probe_begin(vfs_ctx* ctx, int kernel);
 int vfs_probe_end(vfs_ctx* ctx, unsigned long long* launches, double* total_ms, double* alg_bytes);
+/* Record i (0-based, < launches) of the last probe: kernel name, multigrid
+ * level (finest = levels - 1), device time and algorithmic bytes. */
+int vfs_probe_record(vfs_ctx* ctx, int i, char* name, int name_len, int* level, double* ms, double* alg_bytes);
 /* CUDA event `slot` (0..4095) recorded on the stream of a grid; elapsed
  * device time between two recorded slots. */
 int vfs_mark(vfs_ctx* ctx, int grid, int slot);

@@ -144,6 +144,7 @@ SIGNATURES = {
     "vfs_mark": ([_P, _I, _I], _I),
     "vfs_elapsed": ([_P, _I, _I, _DP], _I),
     "vfs_grid_components": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "vfs_probe_record": ([_P, _I, ctypes.c_char_p, _I, ctypes.POINTER(_I), _DP, _DP], _I),
     "vfs_sweep_damping": ([ctypes.POINTER(SolveParams), _I, _I, _DP, _I], _I),
     "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
     "vfs_host_unregister": ([_P], _I),
@@ -153,6 +154,7 @@ SIGNATURES = {
 
 PROBE_SMOOTH = 1
 PROBE_APPLY64 = 2
+PROBE_ALL = 3
 
 
 def launch_count() -> int:
@@ -405,6 +407,17 @@ class Context:
         by = ctypes.c_double()
         self.check(self.L.vfs_probe_end(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(by)))
         return n.value, ms.value, by.value
+
+    def probe_records(self, n: int):
+        """The last probe's records: (kernel, level, ms, algorithmic bytes)."""
+        out = []
+        buf = ctypes.create_string_buffer(64)
+        lv, ms, by = _I(), ctypes.c_double(), ctypes.c_double()
+        for i in range(n):
+            self.check(self.L.vfs_probe_record(self.h, i, buf, 64, ctypes.byref(lv), ctypes.byref(ms),
+                                               ctypes.byref(by)))
+            out.append((buf.value.decode(), lv.value, ms.value, by.value))
+        return out
 
     def host_register(self, a: np.ndarray):
         rc = self.L.vfs_host_register(a.ctypes.data_as(_P), a.nbytes)

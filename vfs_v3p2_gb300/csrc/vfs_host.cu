@@ -33,27 +33,54 @@ std::atomic<unsigned long long> vfs::g_launches{0};
 
 namespace {
 
-// CUDA-event probe around every launch of one kernel of the finest level
-// (timed on the stream the kernel runs on), with its algorithmic bytes.
+// CUDA-event probe around every launch of one kernel of the finest level, or
+// (VFS_PROBE_ALL) around every instrumented launch of a step, timed on the
+// stream the kernel runs on, with its algorithmic bytes: the compulsory HBM
+// reads and writes of the launch (operands once, results once).
+struct ProbeRec {
+  const char* name;
+  int level;
+  int ev;  // index of the start event
+  double bytes;
+  double ms = 0.;  // filled by vfs_probe_end
+};
 struct Probe {
   int kind = 0;  // VFS_PROBE_*
   std::vector<cudaEvent_t> ev;
   int used = 0;
   double bytes = 0.;
   unsigned long long launches = 0;
+  std::vector<ProbeRec> recs;
+  bool wants(int k) const { return kind != 0 && (kind == k || kind == VFS_PROBE_ALL); }
   bool begin(cudaStream_t s) {
     if (used + 2 > (int)ev.size()) return false;
     cudaEventRecord(ev[used], s);
     return true;
   }
-  void end(cudaStream_t s, double b) {
+  void end(cudaStream_t s, double b, const char* name = "", int level = -1) {
     cudaEventRecord(ev[used + 1], s);
+    recs.push_back({name, level, used, b});
     used += 2;
     bytes += b;
     launches++;
   }
 };
 Probe g_probe;
+
+// Probe scope of one launcher call (kind k, or any under VFS_PROBE_ALL).
+struct Probed {
+  bool on;
+  cudaStream_t s;
+  const char* name;
+  int level;
+  double bytes;
+  Probed(int k, cudaStream_t s_, const char* n, int l, double b) : s(s_), name(n), level(l), bytes(b) {
+    on = g_probe.wants(k) && g_probe.begin(s);
+  }
+  ~Probed() {
+    if (on) g_probe.end(s, bytes, name, level);
+  }
+};
 
 // VFS_DEBUG_SYNC=1: synchronise after every launch stage of the solve and
 // report the first stage that leaves a CUDA error (a self-check for faults).
@@ -409,11 +436,18 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 template <typename T>
 void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols,
                    bool solo, cudaStream_t s) {
-  const bool probe = g_probe.kind == VFS_PROBE_SMOOTH && xi && l == g.L - 1 && g_probe.begin(s);
-  int rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo);
-  // the coefficient slots (FP16 or T), x, b and 1/m read, x written
+  // x != 0: the coefficient slots (FP16 or T), x, b and 1/m read, x written;
+  // from a zero guess: the centre (not with the FP16 operator), SP and NP
+  // slots, b and 1/m read, x written
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
-  if (probe) g_probe.end(s, (double)n_interior(A.d) * (slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)));
+  const double bytes = (double)n_interior(A.d) * (xi ? slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)
+                                                     : slot_bytes * (A.hcoef ? 2 : 3) + 3.0 * sizeof(T));
+  const int kind = (xi && l == g.L - 1) ? VFS_PROBE_SMOOTH : VFS_PROBE_ALL;
+  int rc;
+  {
+    Probed pr(kind, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
+    rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo);
+  }
   dbg("smooth", l, rc, s);
 }
 
@@ -437,6 +471,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   if (((W - 1) & 1) == 1) std::swap(bufs[0], bufs[1]);
   if (l == 0) {
     if (binv<T>(L)) {
+      Probed pr(VFS_PROBE_ALL, s, "k_coarse_gemv", l, ((double)L.nco * L.nco + 2.0 * L.nco) * sizeof(T));
       dbg("coarse_gemv", l, launch_coarse_gemv<T>(L.d, binv<T>(L), L.nco, b, bufs[0], dsc_sel<T>(L, half), skip, s),
           s);
       return bufs[0];
@@ -444,7 +479,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     T* cur = nullptr;
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      launch_smooth<T>(A, lf, cur, b, o, (T)c.omega_c, s, c.cols, c.solo);
+      smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega_c, c.cols, c.solo, s);
       cur = o;
     }
     return cur;
@@ -458,16 +493,29 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   Level& C = g.lev[l - 1];
   T** xc = xbuf<T>(C);
-  dbg("residual_restrict", l,
-      launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0], s),
-      s);
+  const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T), nf = (double)n_interior(L.d);
+  {
+    // the slots, x, b and the restriction weights read; the coarse right-hand
+    // side and the cleared coarse x written
+    Probed pr(VFS_PROBE_ALL, s, "k_resrestrict", l,
+              nf * (slot_bytes * popcount(A.mask) + 3.0 * sizeof(T)) + 2.0 * n_interior(C.d) * sizeof(T));
+    dbg("residual_restrict", l,
+        launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0],
+                                    s),
+        s);
+  }
   T* ec = vcycle<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, skip, s);
-  if (!cur) {
-    cur = bufs[q & 1];
-    q++;
-    dbg("prolong", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 0, skip, s), s);
-  } else {
-    dbg("prolong_add", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s), s);
+  {
+    // code byte and coarse correction read, fine x written (read too when added)
+    Probed pr(VFS_PROBE_ALL, s, "k_prolong", l,
+              nf * (1.0 + (cur ? 2.0 : 1.0) * sizeof(T)) + (double)n_interior(C.d) * sizeof(T));
+    if (!cur) {
+      cur = bufs[q & 1];
+      q++;
+      dbg("prolong", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 0, skip, s), s);
+    } else {
+      dbg("prolong_add", l, launch_prolong<T>(L.d, L.pcode, C.d, ec, cur, 1, skip, s), s);
+    }
   }
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
@@ -621,9 +669,12 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
 // captured in a CUDA graph and replayed: V-cycle on T(v_j), w = A z_j with z
 // stored to Z[j], CGS2, Hessenberg/Givens update, v_{j+1} and T(v_{j+1}),
 // and a copy of the convergence flag to pinned memory (monotonic 0 -> 1).
+// nv: the host's count of basis columns (column j + 1), for the probe's
+// byte counts only (-1 when unknown, e.g. while capturing).
 template <typename T>
-void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
+void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s, int nv = -1) {
   const size_t N = ncell(g.d);
+  const double nvb = nv > 0 ? nv : 1, Nd = (double)N;
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
@@ -632,29 +683,54 @@ void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s) {
   const float* dinv = dinv_sel<T>(F, mc.half);
   vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mc, skip, s);
   {
-    const bool probe = g_probe.kind == VFS_PROBE_APPLY64 && g_probe.begin(s);
+    // the FP64 slots, z read; w and the Z column written
+    Probed pr(VFS_PROBE_APPLY64, s, "k_apply64_krylov", g.L - 1,
+              (double)n_interior(F.d) * (8.0 * popcount(F.mask) + 2 * sizeof(T) + 8.0));
     OpView<double> A{F.d, F.mcoef, F.mask, skip};
     launch_apply64_krylov<T>(A, zt, zbase<T>(g), g.st, g.w, s);
-    if (probe) g_probe.end(s, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + 2 * sizeof(T) + 8.0));
   }
   dbg("apply64", g.L - 1, 0, s);
-  dbg("multidot1", 0, launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 1, s), s);
+  {
+    // the nv basis columns and w read (the finish reads block partials only)
+    Probed pr(VFS_PROBE_ALL, s, "k_multidot", g.L - 1, Nd * (nvb + 1.0) * 8.0);
+    dbg("multidot1", 0, launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 1, s), s);
+  }
   if (p.orth == VFS_ORTH_CGS) {
     // one pass: update, next column, next preconditioner input, norm partials
-    dbg("cgs_update", 0, launch_cgs_update<T>(g.st, g.V, g.w, bbuf<T>(F), N, g.parts, s, dinv), s);
-    dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
+    {
+      // w and the nv columns read; the new column and the multigrid input written
+      Probed pr(VFS_PROBE_ALL, s, "k_cgs_update", g.L - 1,
+                Nd * ((nvb + 2.0) * 8.0 + sizeof(T) + (dinv ? 4.0 : 0.0)));
+      dbg("cgs_update", 0, launch_cgs_update<T>(g.st, g.V, g.w, bbuf<T>(F), N, g.parts, s, dinv), s);
+    }
+    {
+      Probed pr(VFS_PROBE_ALL, s, "k_arnoldi_finish", g.L - 1, 0.);
+      dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
+    }
     launch_status_copy(g.st, g.hstat, s);
     return;
   }
-  if (g.m + 1 <= 32) {
-    dbg("gs_update_dots", 0, launch_gs_update_dots(g.st, g.V, -1, g.w, N, g.parts, s, g.m + 1), s);
-  } else {
-    launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 1, s);
-    launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 2, s);
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_gs_update_dots", g.L - 1, Nd * (nvb + 2.0) * 8.0);
+    if (g.m + 1 <= 32) {
+      dbg("gs_update_dots", 0, launch_gs_update_dots(g.st, g.V, -1, g.w, N, g.parts, s, g.m + 1), s);
+    } else {
+      launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 1, s);
+      launch_multidot(g.st, g.V, -1, g.w, N, g.parts, 2, s);
+    }
   }
-  dbg("gs_update2", 0, launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 2, s), s);
-  dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
-  dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, nullptr, bbuf<T>(F), N, s, g.V, dinv), s);
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_gs_update", g.L - 1, Nd * (nvb + 2.0) * 8.0);
+    dbg("gs_update2", 0, launch_gs_update(g.st, g.V, -1, g.w, N, g.parts, 2, s), s);
+  }
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_arnoldi_finish", g.L - 1, 0.);
+    dbg("arnoldi", 0, launch_arnoldi_finish(g.st, krylov_nblocks(N), g.parts, s), s);
+  }
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_vnext_in", g.L - 1, Nd * (16.0 + sizeof(T)));
+    dbg("vnext_in", 0, launch_vnext_in<T>(g.st, g.w, nullptr, bbuf<T>(F), N, s, g.V, dinv), s);
+  }
   launch_status_copy(g.st, g.hstat, s);
 }
 
@@ -711,13 +787,21 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
 // Close a cycle (least squares, x update) and, unless finished, open the next
 // one from the true residual of the updated phi.
 template <typename T>
-void fg_cycle_end(Grid& g, const vfs_solve_params& p, bool last, cudaStream_t s) {
+void fg_cycle_end(Grid& g, const vfs_solve_params& p, bool last, cudaStream_t s, int ncols = 0) {
   const size_t N = ncell(g.d);
   dbg("lsq", 0, launch_lsq_update(g.st, s), s);
-  dbg("x_update", 0, launch_x_update<T>(g.st, zbase<T>(g), N, g.phi, s), s);
+  {
+    // the cycle's ncols directions and phi read, phi written
+    Probed pr(VFS_PROBE_ALL, s, "k_x_update", g.L - 1, (double)N * (ncols * (double)sizeof(T) + 16.0));
+    dbg("x_update", 0, launch_x_update<T>(g.st, zbase<T>(g), N, g.phi, s), s);
+  }
   dbg("restart_reset", 0, launch_restart_reset(g.st, s), s);
   if (last) return;
-  apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s);
+  {
+    Level& F = g.lev[g.L - 1];
+    Probed pr(VFS_PROBE_ALL, s, "k_apply64 (residual)", g.L - 1, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + 24.0));
+    apply_outer(g, g.phi, g.bs, g.V, &g.st->done, s);
+  }
   launch_norm_init(g.st, g.V, N, g.parts, 0, s);
   fg_open_cycle<T>(g, p, s);
 }
@@ -731,13 +815,15 @@ int fg_after(vfs_ctx* ctx, Fgmres& f, cudaStream_t s) {
   f.it++;
   f.j++;
   CK(cudaEventRecord(g.ev[f.it & 1], s));
-  if (f.it >= 2) {
-    CK(cudaEventSynchronize(g.ev[(f.it - 1) & 1]));
+  // the flag of the previous iteration; while probing, of this one (no
+  // iteration is issued past convergence, so the probe counts only work done)
+  if (f.it >= 2 || g_probe.kind) {
+    CK(cudaEventSynchronize(g.ev[(g_probe.kind ? f.it : f.it - 1) & 1]));
     if (g.hstat[0] && g.hstat[1] == f.epoch) f.observed = true;
   }
   if (f.observed || f.it >= p.maxit || f.j == p.restart) {
     const bool last = f.observed || f.it >= p.maxit;
-    fg_cycle_end<T>(g, p, last, s);
+    fg_cycle_end<T>(g, p, last, s, f.j);
     f.finished = last;
     f.j = 0;
   }
@@ -756,7 +842,7 @@ int fg_step(vfs_ctx* ctx, Fgmres& f) {
     CK(cudaGraphLaunch(ex, g.s));
     g_launches += g.ig_kernels;
   } else {
-    issue_iteration<T>(g, *f.p, g.s);
+    issue_iteration<T>(g, *f.p, g.s, f.j + 1);
   }
   return fg_after<T>(ctx, f, g.s);
 }
@@ -918,9 +1004,15 @@ int job_check_enqueue(vfs_ctx* ctx, Job& J) {
   const size_t N = ncell(g.d);
   cudaStream_t s = g.s;
   Level& F = g.lev[g.L - 1];
-  dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
-  dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
-  dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s, g.nb8), s);
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_apply64 (residual)", g.L - 1, (double)n_interior(F.d) * (8.0 * popcount(F.mask) + 24.0));
+    dbg("true_residual", 0, apply_outer(g, g.phi, g.bs, g.w, nullptr, s), s);
+  }
+  {
+    Probed pr(VFS_PROBE_ALL, s, "k_norm2 + k_masked_absmax", g.L - 1, (double)N * (8.0 + 8.0 + (g.nb8 ? 1.0 : 8.0)));
+    dbg("norm2", 0, launch_norm2(g.w, N, g.parts, g.scal + 16, s), s);
+    dbg("masked_max", 0, launch_masked_absmax(F.d, g.w, F.nvert, g.parts, g.scal + 17, s, g.nb8), s);
+  }
   CK(cudaMemcpyAsync(g.hk, g.st, sizeof(KrylovState), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(g.hv, g.scal + 16, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(g.ev_chk, s));
@@ -950,8 +1042,15 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     cudaStream_t s = g.s;
     Level& F = g.lev[g.L - 1];
     const size_t N = ncell(g.d);
-    dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s, g.comp, g.ncomp), s);
-    dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
+    {
+      // per region: nvert and phi read; nvert and phi read, phi written
+      Probed pr(VFS_PROBE_ALL, s, "k_fluid_sum + k_sub_mean", g.L - 1, (double)N * 40.0 * g.ncomp);
+      dbg("remove_mean", 0, launch_remove_mean(F.d, F.nvert, g.phi, g.parts, g.scal, s, g.comp, g.ncomp), s);
+    }
+    {
+      Probed pr(VFS_PROBE_ALL, s, "k_phi_zero + ghosts", g.L - 1, (double)N * 16.0);
+      dbg("phi_finish", 0, launch_phi_finish(F.d, F.nvert, g.phi, s), s);
+    }
     CK(cudaEventRecord(g.t1, s));
     if (J.post) {
       const int rp = step_post(g, J.dt, J.st, J.coeff, J.u_out, J.p_out, J.p_in_pending);
@@ -1893,8 +1992,21 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
   g.dt = dt;
   g.st_ = st;
   g.coeff = coeff;
-  dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8), g.s);
-  dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s, g.comp, g.ncomp), g.s);
+  const double N = (double)ncell(F.d), nvb = g.nb8 ? 1.0 : 8.0;
+  {
+    // two passes over the fluid mask (the interface faces' fluxes and metric
+    // norms are few)
+    Probed pr(VFS_PROBE_ALL, g.s, "k_vflux (2 passes)", g.L - 1, 2.0 * N * nvb);
+    dbg("volume_flux", 0, launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8),
+        g.s);
+  }
+  {
+    // U (3 components) and nvert read, b written; the mean fix reads nvert and
+    // b and writes b
+    Probed pr(VFS_PROBE_ALL, g.s, "k_rhs + k_meanfix", g.L - 1, N * (40.0 + 24.0 * g.ncomp));
+    dbg("rhs", 0, launch_rhs(F.d, g.U(), F.nvert, dt, st, coeff, 1, g.b, g.parts, g.scal + 4, g.s, g.comp, g.ncomp),
+        g.s);
+  }
 }
 // After the solve: pressure, projection, Contra2Cart, divergence.
 // Host outputs (nullable) leave on the grid's copy stream as soon as their
@@ -1911,13 +2023,22 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     if (r != cudaSuccess && e == cudaSuccess) e = r;
   };
   if (p_in_pending) ok(cudaStreamWaitEvent(g.s, g.ev_pin, 0));
-  dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
+  const double Nd = (double)N;
+  {
+    // nvert and phi read, p read and written
+    Probed pr(VFS_PROBE_ALL, g.s, "k_update_p", g.L - 1, Nd * 32.0);
+    dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
+  }
+  // projection: the 9 metric products, 3 face Jacobians, nvert bytes (or
+  // doubles) and phi read, U read and written
+  const double proj_b = 9 * 8.0 + 24.0 + (g.nb8 ? 1.0 : 8.0) + 8.0 + 48.0;
   if (p_out) {
     ok(cudaEventRecord(g.ev_p, g.s));
     ok(cudaStreamWaitEvent(g.cs, g.ev_p, 0));
     ok(cudaMemcpyAsync(p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
   }
   if (!u_out) {
+    Probed pr(VFS_PROBE_ALL, g.s, "k_projection", g.L - 1, Nd * proj_b);
     dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
   } else {
     // Interior planes in slabs: a slab is projected and converted to AoS on
@@ -1939,8 +2060,11 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     const int S = std::min(inner, transfer_slabs(N));
     for (int q = 0; q < S; q++) {
       const int k0 = 1 + (int)((long long)inner * q / S), k1 = 1 + (int)((long long)inner * (q + 1) / S);
-      dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s, k0, k1),
-          g.s);
+      {
+        Probed pr(VFS_PROBE_ALL, g.s, "k_projection", g.L - 1, (double)(k1 - k0) * P * proj_b);
+        dbg("projection", 0,
+            launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s, k0, k1), g.s);
+      }
       to_aos(k0, k1);
       ok(cudaEventRecord(g.ev_u, g.s));
       ok(cudaStreamWaitEvent(g.cs, g.ev_u, 0));
@@ -1955,8 +2079,17 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     download(0, 1);
     download(mz - 1, mz);
   }
-  dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
-  dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8), g.s);
+  {
+    // the inverse metric (9), nvert and U read, Ucat written
+    Probed pr(VFS_PROBE_ALL, g.s, "k_contra2cart", g.L - 1, Nd * (72.0 + 8.0 + 24.0 + 24.0));
+    dbg("contra2cart", 0, launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s), g.s);
+  }
+  {
+    // U, aj and the nvert bytes (or doubles) read
+    Probed pr(VFS_PROBE_ALL, g.s, "k_divergence", g.L - 1, Nd * (24.0 + 8.0 + (g.nb8 ? 1.0 : 8.0)));
+    dbg("divergence", 0, launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8),
+        g.s);
+  }
   if (p_out || u_out) {
     ok(cudaEventRecord(g.ev_cs, g.cs));
     ok(cudaStreamWaitEvent(g.s, g.ev_cs, 0));
@@ -2120,7 +2253,8 @@ int vfs_memory(vfs_ctx* ctx, unsigned long long* used, unsigned long long* budge
 
 int vfs_probe_begin(vfs_ctx* ctx, int kernel) {
   if (!ctx) return VFS_ERR_ARG;
-  if (kernel != VFS_PROBE_SMOOTH && kernel != VFS_PROBE_APPLY64) return fail(ctx, VFS_ERR_ARG, "unknown probe kernel");
+  if (kernel != VFS_PROBE_SMOOTH && kernel != VFS_PROBE_APPLY64 && kernel != VFS_PROBE_ALL)
+    return fail(ctx, VFS_ERR_ARG, "unknown probe kernel");
   CK(cudaSetDevice(ctx->device));
   if (g_probe.ev.empty()) {
     g_probe.ev.resize(2 * 8192);
@@ -2130,6 +2264,7 @@ int vfs_probe_begin(vfs_ctx* ctx, int kernel) {
   g_probe.used = 0;
   g_probe.bytes = 0.;
   g_probe.launches = 0;
+  g_probe.recs.clear();
   return VFS_OK;
 }
 
@@ -2137,15 +2272,29 @@ int vfs_probe_end(vfs_ctx* ctx, unsigned long long* launches, double* total_ms, 
   if (!ctx) return VFS_ERR_ARG;
   CK(cudaDeviceSynchronize());
   double ms = 0.;
-  for (int q = 0; q + 1 < g_probe.used; q += 2) {
+  for (ProbeRec& r : g_probe.recs) {
     float t = 0.f;
-    CK(cudaEventElapsedTime(&t, g_probe.ev[q], g_probe.ev[q + 1]));
+    CK(cudaEventElapsedTime(&t, g_probe.ev[r.ev], g_probe.ev[r.ev + 1]));
+    r.ms = t;
     ms += t;
   }
   if (launches) *launches = g_probe.launches;
   if (total_ms) *total_ms = ms;
   if (alg_bytes) *alg_bytes = g_probe.bytes;
   g_probe.kind = 0;
+  return VFS_OK;
+}
+
+int vfs_probe_record(vfs_ctx* ctx, int i, char* name, int name_len, int* level, double* ms, double* alg_bytes) {
+  if (!ctx || i < 0 || i >= (int)g_probe.recs.size()) return VFS_ERR_ARG;
+  const ProbeRec& r = g_probe.recs[i];
+  if (name && name_len > 0) {
+    std::strncpy(name, r.name, (size_t)name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (level) *level = r.level;
+  if (ms) *ms = r.ms;
+  if (alg_bytes) *alg_bytes = r.bytes;
   return VFS_OK;
 }
 
