@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--config", default="sphere", choices=["channel", "sphere", "terrain", "batch", "serve"])
     ap.add_argument("--requests", type=int, default=400, help="serve: timed requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate, requests/s")
-    ap.add_argument("--tune", action="store_true", help="batch/serve: autotune sweeps and tiles per size class")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batch/serve: default solve parameters instead of the autotuner's per size class")
     ap.add_argument("--scale", type=int, default=1, help="divide each grid extent (quick runs)")
     ap.add_argument("--grid", default=None, help="NIxNJxNK override of the sphere workload (profiling sizes)")
     ap.add_argument("--rtol", type=float, default=1e-9)
@@ -276,10 +277,10 @@ def main_batch(args, dist, rank, local, ws):
         ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
         ids.append(gid)
     tuned = None
-    if args.tune:
+    if not args.no_tune:
         plist, tuned = autotune.tuned_params_batch(ctx, ids, cases, base)
     else:
-        plist = base
+        plist = [base] * len(ids)
     for _ in range(args.warmup):
         ctx.projection_step_batch(ids, plist)
     clk = Clocks(local)
@@ -300,10 +301,9 @@ def main_batch(args, dist, rank, local, ws):
     value = ws * len(ids) * args.steps / total
     fp64 = None
     if not args.no_fp64:
-        # the same grids in plain FP64 (same smoother settings): batched, and
-        # one grid at a time through the single-grid step
-        p64 = capi.default_params(precision="fp64", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
-                                  restart=args.restart)
+        # the same grids in plain FP64 (each with its mixed run's smoothing
+        # settings): batched, and one grid at a time through the single-grid step
+        p64 = [autotune.with_precision(p, capi.VFS_FP64) for p in plist]
         ctx.projection_step_batch(ids, p64)
         K64 = max(2, args.steps // 2)
         t0 = time.perf_counter()
@@ -313,12 +313,12 @@ def main_batch(args, dist, rank, local, ws):
             its64 += [i["iterations"] for i in infos]
             dm64.append(float(dm.max()))
         t_b = allmax(dist, time.perf_counter() - t0)
-        for gid in ids:
-            ctx.projection_step(gid, p64)
+        for gid, p in zip(ids, p64):
+            ctx.projection_step(gid, p)
         t0 = time.perf_counter()
         dm1 = []
-        for gid in ids:
-            _, dm = ctx.projection_step(gid, p64)
+        for gid, p in zip(ids, p64):
+            _, dm = ctx.projection_step(gid, p)
             dm1.append(dm)
         t_1 = allmax(dist, time.perf_counter() - t0)
         r_b, r_1 = ws * len(ids) * K64 / t_b, ws * len(ids) / t_1
@@ -330,7 +330,7 @@ def main_batch(args, dist, rank, local, ws):
             "value": value, "unit": "solves/s", "steps": args.steps,
             "ms_per_step": 1e3 * total / args.steps, **base_line(args, ws),
             "config": {"workload": WORKLOAD["batch"], "grids": len(ids), "cells_total": int(cells),
-                       "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": bool(args.tune),
+                       "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": not args.no_tune,
                        "mg_operator": OPERATOR[base.mg_half],
                        "timer": "host wall clock around synchronous batch calls (results on the host)",
                        "parallelism": f"replicas x{ws}"},
@@ -353,6 +353,11 @@ def main_serve(args, dist, rank, local, ws):
     ctx = capi.Context(local, hbm_budget_bytes=120 * 10**9, max_inflight=16)
     params = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
                                  restart=args.restart, warm_start=1)
+    tuned = None
+    if not args.no_tune:  # per size class, single-grid latency objective
+        plist, tuned = autotune.tuned_params(ctx, [s.case for s in streams], params)
+        for s, p in zip(streams, plist):
+            s.params = p
     srv = serve.Server(ctx, streams, params)
     for s in streams:  # resident hierarchies of the 16 streams (admission)
         srv.ensure_grid(s)
@@ -379,8 +384,10 @@ def main_serve(args, dist, rank, local, ws):
         burst = serve.poisson_arrivals(args.requests, 1e6, 16, seed=11)
         rb, wb = srv.run(burst)
         cap = serve.summarize(rb, allmax(dist, wb))
-        srv.params = capi.default_params(precision="fp64", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
-                                         restart=args.restart, warm_start=1)
+        srv.params = autotune.with_precision(params, capi.VFS_FP64)
+        for s in streams:
+            if s.params is not None:
+                s.params = autotune.with_precision(s.params, capi.VFS_FP64)
         srv.run(warm)
         rb64, wb64 = srv.run(burst)
         cap64 = serve.summarize(rb64, allmax(dist, wb64))
@@ -399,12 +406,15 @@ def main_serve(args, dist, rank, local, ws):
             "config": {"workload": WORKLOAD["serve"], "streams": 16, "rate_req_s": args.rate,
                        "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16,
                        "mg_operator": OPERATOR[params.mg_half], "rtol": args.rtol,
-                       "div_tol": args.div_tol, "timer": "host wall clock, first arrival to last result",
+                       "div_tol": args.div_tol, "autotuned": not args.no_tune,
+                       "timer": "host wall clock, first arrival to last result",
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * summ["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "latency_ms": summ["latency_ms"], "iterations": summ["iterations"], "divmax": summ["divmax"],
             "failed": summ["failed"], "clocks": clocks, "gpu_launches": int(nl), "fp64": fp64}
+    if tuned:
+        line["autotune"] = tuned
     if rank == 0:
         print(json.dumps(line), flush=True)
     srv.close()

@@ -62,16 +62,21 @@ def size_class(case) -> str:
 
 
 def _time_candidate(ctx, gid, case, params, steps):
+    """Seconds per step, each step solving from zero: with a warm start the
+    repeated step would begin at its own solution and time the cycle's cost
+    alone, not the iterations a new request needs."""
     shp = case.grid.nvert.shape
+    p = with_precision(params, params.precision)
+    p.warm_start = 0
     ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
     ctx.set_field(gid, capi.FIELD_P, np.zeros(shp))
-    info, dm = ctx.projection_step(gid, params)  # warm-up: graph capture
+    info, dm = ctx.projection_step(gid, p)  # warm-up: graph capture
     if not info["converged"]:
         return math.inf
     t0 = time.perf_counter()
     for _ in range(steps):
-        info, dm = ctx.projection_step(gid, params)
-        if not info["converged"] or (params.div_tol > 0 and dm > params.div_tol):
+        info, dm = ctx.projection_step(gid, p)
+        if not info["converged"] or (p.div_tol > 0 and dm > p.div_tol and not info.get("div_limited")):
             return math.inf
     return (time.perf_counter() - t0) / steps
 
@@ -93,7 +98,7 @@ def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3)
                 t = math.inf
             if t < best_t:
                 best, best_t = cand, t
-        return best, best_t
+        return (best if best is not None else candidates[0]), best_t
     finally:
         ctx.grid_destroy(gid)
 
@@ -101,6 +106,14 @@ def tune_case(ctx, case, base: capi.SolveParams, candidates=CANDIDATES, steps=3)
 def ctypes_copy(dst, src):
     for name, _ in src._fields_:
         setattr(dst, name, getattr(src, name))
+
+
+def with_precision(p: capi.SolveParams, precision: int) -> capi.SolveParams:
+    """A copy of p in another precision (the same smoothing settings)."""
+    q = capi.SolveParams()
+    ctypes_copy(q, p)
+    q.precision = precision
+    return q
 
 
 def tuned_params(ctx, cases, base: capi.SolveParams, cache_path: str | None = None, steps=3):

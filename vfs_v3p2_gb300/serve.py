@@ -36,6 +36,7 @@ class Stream:
     inputs: list            # page-locked AoS U* variants
     p_out: np.ndarray       # page-locked pressure of the latest result
     grid: int | None = None
+    params: object = None   # the stream's SolveParams (autotuned), else the server's
     last_used: float = 0.0
     served: int = 0
     busy: bool = False
@@ -133,8 +134,8 @@ class Server:
         u = s.inputs[s.served % len(s.inputs)]
         while True:
             try:
-                t = self.ctx.submit(s.grid, self.params, ucont_in=u.ctypes.data, p_out=s.p_out.ctypes.data,
-                                    dt=self.dt)
+                t = self.ctx.submit(s.grid, s.params if s.params is not None else self.params,
+                                    ucont_in=u.ctypes.data, p_out=s.p_out.ctypes.data, dt=self.dt)
                 break
             except capi.VfsError as e:
                 # the solver memory reserved at admission does not fit: free an
