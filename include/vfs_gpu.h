@@ -91,10 +91,11 @@ typedef struct {
   int smooth_cols;  /* y-line smoother tile: i-columns per block, 0 (automatic: 32, fewer
                        for long lines), 8, 16 or 32 */
   int nu1_coarse, nu2_coarse;  /* sweeps on the levels below the finest (-1, the
-                                  default: nu1 / nu2).  More coarse sweeps save
+                                  default: nu1 / nu2).  With the constant
+                                  (Jacobi) damping, more coarse sweeps save
                                   iterations on one large grid (5 / 5 on
-                                  256x128x128) but lengthen small grids' latency-
-                                  bound cycles in a batch */
+                                  256x128x128); the Chebyshev damping needs
+                                  none beyond nu1 / nu2 */
   int mg_half;  /* VFS_MIXED only: 0 (the default) = the multigrid levels'
                    stencil coefficients are stored in FP32; 1 = stored as
                    FP16 normalised by their diagonal, with an FP16
