@@ -580,6 +580,8 @@ def main():
     roof = {"kernel": kname + " (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
             "traffic": traffic, "launches": plaunch, "avg_launch_ms": pms / plaunch if plaunch else None,
+            "timing": "CUDA event pair around each launch on its stream, over repeats of the timed steps "
+                      "(iterations issued uncaptured, convergence read after each; event and launch overhead included)",
             "alg_bytes_per_launch": pbytes / plaunch if plaunch else None}
 
     step_bytes = bytes_all / KP
