@@ -59,3 +59,27 @@ def test_probe_all_records_a_step(gpu_ctx):
 def test_probe_kinds_rejected(gpu_ctx):
     with pytest.raises(capi.VfsError):
         gpu_ctx.probe_begin(7)
+
+
+def test_probe_smooth_counts_real_sweeps(gpu_ctx):
+    """VFS_PROBE_SMOOTH brackets each run of consecutive full finest sweeps
+    with one event pair; it counts every real sweep and none of an iteration
+    past convergence."""
+    case = synth.c2_sphere(scale=4)
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    try:
+        gpu_ctx.poisson_lhs(gid)
+        params = capi.default_params(rtol=1e-9, div_tol=1e-8)
+        gpu_ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
+        gpu_ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
+        gpu_ctx.probe_begin(capi.PROBE_SMOOTH)
+        info, _ = gpu_ctx.projection_step(gid, params)
+        n, ms, by = gpu_ctx.probe_end()
+        sweeps = info["iterations"] * (params.nu1 - 1 + params.nu2)
+        assert n == sweeps and ms > 0
+        assert by == sweeps * g.ni * g.nj * g.nk * (11 * 4 + 16)
+        runs = gpu_ctx.probe_records(2 * info["iterations"])
+        assert all(r[0] == "k_smooth (run)" for r in runs)
+    finally:
+        gpu_ctx.grid_destroy(gid)

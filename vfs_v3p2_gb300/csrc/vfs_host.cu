@@ -57,12 +57,12 @@ struct Probe {
     cudaEventRecord(ev[used], s);
     return true;
   }
-  void end(cudaStream_t s, double b, const char* name = "", int level = -1) {
+  void end(cudaStream_t s, double b, const char* name = "", int level = -1, int count = 1) {
     cudaEventRecord(ev[used + 1], s);
     recs.push_back({name, level, used, b});
     used += 2;
     bytes += b;
-    launches++;
+    launches += count;
   }
 };
 Probe g_probe;
@@ -442,14 +442,40 @@ void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* lf, const T* xi,
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
   const double bytes = (double)n_interior(A.d) * (xi ? slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)
                                                      : slot_bytes * (A.hcoef ? 2 : 3) + 3.0 * sizeof(T));
-  const int kind = (xi && l == g.L - 1) ? VFS_PROBE_SMOOTH : VFS_PROBE_ALL;
   int rc;
   {
-    Probed pr(kind, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
+    Probed pr(VFS_PROBE_ALL, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
     rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo);
   }
   dbg("smooth", l, rc, s);
 }
+
+// VFS_PROBE_SMOOTH: one event pair around each run of consecutive full
+// sweeps (x != 0) of the finest level, so that the event overhead is shared
+// by the run's launches; bytes and launches counted per sweep.
+struct SweepRun {
+  bool on = false;
+  cudaStream_t s = nullptr;
+  int n = 0;
+  double bytes = 0.;
+  void add(bool probe, cudaStream_t s_, double b) {
+    if (!probe) return;
+    if (!on) {
+      s = s_;
+      on = g_probe.begin(s);
+    }
+    if (on) {
+      n++;
+      bytes += b;
+    }
+  }
+  void close() {
+    if (on && n) g_probe.end(s, bytes, "k_smooth (run)", -1, n);
+    on = false;
+    n = 0;
+    bytes = 0.;
+  }
+};
 
 // Number of buffer writes of a level's schedule (smoothing sweeps, plus the
 // prolongation when no pre-sweep wrote first): the result lands in
@@ -486,11 +512,17 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   int q = 0;
   T* cur = nullptr;
+  const bool run_probe = g_probe.kind == VFS_PROBE_SMOOTH && l == g.L - 1;
+  const double sweep_bytes = (double)n_interior(A.d) * ((A.hcoef ? 2.0 : (double)sizeof(T)) * popcount(A.mask) +
+                                                        4.0 * sizeof(T));
+  SweepRun run;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
+    if (cur) run.add(run_probe, s, sweep_bytes);
     smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s);
     cur = o;
   }
+  run.close();
   Level& C = g.lev[l - 1];
   T** xc = xbuf<T>(C);
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T), nf = (double)n_interior(L.d);
@@ -519,9 +551,11 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   }
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
+    run.add(run_probe, s, sweep_bytes);
     smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s);
     cur = o;
   }
+  run.close();
   return cur;
 }
 
