@@ -337,12 +337,6 @@ template <> double** xbuf<double>(Level& L) { return L.x64; }
 template <typename T> T*& bbuf(Level& L);
 template <> float*& bbuf<float>(Level& L) { return L.b32; }
 template <> double*& bbuf<double>(Level& L) { return L.b64; }
-template <typename T> T* lf_of(Level& L);
-template <> float* lf_of<float>(Level& L) { return L.lf32; }
-template <> double* lf_of<double>(Level& L) { return L.lf64; }
-template <typename T> T* rw_of(Level& L);
-template <> float* rw_of<float>(Level& L) { return L.rw32; }
-template <> double* rw_of<double>(Level& L) { return L.rw64; }
 template <typename T> T* binv(Level& L);
 template <> float* binv<float>(Level& L) { return L.Binv32; }
 template <> double* binv<double>(Level& L) { return L.Binv; }
@@ -434,8 +428,8 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // A full smoothing sweep (x != 0) streams the active coefficient slots, x,
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
-void smooth_probed(Grid& g, int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols,
-                   bool solo, cudaStream_t s) {
+void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols, bool solo,
+                   cudaStream_t s) {
   // x != 0: the coefficient slots (FP16 or T), x, b and 1/m read, x written;
   // from a zero guess: the centre (not with the FP16 operator), SP and NP
   // slots, b and 1/m read, x written
@@ -505,7 +499,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     T* cur = nullptr;
     for (int q = 0; q < c.ncoarse; q++) {
       T* o = bufs[q & 1];
-      smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.omega_c, c.cols, c.solo, s);
+      smooth_probed<T>(l, A, lf, cur, b, o, (T)c.omega_c, c.cols, c.solo, s);
       cur = o;
     }
     return cur;
@@ -519,7 +513,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
     if (cur) run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s);
     cur = o;
   }
   run.close();
@@ -552,7 +546,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
     run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(g, l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s);
     cur = o;
   }
   run.close();
@@ -617,11 +611,6 @@ int apply_outer(Grid& g, const double* x, const double* b, double* y, const int*
   Level& F = g.lev[g.L - 1];
   OpView<double> A{F.d, F.mcoef, F.mask, skip};
   return launch_apply64(A, x, b, y, s);
-}
-int apply_outer(Grid& g, const float* x, const double* b, double* y, const int* skip, cudaStream_t s) {
-  Level& F = g.lev[g.L - 1];
-  OpView<double> A{F.d, F.mcoef, F.mask, skip};
-  return launch_apply64_xf(A, x, b, y, s);
 }
 
 // ---------------------------------------------------------------------------
