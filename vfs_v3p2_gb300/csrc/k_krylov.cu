@@ -104,30 +104,51 @@ int launch_vnext(KrylovState* st, const double* w, double* vn, size_t n, cudaStr
 // nv < 0: use the device's current column count st->j + 1 (graph-replayable).
 __device__ __forceinline__ int nv_of(const KrylovState* st, int nv) { return nv < 0 ? st->j + 1 : nv; }
 
+// NQ consecutive basis columns V0 .. V0 + (NQ-1) n against w: two cells per
+// turn (their loads in flight together), each thread's cells accumulated in
+// increasing order.
+template <int NQ>
+__device__ __forceinline__ void dot_chunk(const double* __restrict__ V0, const double* __restrict__ w, size_t n,
+                                          double* a) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; t + stride < n; t += 2 * stride) {
+    const size_t u = t + stride;
+    const double wv = w[t], wu = w[u];
+    double v[NQ], x[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+      v[q] = V0[(size_t)q * n + t];
+      x[q] = V0[(size_t)q * n + u];
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; q++) a[q] = fma(x[q], wu, fma(v[q], wv, a[q]));
+  }
+  if (t < n) {
+    const double wv = w[t];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) a[q] = fma(V0[(size_t)q * n + t], wv, a[q]);
+  }
+}
+
 __global__ void __launch_bounds__(KB) k_multidot(const KrylovState* st, const double* __restrict__ V, int nv,
                                                  const double* __restrict__ w, size_t n, double* parts, int ld) {
   if (is_done(st)) return;
   nv = nv_of(st, nv);
   __shared__ double sh[32];
   for (int q0 = 0; q0 < nv; q0 += 4) {
-    double a0 = 0., a1 = 0., a2 = 0., a3 = 0.;
+    double a[4] = {0., 0., 0., 0.};
     const int nq = min(4, nv - q0);
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-      const double wv = w[t];
-      a0 = fma(V[(size_t)q0 * n + t], wv, a0);
-      if (nq > 1) a1 = fma(V[(size_t)(q0 + 1) * n + t], wv, a1);
-      if (nq > 2) a2 = fma(V[(size_t)(q0 + 2) * n + t], wv, a2);
-      if (nq > 3) a3 = fma(V[(size_t)(q0 + 3) * n + t], wv, a3);
+    const double* V0 = V + (size_t)q0 * n;
+    switch (nq) {
+      case 4: dot_chunk<4>(V0, w, n, a); break;
+      case 3: dot_chunk<3>(V0, w, n, a); break;
+      case 2: dot_chunk<2>(V0, w, n, a); break;
+      default: dot_chunk<1>(V0, w, n, a); break;
     }
-    a0 = block_sum(a0, sh);
-    if (nq > 1) a1 = block_sum(a1, sh);
-    if (nq > 2) a2 = block_sum(a2, sh);
-    if (nq > 3) a3 = block_sum(a3, sh);
-    if (threadIdx.x == 0) {
-      parts[(size_t)blockIdx.x * ld + q0] = a0;
-      if (nq > 1) parts[(size_t)blockIdx.x * ld + q0 + 1] = a1;
-      if (nq > 2) parts[(size_t)blockIdx.x * ld + q0 + 2] = a2;
-      if (nq > 3) parts[(size_t)blockIdx.x * ld + q0 + 3] = a3;
+    for (int q = 0; q < nq; q++) {
+      const double r = block_sum(a[q], sh);
+      if (threadIdx.x == 0) parts[(size_t)blockIdx.x * ld + q0 + q] = r;
     }
   }
 }
