@@ -981,11 +981,15 @@ int job_start(vfs_ctx* ctx, Job& J) {
   const size_t N = ncell(g.d);
   CK(cudaEventRecord(g.t0, g.s));
   if (J.pre) {
+    if (J.u_in || J.p_in) {
+      // host uploads run on the copy stream, after the step stream's earlier
+      // work on the staging buffer, the fluxes and the pressure
+      CK(cudaEventRecord(g.ev_uin, g.s));
+      CK(cudaStreamWaitEvent(g.cs, g.ev_uin, 0));
+    }
     if (J.u_in) {
       // the fluxes go up in k-plane slabs on the copy stream, each slab
       // converted to SoA on the step stream while the next one is in flight
-      CK(cudaEventRecord(g.ev_uin, g.s));
-      CK(cudaStreamWaitEvent(g.cs, g.ev_uin, 0));
       const int mz = g.d.mz;
       const size_t P = (size_t)g.d.mx * g.d.my;
       const int S = std::min(mz, transfer_slabs(N));
