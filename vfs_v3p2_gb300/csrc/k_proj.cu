@@ -90,7 +90,9 @@ int launch_soa2aos(size_t n, const double* x, const double* y, const double* z, 
 __global__ void __launch_bounds__(RB) k_rhs(Dims d, Ucont u, const double* __restrict__ nvert, double dt, double st,
                                             double coeff, double* b, double* parts) {
   __shared__ double sh[32];
-  double lsum = 0., lcnt = 0.;
+  __shared__ unsigned shc[32];
+  double lsum = 0.;
+  unsigned lcnt = 0;  // fluid cells, counted on the integer pipe (exact)
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     double val = 0.;
@@ -106,15 +108,15 @@ __global__ void __launch_bounds__(RB) k_rhs(Dims d, Ucont u, const double* __res
       else val += u.z[cidx(d, i, j, k - 1)];
       val *= -1.0 / dt * st * coeff;
       lsum += val;
-      lcnt += 1.;
+      lcnt += 1;
     }
     b[_t] = val;
   }
   lsum = block_sum(lsum, sh);
-  lcnt = block_sum(lcnt, sh);
+  lcnt = block_sum(lcnt, shc);
   if (threadIdx.x == 0) {
     parts[2 * blockIdx.x] = lsum;
-    parts[2 * blockIdx.x + 1] = lcnt;
+    parts[2 * blockIdx.x + 1] = (double)lcnt;
   }
 }
 // b += -sum / count on fluid interior cells (sc = {sum, count}).
@@ -250,19 +252,21 @@ int launch_volume_flux(const Dims& d, int mode, const Ucont& u, const double* nv
 __global__ void __launch_bounds__(RB) k_fluid_sum(Dims d, const double* __restrict__ nvert, const double* __restrict__ x,
                                                   double* parts, const int* __restrict__ comp, int q) {
   __shared__ double sh[32];
-  double s = 0., n = 0.;
+  __shared__ unsigned shc[32];
+  double s = 0.;
+  unsigned n = 0;  // counted on the integer pipe (exact)
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     if (interior(d, i, j, k) && nvert[_t] < 0.1 && (!comp || comp[_t] == q)) {
       s += x[_t];
-      n += 1.;
+      n += 1;
     }
   }
   s = block_sum(s, sh);
-  n = block_sum(n, sh);
+  n = block_sum(n, shc);
   if (threadIdx.x == 0) {
     parts[2 * blockIdx.x] = s;
-    parts[2 * blockIdx.x + 1] = n;
+    parts[2 * blockIdx.x + 1] = (double)n;
   }
 }
 __global__ void k_sub_mean(Dims d, const double* __restrict__ nvert, const double* __restrict__ sc, double* x,
@@ -329,9 +333,11 @@ int launch_update_pressure(const Dims& d, const double* nvert, const double* phi
 // kcsi.kzet, keta.kzet, kzet.kzet) and M the face Jacobians iaj, jaj, kaj,
 // multiplied in the reference's order: (dpdc * dot) * iaj.
 // ---------------------------------------------------------------------------
-// x / coeff is skipped when coeff == 1 (x / 1.0 == x exactly); r1 = r2 = r3
-// = 1 (no level set), so their divisions are always exact and omitted.
+// x / coeff is skipped when coeff == 1 (x / 1.0 == x exactly), and x * st
+// when st == 1 (x * 1.0 == x exactly); r1 = r2 = r3 = 1 (no level set), so
+// their divisions are always exact and omitted.
 __device__ __forceinline__ double div_c(double x, double coeff) { return coeff == 1.0 ? x : x / coeff; }
+__device__ __forceinline__ double mul_st(double x, double st) { return st == 1.0 ? x : x * st; }
 
 template <bool NVI>
 __global__ void __launch_bounds__(128) k_projection(Dims d, size_t c0, size_t c1, const double* __restrict__ pd,
@@ -387,7 +393,7 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, size_t c0, size_t c1
         }
         if (LT2((i, j, k), (i + 1, j, k))) {
           const double a = iaj[c];
-          u.x[c] -= div_c((dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt * st, coeff);
+          u.x[c] -= div_c(mul_st((dpdc * pd[0 * N + c] * a + dpde * pd[1 * N + c] * a + dpdz * pd[2 * N + c] * a) * dt, st), coeff);
         }
       }
     if (i > 0 && i < mx - 1 && k > 0 && k < mz - 1)
@@ -416,7 +422,7 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, size_t c0, size_t c1
         }
         if (LT2((i, j, k), (i, j + 1, k))) {
           const double a = jaj[c];
-          u.y[c] -= div_c((dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt * st, coeff);
+          u.y[c] -= div_c(mul_st((dpdc * pd[3 * N + c] * a + dpde * pd[4 * N + c] * a + dpdz * pd[5 * N + c] * a) * dt, st), coeff);
         }
       }
     if (i > 0 && i < mx - 1 && j > 0 && j < my - 1)
@@ -445,7 +451,7 @@ __global__ void __launch_bounds__(128) k_projection(Dims d, size_t c0, size_t c1
         else dpdz = PH(i, j, k + 1) - PH(i, j, k);
         if (LT2((i, j, k), (i, j, k + 1))) {
           const double a = kaj[c];
-          u.z[c] -= div_c((dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt * st, coeff);
+          u.z[c] -= div_c(mul_st((dpdc * pd[6 * N + c] * a + dpde * pd[7 * N + c] * a + dpdz * pd[8 * N + c] * a) * dt, st), coeff);
         }
       }
 #undef PH
