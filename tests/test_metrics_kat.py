@@ -1,0 +1,94 @@
+"""Known answers of the metrics on affine grids (FormMetrics, metrics.c:4-1290).
+
+On a grid with node r(i, j, k) = (i dx + s k dz + t j dy, j dy, k dz) every
+metric is constant: the area vectors are the cross products of the two
+other edge vectors, csi = r_eta x r_zeta, eta = r_zeta x r_xi,
+zet = r_xi x r_eta, and aj = 1 / det[r_xi r_eta r_zeta], at cell centres
+and on every face family alike (central and one-sided differences of a
+linear map are exact).  A uniform Cartesian velocity V then has face fluxes
+U = V . (face area vector); Contra2Cart returns V and the divergence is
+zero.  Checked on the oracle (CPU) and, through the metric hook, on the
+CUDA path."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from vfs_v3p2_gb300 import synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
+import oracle as O  # noqa: E402
+
+GEOMS = [(8, 6, 5, 0.5, 0.25, 0.2, 0.0, 0.0), (8, 6, 5, 0.5, 0.25, 0.2, 0.3, 0.0),
+         (10, 8, 6, 0.3, 0.4, 0.25, -0.2, 0.15)]
+
+
+def _grid(ni, nj, nk, dx, dy, dz, s, t):
+    mx, my, mz = ni + 2, nj + 2, nk + 2
+    coor = np.zeros((mz, my, mx, 3))
+    k, j, i = np.meshgrid(np.arange(nk + 1), np.arange(nj + 1), np.arange(ni + 1), indexing="ij")
+    coor[:nk + 1, :nj + 1, :ni + 1, 0] = i * dx + s * k * dz + t * j * dy
+    coor[:nk + 1, :nj + 1, :ni + 1, 1] = j * dy
+    coor[:nk + 1, :nj + 1, :ni + 1, 2] = k * dz
+    return synth.Grid(ni, nj, nk, coor, np.zeros((mz, my, mx)), 0, 0, 0)
+
+
+def _expected(dx, dy, dz, s, t):
+    rx = np.array([dx, 0.0, 0.0])
+    ry = np.array([t * dy, dy, 0.0])
+    rz = np.array([s * dz, 0.0, dz])
+    csi, eta, zet = np.cross(ry, rz), np.cross(rz, rx), np.cross(rx, ry)
+    aj = 1.0 / np.dot(rx, np.cross(ry, rz))
+    return csi, eta, zet, aj
+
+
+def _check_pack(M, d, geom):
+    csi, eta, zet, aj = _expected(*geom[3:])
+    inner = (slice(1, -1), slice(1, -1), slice(1, -1))
+    want = dict(csi=csi, eta=eta, zet=zet, icsi=csi, ieta=eta, izet=zet, jcsi=csi, jeta=eta, jzet=zet,
+                kcsi=csi, keta=eta, kzet=zet)
+    for name, v in want.items():
+        a = O.metric(M, d, name)[inner]
+        assert np.allclose(a, v, rtol=0, atol=1e-13 * np.abs(v).max()), (name, np.abs(a - v).max())
+    for name in ("aj", "iaj", "jaj", "kaj"):
+        a = O.metric(M, d, name)[inner]
+        assert np.allclose(a, aj, rtol=1e-13, atol=0), (name, np.abs(a - aj).max())
+
+
+@pytest.mark.parametrize("geom", GEOMS)
+def test_oracle_affine_metrics(geom):
+    g = _grid(*geom)
+    d = O.dims_of(g)
+    _check_pack(O.form_metrics(d, g.coor), d, geom)
+
+
+@pytest.mark.parametrize("geom", GEOMS)
+def test_oracle_uniform_velocity(geom):
+    g = _grid(*geom)
+    d = O.dims_of(g)
+    M = O.form_metrics(d, g.coor)
+    V = np.array([0.7, -0.4, 0.25])
+    u = np.zeros(g.nvert.shape + (3,))
+    u[..., 0] = O.metric(M, d, "icsi") @ V
+    u[..., 1] = O.metric(M, d, "jeta") @ V
+    u[..., 2] = O.metric(M, d, "kzet") @ V
+    ucat = O.contra2cart(d, M, g.nvert, u)
+    inner = (slice(1, -1), slice(1, -1), slice(1, -1))
+    assert np.allclose(ucat[inner], V, rtol=0, atol=1e-13)
+    assert O.divergence(d, u, O.metric(M, d, "aj"), g.nvert) <= 1e-12
+    b, _ = O.rhs(d, u, g.nvert, 0.04, 1.0, 1.0, False)
+    assert np.abs(b).max() <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("geom", GEOMS)
+def test_cuda_affine_metrics(gpu_ctx, geom):
+    g = _grid(*geom)
+    d = O.dims_of(g)
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, 1, 0, periodic=(0, 0, 0))
+    try:
+        _check_pack(gpu_ctx.metrics(gid, 0), d, geom)
+    finally:
+        gpu_ctx.grid_destroy(gid)
