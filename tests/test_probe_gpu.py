@@ -83,3 +83,37 @@ def test_probe_smooth_counts_real_sweeps(gpu_ctx):
         assert all(r[0] == "k_smooth (run)" for r in runs)
     finally:
         gpu_ctx.grid_destroy(gid)
+
+
+def test_probe_open_across_a_batch(gpu_ctx):
+    """A probe open during a batched call skips the launches captured into
+    the batch graph (their events would become graph nodes) and times the
+    rest; the batch's results are those of an unprobed batch."""
+    cases = [synth.c2_sphere(scale=8), synth.c1_channel(scale=4)]
+    ids = []
+    try:
+        for c in cases:
+            gid = gpu_ctx.grid_create(c.grid.coor, c.grid.nvert, c.levels, c.immersed)
+            gpu_ctx.poisson_lhs(gid)
+            ids.append(gid)
+        params = capi.default_params(rtol=1e-9, div_tol=1e-8)
+        out = []
+        for probe in (False, True):
+            for gid, c in zip(ids, cases):
+                gpu_ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
+                gpu_ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
+            if probe:
+                gpu_ctx.probe_begin(capi.PROBE_ALL)
+            infos, dm = gpu_ctx.projection_step_batch(ids, params)
+            if probe:
+                n, ms, by = gpu_ctx.probe_end()
+                recs = gpu_ctx.probe_records(n)
+                assert all(np.isfinite(r[2]) and r[2] >= 0 for r in recs)
+            out.append(([i["iterations"] for i in infos], dm.copy(),
+                        [gpu_ctx.get_field(gid, capi.FIELD_UCONT, c.ucont.shape) for gid, c in zip(ids, cases)]))
+        (it0, dm0, u0), (it1, dm1, u1) = out
+        assert it0 == it1 and np.array_equal(dm0, dm1)
+        assert all(np.array_equal(a, b) for a, b in zip(u0, u1))
+    finally:
+        for gid in ids:
+            gpu_ctx.grid_destroy(gid)

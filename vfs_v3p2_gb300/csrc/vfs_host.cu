@@ -51,7 +51,13 @@ struct Probe {
   double bytes = 0.;
   unsigned long long launches = 0;
   std::vector<ProbeRec> recs;
-  bool wants(int k) const { return kind != 0 && (kind == k || kind == VFS_PROBE_ALL); }
+  // a probe kind k is open; launches issued into a capturing stream (a batch
+  // graph) are not probed: their events would become graph nodes
+  bool wants(int k, cudaStream_t s) const {
+    if (kind == 0 || (kind != k && kind != VFS_PROBE_ALL)) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
+  }
   bool begin(cudaStream_t s) {
     if (used + 2 > (int)ev.size()) return false;
     cudaEventRecord(ev[used], s);
@@ -75,7 +81,7 @@ struct Probed {
   int level;
   double bytes;
   Probed(int k, cudaStream_t s_, const char* n, int l, double b) : s(s_), name(n), level(l), bytes(b) {
-    on = g_probe.wants(k) && g_probe.begin(s);
+    on = g_probe.wants(k, s) && g_probe.begin(s);
   }
   ~Probed() {
     if (on) g_probe.end(s, bytes, name, level);
@@ -456,7 +462,7 @@ struct SweepRun {
     if (!probe) return;
     if (!on) {
       s = s_;
-      on = g_probe.begin(s);
+      on = g_probe.wants(VFS_PROBE_SMOOTH, s) && g_probe.begin(s);
     }
     if (on) {
       n++;
