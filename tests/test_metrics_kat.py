@@ -109,6 +109,25 @@ def test_oracle_projection_of_a_linear_potential(geom):
             assert np.abs(got[sl] - want[sl]).max() <= 1e-12 * np.abs(want).max(), name
 
 
+@pytest.mark.parametrize("geom", GEOMS)
+def test_oracle_operator_annihilates_linear_potentials(geom):
+    """The assembled 19-point operator (PoissonLHSNew, poisson.c:1146-1630)
+    is consistent: on an affine grid it maps a linear potential to zero on
+    every cell whose stencil stays in the interior (the face fluxes of a
+    uniform gradient cancel, cross terms included), and constants to zero
+    everywhere.  The CUDA coefficients equal these bit for bit
+    (tests/test_parity_gpu.py)."""
+    g = _grid(*geom)
+    d = O.dims_of(g)
+    M = O.form_metrics(d, g.coor)
+    coef = O.lhs(d, O.gtensor(d, M), g.nvert)
+    phi = O.metric(M, d, "cent") @ np.array([0.3, -0.7, 0.45])
+    y = O.matvec(d, coef, phi)
+    scale = np.abs(coef).max() * np.abs(phi).max()
+    assert np.abs(y[2:-2, 2:-2, 2:-2]).max() <= 1e-14 * scale
+    assert np.abs(O.matvec(d, coef, np.ones_like(phi))[1:-1, 1:-1, 1:-1]).max() <= 1e-14 * np.abs(coef).max()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("geom", GEOMS)
 def test_cuda_affine_metrics(gpu_ctx, geom):
