@@ -1,4 +1,5 @@
-"""Known answers of the metrics on affine grids (FormMetrics, metrics.c:4-1290).
+"""Known answers on affine grids and linear fields: the metrics (FormMetrics,
+metrics.c:4-1290), the operator, the projection and the transfer operators.
 
 On a grid with node r(i, j, k) = (i dx + s k dz + t j dy, j dy, k dz) every
 metric is constant: the area vectors are the cross products of the two
@@ -126,6 +127,39 @@ def test_oracle_operator_annihilates_linear_potentials(geom):
     scale = np.abs(coef).max() * np.abs(phi).max()
     assert np.abs(y[2:-2, 2:-2, 2:-2]).max() <= 1e-14 * scale
     assert np.abs(O.matvec(d, coef, np.ones_like(phi))[1:-1, 1:-1, 1:-1]).max() <= 1e-14 * np.abs(coef).max()
+
+
+def test_oracle_transfers_of_linear_fields():
+    """MyInterpolation (poisson.c:526-669) is cell-centred trilinear with
+    weights (27, 9, 9, 3, 9, 3, 3, 1) / 64: a field linear in the cell index
+    comes back exactly away from the clamped edges.  MyRestriction
+    (poisson.c:364-471) averages the 8 children: a linear fine field gives
+    its value at the coarse cell centre.  The CUDA transfers match these
+    within 1e-14 (tests/test_parity_gpu.py)."""
+    case = synth.channel_case(16, 16, 16, seed=5, levels=2)
+    g = case.grid
+    d = O.dims_of(g)
+    mg = O.MG(d, g.coor, g.nvert, 2)
+    try:
+        dc = mg.level_dims(0)
+        c = np.array([1.0, 2.0, -0.5])  # coefficients of i, j, k
+
+        def lin(shape, off, scale):
+            k, j, i = np.meshgrid(*(np.arange(n) for n in shape), indexing="ij")
+            return c[0] * (i + off) * scale + c[1] * (j + off) * scale + c[2] * (k + off) * scale
+
+        xc = lin((dc.mz, dc.my, dc.mx), 0.0, 1.0)        # coarse cell index
+        fine_in_coarse = lin((d.mz, d.my, d.mx), 0.5, 0.5)  # fine cell i sits at coarse (i + 0.5) / 2
+        yf = mg.prolong(1, xc)
+        inner = (slice(2, -2), slice(2, -2), slice(2, -2))
+        assert np.abs(yf[inner] - fine_in_coarse[inner]).max() <= 1e-13 * np.abs(yf[inner]).max()
+        xf = lin((d.mz, d.my, d.mx), 0.0, 1.0)
+        yc = mg.restrict(1, xf)
+        coarse_centre = lin((dc.mz, dc.my, dc.mx), -0.25, 2.0)  # children 2ic-1, 2ic: mean index 2ic - 0.5
+        cin = (slice(1, -1), slice(1, -1), slice(1, -1))
+        assert np.abs(yc[cin] - coarse_centre[cin]).max() <= 1e-13 * np.abs(yc[cin]).max()
+    finally:
+        mg.close()
 
 
 @pytest.mark.gpu
