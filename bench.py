@@ -216,6 +216,11 @@ def cpu_baseline(case, args, steps=2):
     return steps / dt, O.lib().orc_num_threads(), r
 
 
+# the headline metric, identical on every line of both arms (the workload and
+# what a line measures are in its config)
+METRIC = "Pressure solves/s, HBM GB/s, p50/p99 latency: mixed vs FP64 at \u2016div u\u2016<1e-8"
+
+
 def run_reference(args):
     dist, rank, local, ws = dist_init()
     if rank != 0:
@@ -232,10 +237,12 @@ def run_reference(args):
         rates = [cpu_baseline(c, args, steps=1)[0] for c in sample]
         val = float(len(rates) / sum(1.0 / r for r in rates))
         cores = os.cpu_count()
-        line = {"metric": "pressure projection steps/s (solves/s)", "value": val, "unit": "solves/s",
+        line = {"metric": METRIC, "value": val, "unit": "solves/s",
                 "impl": "reference", "n_gpus": args.gpus, "steps": len(sample), "warmup": 1,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded)", "config": {"workload": WORKLOAD[args.config]},
+                "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD[args.config], "rtol": args.rtol, "div_tol": args.div_tol,
+                           "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG)"},
                 "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
                                  "sample": "two median-size grids of the workload, one step each after a warm-up"},
                 "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -245,10 +252,13 @@ def run_reference(args):
     case = make_case(args)
     val, cores, r = cpu_baseline(case, args, steps=max(1, min(args.steps, 3)))
     line = {
-        "metric": "pressure projection steps/s (solves/s)", "value": val, "unit": "solves/s", "impl": "reference",
+        "metric": METRIC, "value": val, "unit": "solves/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": max(1, min(args.steps, 3)), "warmup": 1, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD[args.config], "grid": case.name, "rtol": args.rtol, "mg_levels": case.levels},
+        "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(case.grid.ni * case.grid.nj *
+                                                                                   case.grid.nk),
+                   "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol,
+                   "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG)"},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": f"{WORKLOAD[args.config]}: full-size steps timed after 1 warm-up"},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -325,11 +335,12 @@ def main_batch(args, dist, rank, local, ws):
         fp64 = {"batched": {"value": r_b, "iterations_mean": float(np.mean(its64)), "divmax": max(dm64)},
                 "one_grid_at_a_time": {"value": r_1, "divmax": max(dm1)},
                 "mixed_batched_over_fp64_batched": value / r_b, "mixed_batched_over_fp64_one_at_a_time": value / r_1}
-    line = {"metric": "batched pressure projection steps/s (64 uneven grids, one graph launch per FGMRES iteration), "
-                      "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+    line = {"metric": METRIC,
             "value": value, "unit": "solves/s", "steps": args.steps,
             "ms_per_step": 1e3 * total / args.steps, **base_line(args, ws),
             "config": {"workload": WORKLOAD["batch"], "grids": len(ids), "cells_total": int(cells),
+                       "measures": "batched pressure projection steps/s (64 uneven grids, one graph launch per "
+                                   "FGMRES iteration), mixed FP32-MG/FP64-FGMRES",
                        "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": not args.no_tune,
                        "mg_operator": OPERATOR[base.mg_half],
                        "timer": "host wall clock around synchronous batch calls (results on the host)",
@@ -399,11 +410,12 @@ def main_serve(args, dist, rank, local, ws):
                                           "mixed_over_fp64": cap["solves_per_s"] / cap64["solves_per_s"],
                                           "divmax": {"mixed": cap["divmax"], "fp64": cap64["divmax"]},
                                           "requests": len(burst)}}
-    line = {"metric": "served pressure projection steps/s with p50/p99 latency (Poisson arrivals, continuous batching), "
-                      "mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+    line = {"metric": METRIC,
             "value": ws * summ["solves_per_s"], "unit": "solves/s", "steps": len(recs),
             "ms_per_step": 1e3 * wall / len(recs), **base_line(args, ws),
             "config": {"workload": WORKLOAD["serve"], "streams": 16, "rate_req_s": args.rate,
+                       "measures": "served pressure projection steps/s with p50/p99 latency (Poisson arrivals, "
+                                   "continuous batching), mixed FP32-MG/FP64-FGMRES",
                        "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16,
                        "mg_operator": OPERATOR[params.mg_half], "rtol": args.rtol,
                        "div_tol": args.div_tol, "autotuned": not args.no_tune,
@@ -600,11 +612,12 @@ def main():
     if rank == 0:
         its = [i["iterations"] for i in infos]
         line = {
-            "metric": "pressure projection steps/s (solves/s), mixed FP32-MG/FP64-FGMRES at max|div u| < 1e-8",
+            "metric": METRIC,
             "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": tmax / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-mg/f64-krylov", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(g.ni * g.nj * g.nk),
+                       "measures": "pressure projection steps/s with U* resident, mixed FP32-MG/FP64-FGMRES",
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
                        "restart": args.restart, "orth": args.orth, **smoother_config(args),
                        "mg_operator": OPERATOR[args.mg_half],
