@@ -129,6 +129,37 @@ def test_oracle_operator_annihilates_linear_potentials(geom):
     assert np.abs(O.matvec(d, coef, np.ones_like(phi))[1:-1, 1:-1, 1:-1]).max() <= 1e-14 * np.abs(coef).max()
 
 
+@pytest.mark.parametrize("geom", GEOMS)
+def test_oracle_rhs_of_a_uniform_expansion(geom):
+    """PoissonRHS2_hypre (poisson_hypre.c:342-429): val = -(U_i - U_i-1 + ...)
+    then val *= -1 / dt * st * coeff, so b = +(net outward face flux) / dt *
+    st * coeff (the opposite sign to PoissonRHS in poisson.c, paired with an
+    operator of the matching sign).  For v = (a x, 0, 0) the i-face fluxes
+    are a x_face times the face area vector's x part, so on an affine grid
+    every cell's net flux is a times its volume and aj b = a st coeff / dt in
+    every interior cell.  The CUDA right-hand side matches this oracle
+    (tests/test_parity_gpu.py)."""
+    g = _grid(*geom)
+    d = O.dims_of(g)
+    M = O.form_metrics(d, g.coor)
+    a = 0.8
+    u = np.zeros(g.nvert.shape + (3,))
+    # the i-face of cell (i, j, k) lies on node column i with corners at
+    # nodes j-1, j and k-1, k (cell j spans nodes j-1..j); only x matters
+    c = g.coor
+    mz, my, mx = g.nvert.shape
+    xf = 0.25 * (c[0:mz - 2, 0:my - 2, :, 0] + c[1:mz - 1, 0:my - 2, :, 0] + c[0:mz - 2, 1:my - 1, :, 0] +
+                 c[1:mz - 1, 1:my - 1, :, 0])
+    icsi = O.metric(M, d, "icsi")
+    u[1:mz - 1, 1:my - 1, :, 0] = a * xf * icsi[1:mz - 1, 1:my - 1, :, 0]
+    for dt, st, coeff in ((0.04, 1.0, 1.0), (0.02, 1.5, 1.5)):
+        b, _ = O.rhs(d, u, g.nvert, dt, st, coeff, False)
+        aj = O.metric(M, d, "aj")
+        inner = (slice(1, -1), slice(1, -1), slice(1, -1))
+        want = a * st * coeff / dt
+        assert np.allclose((aj * b)[inner], want, rtol=1e-12, atol=0)
+
+
 def test_oracle_transfers_of_linear_fields():
     """MyInterpolation (poisson.c:526-669) is cell-centred trilinear with
     weights (27, 9, 9, 3, 9, 3, 3, 1) / 64: a field linear in the cell index
