@@ -127,11 +127,15 @@ typedef struct {
  * divided by dt st / coeff, so the solve stops when ||r_s|| <= rtol ||aj b||
  * and, when div_tol > 0, the masked max of dt st / coeff * |r_s| (the
  * divergence the projection will leave) is at most div_tol.  A projection
- * step then measures max |div u|; if the rounding of the flux update left it
- * above div_tol, one more projection pass on the corrected fluxes removes the
- * rest (at most two).  Where FP64 rounding keeps the masked max above the
- * target (very small cells, large aj) the solve stops once another round no
- * longer halves it and sets info.div_limited. */
+ * step then measures max |div u|.  Where FP64 rounding keeps the masked max
+ * above the target (large |phi| on strongly stretched grids: the solve rounds
+ * stop once another round no longer halves it), or the rounding of the flux
+ * update left it above div_tol, one more projection pass on the corrected
+ * fluxes removes the rest (at most two; each solves for the small remaining
+ * phi, whose rounding floor is far lower).  The aj-scaled operator drops
+ * entries after scaling (|aj v| <= 1e-10, the multigrid path's form,
+ * poisson.c:1560, 1607-1616), so it is consistent with the projection even
+ * where aj is large. */
 
 typedef struct {
   int iterations;  /* preconditioner applications */
@@ -139,9 +143,10 @@ typedef struct {
   double relres;   /* true ||aj (b - A phi)|| / ||aj b|| at exit */
   double bnorm;
   double time_ms;  /* device time of the solve */
-  int div_limited; /* 1: div_tol was not reachable (the masked residual max stopped
-                      falling: FP64 rounding floor of the grid) and the solve
-                      stopped at the rtol criterion */
+  int div_limited; /* 1: div_tol was not reached: after a projection step, the
+                      measured max |div u| is above div_tol after every
+                      projection pass; for a solve alone, the masked residual
+                      max stopped falling (the FP64 rounding floor of phi) */
   int mg_half_used; /* 1: the multigrid ran on the FP16 normalised operator
                        (mixed precision, mg_half = 1, and every normalised
                        coefficient of the grid within 6e4; else FP32) */

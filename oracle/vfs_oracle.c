@@ -393,10 +393,17 @@ int orc_gid(const orc_dims* d, const double* nvert, int* gid) {
 /* rule of poisson.c:1607-1616 (|v| <= 1e-10 or a column without a fluid id   */
 /* is dropped, the diagonal is always kept).  Non-fluid rows are all zero.    */
 /* The additions happen in the reference's order, so entries are bit-equal    */
-/* to the values handed to HYPRE_IJMatrixSetValues.  levelset (r != 1) and    */
-/* poisson == -1 (aj scaling) are not restated.                               */
+/* to the values handed to HYPRE_IJMatrixSetValues.  levelset (r != 1) is not */
+/* restated.  orc_lhs_scaled is the multigrid path's form (poisson == -1):    */
+/* every entry of the row is multiplied by aj first (poisson.c:1560) and the  */
+/* drop rule then applies to the scaled values.                               */
 /* ------------------------------------------------------------------------- */
-void orc_lhs(const orc_dims* d, const double* g, const double* nvert, double* coef) {
+static void lhs_rows(const orc_dims* d, const double* g, const double* nvert, const double* aj, double* coef);
+void orc_lhs(const orc_dims* d, const double* g, const double* nvert, double* coef) { lhs_rows(d, g, nvert, NULL, coef); }
+void orc_lhs_scaled(const orc_dims* d, const double* g, const double* nvert, const double* aj, double* coef) {
+  lhs_rows(d, g, nvert, aj, coef);
+}
+static void lhs_rows(const orc_dims* d, const double* g, const double* nvert, const double* aj, double* coef) {
   const int mx = d->mx, my = d->my, mz = d->mz;
   const int ip = d->ip, jp = d->jp, kp = d->kp;
   const size_t N = (size_t)mx * my * mz;
@@ -615,6 +622,8 @@ void orc_lhs(const orc_dims* d, const double* g, const double* nvert, double* co
           vol[CP] -= g33[b] / r;
           vol[BP] += g33[b] / r;
         }
+        if (aj)  /* poisson == -1, poisson.c:1560 */
+          for (int m = 0; m < 19; m++) vol[m] *= aj[c];
         /* drop rule, poisson.c:1607-1616 */
         for (int m = 0; m < 19; m++) {
           int ni = wrapi(i + SDI[m], mx, ip), nj = wrapi(j + SDJ[m], my, jp), nk = wrapi(k + SDK[m], mz, kp);
@@ -1340,9 +1349,7 @@ static void level_setup(orc_level* L) {
   orc_form_metrics(&L->d, L->coor, L->M);
   orc_gtensor(&L->d, L->M, L->g);
   orc_lhs(&L->d, L->g, L->nvert, L->coef);
-  const double* aj = L->M + N * M_AJ;
-  for (int m = 0; m < NSTENCIL; m++)
-    for (size_t c = 0; c < N; c++) L->mcoef[(size_t)m * N + c] = L->coef[(size_t)m * N + c] * aj[c];
+  orc_lhs_scaled(&L->d, L->g, L->nvert, L->M + N * M_AJ, L->mcoef);
   line_factors(L);
 }
 

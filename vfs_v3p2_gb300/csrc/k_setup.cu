@@ -506,21 +506,29 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
         vol[BP] += g33[b] / r;
       }
 #undef NV
-      // drop rule, poisson.c:1607-1616
+      // drop rule, poisson.c:1607-1616: the unscaled row (the built HYPRE
+      // path) drops |v| <= 1e-10; the aj-scaled row (the multigrid path,
+      // poisson == -1) is scaled first (poisson.c:1560) and the same rule
+      // applies to the scaled values
+      const double a = aj[_t];
 #pragma unroll
       for (int m = 0; m < 19; m++) {
-        bool keep = (m == CP) || (fabs(vol[m]) > 1.e-10 && has_id(d, nvert, i + slot_di(m), j + slot_dj(m), k + slot_dk(m)));
-        if (!keep) vol[m] = 0.;
+        const bool col = (m == CP) || has_id(d, nvert, i + slot_di(m), j + slot_dj(m), k + slot_dk(m));
+        const double s = vol[m] * a;
+        const bool keep_u = (m == CP) || (fabs(vol[m]) > 1.e-10 && col);
+        const bool keep_s = (m == CP) || (fabs(s) > 1.e-10 && col);
+        coef[(size_t)m * N + _t] = keep_u ? vol[m] : 0.;
+        mcoef[(size_t)m * N + _t] = keep_s ? s : 0.;
+        mcoef32[(size_t)m * N + _t] = keep_s ? (float)s : 0.f;
+        if ((keep_u && vol[m] != 0.) || (keep_s && s != 0.)) mymask |= 1u << m;
       }
+      continue;
     }
-    const double a = aj[_t];
 #pragma unroll
     for (int m = 0; m < 19; m++) {
-      coef[(size_t)m * N + _t] = vol[m];
-      double s = vol[m] * a;
-      mcoef[(size_t)m * N + _t] = s;
-      mcoef32[(size_t)m * N + _t] = (float)s;
-      if (vol[m] != 0.) mymask |= 1u << m;
+      coef[(size_t)m * N + _t] = 0.;
+      mcoef[(size_t)m * N + _t] = 0.;
+      mcoef32[(size_t)m * N + _t] = 0.f;
     }
   }
   atomicOr(mask, mymask);
