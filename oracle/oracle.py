@@ -2,7 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline / reference arm of bench.py, never by the product package.
-Parity unpinned: see the header of vfs_oracle.c.
+Pinned to the reference's own code (oracle/ref.mk, tests/test_ref_oracle.py): see
+the header of vfs_oracle.c.
 """
 from __future__ import annotations
 

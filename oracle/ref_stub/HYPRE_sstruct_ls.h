@@ -1,0 +1,2 @@
+/* Single-rank stand-in: see vfs_ref_stub.h. */
+#include "vfs_ref_stub.h"

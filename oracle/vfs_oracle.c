@@ -6,15 +6,22 @@
  * cpu_baseline / reference arm of bench.py may load it.  The product path
  * never links or calls it.
  *
- * PARITY UNPINNED.  The reference (trunglendsu/VFS_v3p2) cannot be compiled
- * here: its hot path includes PETSc 3.2-p7, HYPRE and MPI headers and links
- * those libraries (variables.h:4-18, makefile:1-53), none of which exist in
- * this image, and the reference ships no tests, fixtures or golden vectors
- * (.MISSING_LARGE_BLOBS lists the stripped data).  This restatement is
- * therefore pinned only by project-written known-answer tests derived from
- * the discretisation (uniform-grid eigenvalues, operator/projection
- * consistency, constant null space, symmetry without skew), which live in
- * tests/test_oracle.py.
+ * PINNED TO THE REFERENCE'S OWN CODE.  The reference cannot be built as a
+ * program here (its hot path links PETSc 3.2-p7, HYPRE and MPI, none of
+ * which exist in this image: variables.h:4-18, makefile:1-53), and it ships
+ * no tests or golden data.  Its path functions are compiled unmodified from
+ * their sources instead, against single-rank stand-ins of the library calls
+ * they make (oracle/ref.mk, oracle/ref_stub/, oracle/ref_harness.cpp), and
+ * tests/test_ref_oracle.py checks this restatement against them bit for bit:
+ * FormMetrics, setup_lidx2 + PoissonLHSNew (every matrix entry),
+ * VolumeFlux, PoissonRHS2_hypre / PoissonRHS2, Convert_Phi2_Phi,
+ * UpdatePressure, Projection + Contra2Cart, Divergence, MyNvertRestriction,
+ * MyRestriction and MyInterpolation (with semi-coarsening).  The committed
+ * fixtures tests/golden/golden_small.npz hold the reference's outputs, so
+ * the same check runs where its sources are absent.  The solve itself is
+ * HYPRE's (absent): the converged solution of the same assembled system is
+ * what is compared.  Known-answer tests derived from the discretisation
+ * (tests/test_oracle.py) cover it besides.
  *
  * Array conventions follow the reference's PETSc DMDA arrays exactly:
  *   - extents mx = ni+2, my = nj+2, mz = nk+2 (one ghost/boundary cell per
@@ -219,16 +226,12 @@ void orc_form_metrics(const orc_dims* d, const double* coor, double* M) {
       a = ID(d, i, j, mz - 1); b = ID(d, i, j, mz - 2);
       st3(csi, a, ld3(csi, b)); st3(eta, a, ld3(eta, b)); st3(zet, a, ld3(zet, b)); aj[a] = aj[b];
     }
-  /* periodic ghost copies, metrics.c:470-510 (sources are never ghosts) */
-  for (int k = 0; k < mz; k++)
-    for (int j = 0; j < my; j++)
-      for (int i = 0; i < mx; i++) {
-        int a = wrapi(i, mx, d->ip), b = wrapi(j, my, d->jp), c = wrapi(k, mz, d->kp);
-        if (a != i || b != j || c != k) {
-          size_t t = ID(d, i, j, k), s = ID(d, a, b, c);
-          st3(csi, t, ld3(csi, s)); st3(eta, t, ld3(eta, s)); st3(zet, t, ld3(zet, s)); aj[t] = aj[s];
-        }
-      }
+  /* The periodic ghost copies of metrics.c:470-510 act on the local vectors
+   * only, and their one reader (the face-metric fallbacks at metrics.c:713-720,
+   * 835-842, 993-1000) is commented out; the final scatter of the global
+   * vectors (metrics.c:1212-1244) then restores the mirror values on every
+   * boundary plane (a periodic axis has one rank, init.c:144-146, so its ghost
+   * planes are owned points).  The mirror copies above are therefore final. */
   /* i-face metrics from x-face centres, metrics.c:592-723 */
   double* cx = tmp; /* reuse: face centres */
   memset(tmp, 0, sizeof(double) * N * 9);
@@ -673,7 +676,10 @@ int orc_csr(const orc_dims* d, const double* coef, const double* nvert, int* row
         if (gid[c] < 0) continue;
         for (int m = 0; m < 19; m++) {
           double a = coef[(size_t)m * N + c];
-          if (a != 0. || m == CP) {
+          /* the reference writes a row only for the cells it assembles
+           * (nvert <= 0.1): a numbered cell with 0.1 < nvert < 1 keeps an
+           * empty row (poisson.c:1160-1163) */
+          if (a != 0. || (m == CP && !(nvert[c] > THR))) {
             col[nnz] = gid[ID(d, i + SDI[m], j + SDJ[m], k + SDK[m])];
             val[nnz] = a;
             if (col[nnz] < 0) continue;

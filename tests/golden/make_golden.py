@@ -1,12 +1,23 @@
-"""Generates tests/golden/golden_small.npz: outputs of the CPU oracle (the
-restatement of the reference's pressure path) for two small seeded cases.
-The reference itself cannot be built here (PETSc/HYPRE/MPI absent), so these
-fixtures anchor the oracle against drift and give the CUDA path fixed
-targets.  Inputs are not stored: they are regenerated from the seeded
-synthetic generators, and a checksum of them is stored to detect generator
-drift.
+"""Generates tests/golden/golden_small.npz from the reference's own code: the
+pressure-path functions compiled unmodified from the reference's sources
+(oracle/ref.mk, run through oracle/ref.py and tests/refstep.py) on small
+seeded grids.  Stored per case:
 
-    python tests/golden/make_golden.py
+* M: FormMetrics' 17 fields (metrics.c:4-1290) in the oracle's 43-array pack;
+* lhs_rows, lhs_cols, lhs_vals, gid: every entry PoissonLHSNew hands to
+  HYPRE (poisson.c:976-1691) in its compact fluid numbering (setup_lidx2);
+* b: PoissonRHS2 of the balanced fluxes (poisson.c:1789-1915);
+* phi, p, ucont, divmax: the step through the reference's Remove_Nullspace,
+  Convert_Phi2_Phi, UpdatePressure, Projection and Divergence around a direct
+  solve of its matrix (HYPRE itself is not part of the sources).
+
+Inputs are not stored: they are regenerated from the seeded synthetic
+generators, and a digest of them is stored to detect generator drift.  The
+fixtures let the oracle (tests/test_golden_cpu.py) and the CUDA path
+(tests/test_golden_gpu.py) be checked against the reference where its
+sources are absent.
+
+    python tests/golden/make_golden.py     (needs the reference's sources)
 """
 import hashlib
 import math
@@ -19,6 +30,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.dirname(HERE))
 
 
 def cases():
@@ -27,6 +39,7 @@ def cases():
         "channel_12x8x8": synth.channel_case(12, 8, 8, seed=2101, levels=2),
         "sphere_16x8x8": synth.channel_case(16, 8, 8, seed=2102, spheres=[(math.pi, 0.0, math.pi / 2, 0.7)],
                                             sigma=0.5, levels=2),
+        "terrain_16x8x8": synth.c3_terrain(scale=32),
     }
 
 
@@ -37,23 +50,18 @@ def input_digest(case) -> str:
     return h.hexdigest()
 
 
-def outputs(case):
-    import oracle as O
-    g = case.grid
-    d = O.dims_of(g)
-    M = O.form_metrics(d, g.coor)
-    G = O.gtensor(d, M)
-    coef = O.lhs(d, G, g.nvert)
-    r = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, orth=1)
-    return {"aj": O.metric(M, d, "aj"), "coef": coef, "b": r["b"], "phi": r["phi"], "p": r["p"],
-            "ucont": r["ucont"], "divmax": np.array(r["divmax"])}
+def reference_outputs(case):
+    import refstep
+    r = refstep.reference_step(case)
+    return {"M": r["M"], "lhs_rows": r["rows"], "lhs_cols": r["cols"], "lhs_vals": r["vals"], "gid": r["gid"],
+            "b": r["b"], "phi": r["phi"], "p": r["p"], "ucont": r["ucont"], "divmax": np.array(r["divmax"])}
 
 
 def main():
     out = {}
     for name, c in cases().items():
         out[f"{name}/digest"] = np.array(input_digest(c))
-        for k, v in outputs(c).items():
+        for k, v in reference_outputs(c).items():
             out[f"{name}/{k}"] = v
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)
 

@@ -1,14 +1,17 @@
-"""The CUDA path (through the C ABI) against the committed golden fixtures:
-operator coefficients bit for bit, and the full projection step (FP64 and
-mixed) to the solution criterion of the pressure path: relative L2 of phi
-<= 1e-8 after removing the fluid mean, p and U within 1e-8, and
-max |div u| < 1e-8."""
+"""The CUDA path (through the C ABI) against the committed golden fixtures,
+which tests/golden/make_golden.py generated from the reference's own code:
+the finest level's metrics and the operator's entries bit for bit (the
+coefficients exported in the reference's compact fluid numbering), and the
+full projection step (FP64 and mixed) to the solution criterion of the
+pressure path: relative L2 of phi <= 1e-8 after removing the fluid mean, p
+and U within 1e-8, and max |div u| < 1e-8."""
 import os
 import sys
 
 import numpy as np
 import pytest
 
+import oracle as O
 from vfs_v3p2_gb300 import capi
 
 pytestmark = pytest.mark.gpu
@@ -23,13 +26,22 @@ CASES = MG.cases()
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_cuda_path_matches_golden(gpu_ctx, name, precision):
+def test_cuda_path_matches_reference_golden(gpu_ctx, name, precision):
     case = CASES[name]
     g = case.grid
+    d = O.dims_of(g)
     gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
     try:
         gpu_ctx.poisson_lhs(gid)
-        assert np.array_equal(gpu_ctx.coef(gid, case.levels - 1, 0), GOLD[f"{name}/coef"])
+        L = case.levels - 1
+        assert np.array_equal(gpu_ctx.metrics(gid, L), GOLD[f"{name}/M"])
+        coef = gpu_ctx.coef(gid, L, 0).reshape((19,) + g.nvert.shape)
+        A, _ = O.csr(d, coef, g.nvert)  # the oracle's CSR export, as test infrastructure
+        Ac = A.tocoo()
+        order = np.lexsort((Ac.col, Ac.row))
+        assert np.array_equal(Ac.row[order], GOLD[f"{name}/lhs_rows"])
+        assert np.array_equal(Ac.col[order], GOLD[f"{name}/lhs_cols"])
+        assert np.array_equal(Ac.data[order], GOLD[f"{name}/lhs_vals"])
         u = np.ascontiguousarray(case.ucont.copy())
         p = np.zeros(g.nvert.shape)
         params = capi.default_params(precision=precision, rtol=1e-12, div_tol=1e-8)

@@ -149,21 +149,11 @@ __global__ void k_metrics_mirror(Dims d, double* M, int axis) {
   }
 }
 
-// Periodic ghost copies of the cell-centred metrics, metrics.c:470-510.
-__global__ void k_metrics_periodic(Dims d, double* M) {
-  const size_t N = ncell(d);
-  double *csi = M + N * MP_CSI, *eta = M + N * MP_ETA, *zet = M + N * MP_ZET, *aj = M + N * MP_AJ;
-  GRID_LOOP(d) {
-    DECOMP(d, i, j, k);
-    int a = wrapi(i, d.mx, d.ip), b = wrapi(j, d.my, d.jp), c = wrapi(k, d.mz, d.kp);
-    if (a == i && b == j && c == k) continue;
-    size_t s = cidx(d, a, b, c);
-    st3(csi, _t, ld3(csi, s));
-    st3(eta, _t, ld3(eta, s));
-    st3(zet, _t, ld3(zet, s));
-    aj[_t] = aj[s];
-  }
-}
+// The mirror copies are the final ghost values of the cell-centred metrics:
+// the reference's periodic copies (metrics.c:470-510) go to its local vectors
+// only, nothing reads them there (the face-metric fallbacks that would are
+// commented out), and its closing scatter of the global vectors
+// (metrics.c:1212-1244) restores the mirror values on every boundary plane.
 
 __device__ __forceinline__ void face_metric(double dxdc, double dydc, double dzdc, double dxde, double dyde, double dzde,
                                             double dxdz, double dydz, double dzdz, double* M, size_t N, size_t t,
@@ -737,7 +727,6 @@ int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tm
   k_metrics_cells<<<nblk(N), 256, 0, s>>>(d, coor, M, tmp); ++g_launches;
   k_metrics_centred<<<nblk(N), 256, 0, s>>>(d, coor, M, tmp); ++g_launches;
   for (int a = 0; a < 3; a++) k_metrics_mirror<<<nblk(N), 256, 0, s>>>(d, M, a); ++g_launches;
-  k_metrics_periodic<<<nblk(N), 256, 0, s>>>(d, M); ++g_launches;
   k_metrics_faces<<<nblk(N), 256, 0, s>>>(d, coor, M); ++g_launches;
   return (int)cudaGetLastError();
 }
