@@ -68,14 +68,17 @@ def parse():
     ap.add_argument("--cheb-ratio", type=float, default=6.0)
     ap.add_argument("--omega", type=float, default=0.9, help="y-line Jacobi damping (--smoother jacobi)")
     ap.add_argument("--smooth-cols", type=int, default=0, help="smoother tile columns (0: automatic)")
-    ap.add_argument("--mg-half", type=int, default=0, choices=[0, 1],
-                    help="multigrid stencil coefficients stored in FP32 (0, the specified form) or as FP16 "
-                         "normalised by their diagonal (1); FP32 arithmetic either way")
+    ap.add_argument("--mg-half", type=int, default=0, choices=[0, 1, 2],
+                    help="multigrid operator storage: FP32 face form on 11-slot levels (0), FP16 normalised by "
+                         "the diagonal (1), FP32 assembled coefficients (2); FP32 arithmetic in every case")
     ap.add_argument("--restart", type=int, default=30)
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the headline phi check against the oracle")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the compact runs of the channel, batch and serving workloads on the default line")
     return ap.parse_args()
 
 
@@ -94,7 +97,9 @@ def make_case(args):
 
 
 # storage of the FP32 multigrid's level operators (vfs_solve_params.mg_half)
-OPERATOR = {0: "fp32", 1: "fp16 diagonal-normalised, row sums kept (fp32 arithmetic)"}
+OPERATOR = {0: "fp32 (face form on 11-slot levels: 3 face weights + 2 cross weights + aj + code byte per cell)",
+            1: "fp16 diagonal-normalised, row sums kept (fp32 arithmetic)",
+            2: "fp32 assembled coefficients (11 or 19 slots)"}
 
 WORKLOAD = {
     "channel": "channel 64x64x64, tanh beta 2.0, skew 0.05 sin(z), no body, U ~ N(0,1) per face",
@@ -196,24 +201,57 @@ def ncu_traffic(kernel_key: str):
         return None
 
 
-def cpu_baseline(case, args, steps=2):
-    """The CPU oracle (same discretisation, FP64 FGMRES + GMG, OpenMP over all
-    host cores) on the same workload; returns steps/s and the sample."""
+# the oracle's multigrid settings: y-line Jacobi, 2 + 2 sweeps damped 0.8 on
+# every level, 32 sweeps on the coarsest (its defaults); the GPU arm's
+# Chebyshev-damped 3 + 3 sweeps change the iteration history, not the answer
+ORACLE_MG = {"nu1": 2, "nu2": 2, "coarsest_sweeps": 32, "omega": 0.8, "omega_coarsest": 0.8,
+             "smoother": "y-line Jacobi, constant damping"}
+
+
+def oracle_module():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     import oracle as O
     O.build()
+    return O
+
+
+def cpu_baseline(case, args, steps=2):
+    """The CPU oracle (same discretisation, FP64 FGMRES + GMG, OpenMP over all
+    host cores) on the same workload with the GPU arm's stopping rule (rtol
+    and max |div u| <= div_tol); returns steps/s, threads and the last step."""
+    O = oracle_module()
     g = case.grid
     d = O.dims_of(g)
     mg = O.MG(d, g.coor, g.nvert, case.levels)
-    mg.set_params(2, 2, 32, 0.8, 0.8)
-    O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=args.rtol, mg=mg)  # warm-up
+    mg.set_params(ORACLE_MG["nu1"], ORACLE_MG["nu2"], ORACLE_MG["coarsest_sweeps"], ORACLE_MG["omega"],
+                  ORACLE_MG["omega_coarsest"])
+    kw = dict(levels=case.levels, immersed=case.immersed, rtol=args.rtol, div_tol=args.div_tol, mg=mg)
+    O.projection_step(g, case.ucont, **kw)  # warm-up
     t = time.perf_counter()
     for _ in range(steps):
-        r = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=args.rtol, mg=mg)
+        r = O.projection_step(g, case.ucont, **kw)
     dt = time.perf_counter() - t
     mg.close()
     return steps / dt, O.lib().orc_num_threads(), r
+
+
+def oracle_parity(case, phis):
+    """Relative L2 (fluid mean removed) of each phi against a tight oracle
+    solve of the same step (rtol 1e-13), outside any timed region."""
+    O = oracle_module()
+    g = case.grid
+    ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=600)
+    fl = g.nvert < 0.1
+    fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = (False,) * 6
+    r = ref["phi"][fl] - ref["phi"][fl].mean()
+    out = {}
+    for k, phi in phis.items():
+        if phi is not None:
+            a = phi[fl] - phi[fl].mean()
+            out[k] = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    return {"phi_rel_l2_vs_oracle": out, "oracle_rtol": 1e-13, "oracle_divmax": ref["divmax"],
+            "bar": "phi rel L2 <= 1e-8 after removing the fluid mean"}
 
 
 # the headline metric, identical on every line of both arms (the workload and
@@ -234,7 +272,8 @@ def run_reference(args):
             pool = [s.case for s in serve.serving_streams(16)]
         pool.sort(key=lambda c: c.grid.nvert.size)
         sample = pool[len(pool) // 2 - 1:len(pool) // 2 + 1]
-        rates = [cpu_baseline(c, args, steps=1)[0] for c in sample]
+        runs = [cpu_baseline(c, args, steps=1) for c in sample]
+        rates = [r[0] for r in runs]
         val = float(len(rates) / sum(1.0 / r for r in rates))
         cores = os.cpu_count()
         line = {"metric": METRIC, "value": val, "unit": "solves/s",
@@ -242,11 +281,15 @@ def run_reference(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD[args.config], "rtol": args.rtol, "div_tol": args.div_tol,
-                           "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG)"},
+                           "oracle_mg": ORACLE_MG,
+                           "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG, the "
+                                       "GPU arm's stopping rule)"},
+                "divmax": max(r[2]["divmax"] for r in runs),
                 "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
                                  "sample": "two median-size grids of the workload, one step each after a warm-up"},
                 "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "reference build unavailable (PETSc/HYPRE/MPI absent); CPU oracle restatement"}
+                "note": "the reference links PETSc/HYPRE/MPI, absent here: its CPU algorithm is timed as the "
+                        "oracle restatement, which matches the reference's own compiled path functions bit for bit"}
         print(json.dumps(line), flush=True)
         return
     case = make_case(args)
@@ -257,13 +300,17 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD[args.config], "grid": case.name, "cells": int(case.grid.ni * case.grid.nj *
                                                                                    case.grid.nk),
-                   "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol,
-                   "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG)"},
+                   "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "oracle_mg": ORACLE_MG,
+                   "measures": "pressure projection steps/s of the CPU oracle (FP64 FGMRES + GMG, the GPU arm's "
+                               "stopping rule)"},
         "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": f"{WORKLOAD[args.config]}: full-size steps timed after 1 warm-up"},
         "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "divmax": r["divmax"], "iterations": r["info"]["iterations"],
-        "note": "reference build unavailable (PETSc/HYPRE/MPI absent); CPU oracle restatement of its algorithm",
+        "divmax": r["divmax"], "iterations": r["info"]["iterations"], "div_rounds": r["info"]["rounds"],
+        "same_config_note": "same grid, inputs, rtol and div_tol as the GPU arm; its own smoother settings "
+                            "(oracle_mg) and step count, so iteration histories differ",
+        "note": "the reference links PETSc/HYPRE/MPI, absent here: its CPU algorithm is timed as the oracle "
+                "restatement, which matches the reference's own compiled path functions bit for bit",
     }
     print(json.dumps(line), flush=True)
 
@@ -274,6 +321,12 @@ def base_line(args, ws):
 
 
 def main_batch(args, dist, rank, local, ws):
+    line = run_batch(args, dist, local, ws)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_batch(args, dist, local, ws):
     from vfs_v3p2_gb300 import autotune, capi, synth
     sc = max(1, args.scale)
     cases = synth.c4_batch(64, seed=1004, lo=(32 // sc, 32 // sc, 32 // sc), hi=(192 // sc, 96 // sc, 96 // sc))
@@ -350,14 +403,19 @@ def main_batch(args, dist, rank, local, ws):
             "clocks": clocks, "gpu_launches": int(nl), "fp64": fp64}
     if tuned:
         line["autotune"] = tuned
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     for gid in ids:
         ctx.grid_destroy(gid)
     ctx.close()
+    return line
 
 
 def main_serve(args, dist, rank, local, ws):
+    line = run_serve(args, dist, local, ws)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_serve(args, dist, local, ws):
     from vfs_v3p2_gb300 import autotune, capi, serve
     sc = max(1, args.scale)
     streams = serve.serving_streams(16, lo=(32 // sc,) * 3, hi=(256 // sc, 128 // sc, 128 // sc))
@@ -427,10 +485,9 @@ def main_serve(args, dist, rank, local, ws):
             "failed": summ["failed"], "clocks": clocks, "gpu_launches": int(nl), "fp64": fp64}
     if tuned:
         line["autotune"] = tuned
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     srv.close()
     ctx.close()
+    return line
 
 
 def kernel_table(recs, top):
@@ -460,6 +517,67 @@ def smoother_config(args) -> dict:
     if args.smoother == "chebyshev":
         return {"smoother": "chebyshev", "cheb_interval": [args.cheb_hi / args.cheb_ratio, args.cheb_hi]}
     return {"smoother": "jacobi", "omega": args.omega}
+
+
+def compact_single(args, dist, local, ws, config):
+    """Mixed and plain FP64 steps/s of one single-grid workload (U* resident,
+    the headline's stopping rule and smoother), for the default line."""
+    from vfs_v3p2_gb300 import capi
+    a = argparse.Namespace(**vars(args))
+    a.config, a.grid, a.scale = config, None, 1
+    case = make_case(a)
+    g = case.grid
+    ctx = capi.Context(local)
+    gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    ctx.poisson_lhs(gid)
+    ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
+    ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
+    out = {"workload": WORKLOAD[config], "grid": case.name, "mg_levels": case.levels}
+    K = 20
+    for prec in ("mixed", "fp64"):
+        params = capi.default_params(precision=prec, rtol=args.rtol, div_tol=args.div_tol, maxit=400)
+        for _ in range(3):
+            ctx.projection_step(gid, params)
+        barrier(dist)
+        ctx.mark(gid, 0)
+        its, dms = [], []
+        for _ in range(K):
+            info, dm = ctx.projection_step(gid, params)
+            its.append(info["iterations"])
+            dms.append(dm)
+        ctx.mark(gid, 1)
+        t = allmax(dist, ctx.elapsed(0, 1))
+        out[prec] = {"value": ws * K / (t / 1e3), "unit": "solves/s", "iterations": statistics.mean(its),
+                     "divmax": max(dms), "steps": K}
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    ctx.grid_destroy(gid)
+    ctx.close()
+    return out
+
+
+def compact_workloads(args, dist, local, ws):
+    """The channel, batched and served workloads in short runs (default
+    solver parameters, no autotuning), so that one default bench line records
+    every configuration; --config batch / serve give the full runs."""
+    out = {"channel_64x64x64": compact_single(args, dist, local, ws, "channel")}
+    b = argparse.Namespace(**vars(args))
+    b.steps, b.warmup, b.no_tune, b.no_fp64, b.scale = 3, 1, True, False, 1
+    bl = run_batch(b, dist, local, ws)
+    out["batch_64_grids"] = {"workload": WORKLOAD["batch"], "value": bl["value"], "unit": "solves/s",
+                             "steps": bl["steps"], "latency_ms": bl["latency_ms"], "divmax": bl["divmax"],
+                             "iterations": bl["iterations"], "autotuned": False,
+                             "fp64_batched": bl["fp64"]["batched"]["value"],
+                             "mixed_over_fp64_batched": bl["fp64"]["mixed_batched_over_fp64_batched"],
+                             "fp64_divmax": bl["fp64"]["batched"]["divmax"]}
+    v = argparse.Namespace(**vars(args))
+    v.requests, v.warmup, v.no_tune, v.no_fp64, v.scale = 200, 1, True, False, 1
+    sl = run_serve(v, dist, local, ws)
+    out["serve_16_streams"] = {"workload": WORKLOAD["serve"], "value": sl["value"], "unit": "solves/s",
+                               "requests": sl["steps"], "rate_req_s": v.rate, "latency_ms": sl["latency_ms"],
+                               "divmax": sl["divmax"], "failed": sl["failed"], "autotuned": False,
+                               "fp64_latency_ms": sl["fp64"]["latency_ms"], "fp64_divmax": sl["fp64"]["divmax"],
+                               "capacity_solves_per_s": sl["fp64"]["capacity_solves_per_s"]}
+    return out
 
 
 def main():
@@ -493,7 +611,7 @@ def main():
     other = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
-                                mg_half=1 - args.mg_half)
+                                mg_half=2 if args.mg_half == 0 else 0)
     fp64 = capi.default_params(precision="fp64", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols)
@@ -548,7 +666,7 @@ def main():
                "iterations": statistics.mean(i["iterations"] for i in infa), "divmax": max(diva)}
 
     # ---- plain FP64 on the same grid ----
-    fp64_rate, fp64_iters, fp64_div, mix_vs_fp64_err = None, None, None, None
+    fp64_rate, fp64_iters, fp64_div, mix_vs_fp64_err, phi64 = None, None, None, None, None
     if not args.no_fp64:
         steps(fp64, 2, 200)
         K64 = max(3, args.steps // 2)
@@ -586,15 +704,23 @@ def main():
                "d2h_bytes_per_step": hbytes}
 
     peak, peak_kind = measured_peak()
-    achieved = (pbytes / plaunch) / ((pms / plaunch) / 1e3) / 1e9 if plaunch else None
-    kname = "k_smooth<float, __half>" if args.mg_half else "k_smooth<float, float>"
+    # algorithmic bytes of one finest sweep: the FP32 smoother's 53 bytes per
+    # interior cell (9 FP32 metric coefficients, a case byte, x, b, the line
+    # diagonal and the new x), whatever the storage streams
+    n_int = g.ni * g.nj * g.nk
+    alg = 53.0 * n_int
+    avg_ms = pms / plaunch if plaunch else None
+    achieved = alg / (avg_ms / 1e3) / 1e9 if plaunch else None
+    kname = {0: "k_smooth<float, FaceOp>", 1: "k_smooth<float, __half>", 2: "k_smooth<float, float>"}[args.mg_half]
     traffic = ncu_traffic(kname + ":" + case.name)
     roof = {"kernel": kname + " (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-            "traffic": traffic, "launches": plaunch, "avg_launch_ms": pms / plaunch if plaunch else None,
-            "timing": "CUDA event pair around each launch on its stream, over repeats of the timed steps "
-                      "(iterations issued uncaptured, convergence read after each; event and launch overhead included)",
-            "alg_bytes_per_launch": pbytes / plaunch if plaunch else None}
+            "traffic": traffic, "launches": plaunch, "avg_launch_ms": avg_ms,
+            "timing": "CUDA event pair around each run of consecutive finest sweeps on their stream, over repeats "
+                      "of the timed steps (iterations issued uncaptured, convergence read after each)",
+            "alg_bytes_per_launch": alg, "alg_bytes_per_cell": 53.0,
+            "streamed_bytes_per_launch": pbytes / plaunch if plaunch else None,
+            "streamed_frac": ((pbytes / plaunch) / (avg_ms / 1e3) / 1e9 / peak) if plaunch else None}
 
     step_bytes = bytes_all / KP
     solve_hbm = {"alg_bytes_per_step": step_bytes, "achieved_gbs": step_bytes / (tmax / args.steps / 1e3) / 1e9,
@@ -609,6 +735,11 @@ def main():
         cpu = {"value": cval, "unit": "solves/s", "cores": cores, "kind": "port",
                "sample": f"2 full-size steps of {case.name} after 1 warm-up (FP64 FGMRES + GMG, OpenMP)"}
 
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = oracle_parity(case, {"mixed": phi_mixed, "fp64": phi64})
+
+    line = None
     if rank == 0:
         its = [i["iterations"] for i in infos]
         line = {
@@ -631,10 +762,15 @@ def main():
                      "phi_rel_l2_mixed_vs_fp64": mix_vs_fp64_err},
             "mixed_other_operator": alt,
             "roofline": roof, "solve_hbm": solve_hbm, "kernels": kernels,
-            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl),
+            "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(nl), "parity": parity,
         }
-        print(json.dumps(line), flush=True)
     ctx.close()
+    if not args.no_workloads and args.config == "sphere" and not args.grid and args.scale == 1:
+        workloads = compact_workloads(args, dist, local, ws)
+        if line is not None:
+            line["workloads"] = workloads
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 

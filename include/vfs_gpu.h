@@ -96,14 +96,19 @@ typedef struct {
                                   iterations on one large grid (5 / 5 on
                                   256x128x128); the Chebyshev damping needs
                                   none beyond nu1 / nu2 */
-  int mg_half;  /* VFS_MIXED only: 0 (the default) = the multigrid levels'
-                   stencil coefficients are stored in FP32; 1 = stored as
-                   FP16 normalised by their diagonal, with an FP16
-                   centre-slot correction that keeps every row sum (the
-                   arithmetic stays FP32; a smoothing sweep streams 38
-                   instead of 60 bytes per cell: faster on 19-slot grids,
-                   same iterations).  The FP64 FGMRES operator is the same
-                   either way. */
+  int mg_half;  /* VFS_MIXED only: storage of the multigrid levels' operator.
+                   0 (the default): FP32; on levels whose cross terms are the
+                   i-k ones only (the 11-slot operator: channel and sphere
+                   grids) in face form: per cell its three faces' FP32
+                   weights (g11, g22, g33 and the cross weights with the
+                   one-sided regime folded in), aj and a code byte, the row
+                   being aj times the divergence of the face fluxes (a sweep
+                   streams 41 instead of 60 bytes per cell); elsewhere the 19
+                   assembled FP32 coefficients.  2: the assembled FP32
+                   coefficients on every level.  1: FP16 normalised by the
+                   diagonal, with an FP16 centre-slot correction that keeps
+                   every row sum.  The arithmetic is FP32 in every case, and
+                   the FP64 FGMRES operator is the same. */
   int smoother;       /* VFS_SMOOTH_CHEBYSHEV (the default) or VFS_SMOOTH_JACOBI.
                          Both are y-line Jacobi sweeps x += w T^-1 (b - A x), T
                          the j-tridiagonal part of A.  JACOBI: w = omega on every
@@ -214,8 +219,8 @@ int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out);
  *
  * What it does: max over interior cells of |div U| * aj, 0 where the cell or
  * a face neighbour has nvert (the same kernels as vfs_divergence_max), for
- * the ghosted grid mx x my x mz ([mz][my][mx], i fastest) with periodic flags,
- * contravariant fluxes as three component arrays ucont_x/_y/_z, aj and nvert,
+ * the ghosted grid mx x my x mz ([mz][my][mx], i fastest), contravariant
+ * fluxes as three component arrays ucont_x/_y/_z, aj and nvert,
  * all device pointers on `device`.  The result is written to the device
  * double *out, ordered on `stream` (a cudaStream_t; NULL = legacy default
  * stream); the call does not synchronise.
@@ -229,8 +234,13 @@ int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out);
  * streams, or threads, on the same device without ordering between them)
  * race and give undefined results: order them.  The first call on a device
  * looks up the scratch address (cudaGetSymbolAddress, with that device
- * current) and should come before any stream capture.  err (may be NULL)
- * receives a message of at most err_len - 1 characters. */
+ * current) and should come before any stream capture; the address is kept
+ * for the life of the process, so the device must not be reset
+ * (cudaDeviceReset) between calls.  Periodic axes: the flags are accepted
+ * but unused; like the reference's Divergence (main.c:1279-1349) the check
+ * reads each cell's west, south and back faces at index - 1, so a periodic
+ * axis's ghost faces (index 0 = index m - 2) must be filled before the call.
+ * err (may be NULL) receives a message of at most err_len - 1 characters. */
 int vfs_divergence_max_noalloc(int device, int mx, int my, int mz, int i_periodic, int j_periodic, int k_periodic,
                                const double* ucont_x, const double* ucont_y, const double* ucont_z, const double* aj,
                                const double* nvert, double* out, void* stream, char* err, int err_len);

@@ -302,27 +302,44 @@ class MG:
 
 
 def projection_step(grid, ucont, levels=3, dt=0.04, st=1.0, coeff=1.0, immersed=0, rtol=1e-12, maxit=400,
-                    restart=30, p=None, mg=None, orth=2):
+                    restart=30, p=None, mg=None, orth=2, div_tol=0.0, max_rounds=4):
     """The whole CPU pressure-projection step, in the reference's order
     (poisson_hypre.c:580-771, solvers.c:874-930): flux balance, RHS with the
     compatibility fix, FGMRES+GMG solve, null-space removal, phi finish,
-    UpdatePressure, Projection, Contra2Cart, Divergence."""
+    UpdatePressure, Projection, Contra2Cart, Divergence.
+
+    div_tol > 0 applies the CUDA path's stopping rule: while the projected
+    fluxes leave max |div u| above div_tol, the solve continues from its phi
+    with a ten times tighter rtol (at most max_rounds further rounds) and the
+    projection is redone from the balanced fluxes."""
     d = dims_of(grid)
     M = form_metrics(d, grid.coor)
-    u = np.array(ucont, dtype=np.float64, copy=True)
-    fa = volume_flux(d, 1 if immersed else 0, u, grid.nvert, M)
-    b, _ = rhs(d, u, grid.nvert, dt, st, coeff, True)
+    u0 = np.array(ucont, dtype=np.float64, copy=True)
+    fa = volume_flux(d, 1 if immersed else 0, u0, grid.nvert, M)
+    b, _ = rhs(d, u0, grid.nvert, dt, st, coeff, True)
     own = mg is None
     if own:
         mg = MG(d, grid.coor, grid.nvert, levels)
+    aj = metric(M, d, "aj")
     phi, info = mg.fgmres(b, rtol=rtol, maxit=maxit, restart=restart, orth=orth)
+    rounds, its = 0, info["iterations"]
+    while True:
+        ph = phi.copy()
+        remove_mean(d, grid.nvert, ph)
+        phi_finish(d, grid.nvert, ph)
+        u = u0.copy()
+        projection(d, M, grid.nvert, ph, u, dt, st, coeff)
+        divmax = divergence(d, u, aj, grid.nvert)
+        if div_tol <= 0 or divmax <= div_tol or rounds >= max_rounds:
+            break
+        rounds += 1
+        rtol *= 0.1
+        phi, info = mg.fgmres(b, x0=phi, rtol=rtol, maxit=maxit, restart=restart, orth=orth)
+        its += info["iterations"]
     if own:
         mg.close()
-    remove_mean(d, grid.nvert, phi)
-    phi_finish(d, grid.nvert, phi)
-    p = np.zeros(_shape(d)) if p is None else np.array(p, dtype=np.float64, copy=True)
-    update_pressure(d, grid.nvert, phi, p)
-    projection(d, M, grid.nvert, phi, u, dt, st, coeff)
+    info = dict(info, iterations=its, rounds=rounds)
+    pp = np.zeros(_shape(d)) if p is None else np.array(p, dtype=np.float64, copy=True)
+    update_pressure(d, grid.nvert, ph, pp)
     ucat = contra2cart(d, M, grid.nvert, u)
-    divmax = divergence(d, u, metric(M, d, "aj"), grid.nvert)
-    return dict(phi=phi, p=p, ucont=u, ucat=ucat, b=b, info=info, divmax=divmax, flux=fa, M=M)
+    return dict(phi=ph, p=pp, ucont=u, ucat=ucat, b=b, info=info, divmax=divmax, flux=fa, M=M)

@@ -9,9 +9,11 @@ are present; nothing of the product loads it.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -69,6 +71,23 @@ def lib():
     return _lib
 
 
+@contextlib.contextmanager
+def _quiet_stdout():
+    """The reference prints progress with printf (setup_lidx2): drop it."""
+    sys.stdout.flush()
+    saved = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    try:
+        os.dup2(null, 1)
+        yield
+    finally:
+        libc = ctypes.CDLL(None)
+        libc.fflush(None)
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(null)
+
+
 def _p(a):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -104,7 +123,8 @@ class RefGrid:
         vals = np.zeros(cap)
         gid = np.zeros(N)
         ip = ctypes.POINTER(ctypes.c_int)
-        n = lib().vfs_ref_lhs(self.h, rows.ctypes.data_as(ip), cols.ctypes.data_as(ip), _p(vals), cap, _p(gid))
+        with _quiet_stdout():
+            n = lib().vfs_ref_lhs(self.h, rows.ctypes.data_as(ip), cols.ctypes.data_as(ip), _p(vals), cap, _p(gid))
         self.gid = gid.reshape(self.shape)
         self.n_fluid = int(gid.max()) + 1
         return rows[:n], cols[:n], vals[:n], self.gid

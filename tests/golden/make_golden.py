@@ -11,9 +11,10 @@ seeded grids.  Stored per case:
   Convert_Phi2_Phi, UpdatePressure, Projection and Divergence around a direct
   solve of its matrix (HYPRE itself is not part of the sources).
 
-Inputs are not stored: they are regenerated from the seeded synthetic
-generators, and a digest of them is stored to detect generator drift.  The
-fixtures let the oracle (tests/test_golden_cpu.py) and the CUDA path
+The inputs (node coordinates, nvert, fluxes) are stored too: the seeded
+generators use numpy's exp and tanh, whose last bit may differ between
+machines, so a check elsewhere runs on the stored inputs; a digest of the
+inputs detects generator drift where they are regenerated.  The fixtures let the oracle (tests/test_golden_cpu.py) and the CUDA path
 (tests/test_golden_gpu.py) be checked against the reference where its
 sources are absent.
 
@@ -50,6 +51,15 @@ def input_digest(case) -> str:
     return h.hexdigest()
 
 
+def stored_case(gold, name):
+    """The case with the inputs stored in the fixtures (bit-identical on any machine)."""
+    c = cases()[name]
+    c.grid.coor = np.array(gold[f"{name}/in_coor"])
+    c.grid.nvert = np.array(gold[f"{name}/in_nvert"])
+    c.ucont = np.array(gold[f"{name}/in_ucont"])
+    return c
+
+
 def reference_outputs(case):
     import refstep
     r = refstep.reference_step(case)
@@ -61,6 +71,9 @@ def main():
     out = {}
     for name, c in cases().items():
         out[f"{name}/digest"] = np.array(input_digest(c))
+        out[f"{name}/in_coor"] = c.grid.coor
+        out[f"{name}/in_nvert"] = c.grid.nvert
+        out[f"{name}/in_ucont"] = c.ucont
         for k, v in reference_outputs(c).items():
             out[f"{name}/{k}"] = v
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)

@@ -37,12 +37,12 @@ def _fields(ctx, gid, case):
             ctx.get_field(gid, capi.FIELD_UCONT, shp + (3,)))
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed_fp16_operator", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp16_operator", "mixed_fp32_assembled", "fp64"])
 def test_batch_equals_one_at_a_time(gpu_ctx, precision):
     cases = _cases()
     ids = _load(gpu_ctx, cases)
     try:
-        half = 1 if precision == "mixed_fp16_operator" else 0
+        half = {"mixed_fp16_operator": 1, "mixed_fp32_assembled": 2}.get(precision, 0)
         params = capi.default_params(precision=precision.split("_")[0], rtol=1e-9, div_tol=1e-8, mg_half=half)
         for gid, c in zip(ids, cases):
             _reset(gpu_ctx, gid, c)
@@ -82,7 +82,7 @@ def test_batch_per_grid_parameters(gpu_ctx):
             gpu_ctx.grid_destroy(gid)
 
 
-@pytest.mark.parametrize("precision,half", [("mixed", 1), ("mixed", 0), ("fp64", 0)])
+@pytest.mark.parametrize("precision,half", [("mixed", 1), ("mixed", 0), ("mixed", 2), ("fp64", 0)])
 def test_smoother_tile_does_not_change_results(gpu_ctx, precision, half):
     """The y-line smoother's tile (i-columns per block) only regroups
     independent column solves: every tile gives the same bits."""

@@ -116,22 +116,24 @@ def test_half_solve_matches_fp32_storage(gpu_ctx, orth):
     try:
         gpu_ctx.poisson_lhs(gid)
         out = {}
-        for half in (0, 1):
+        for half in (0, 1, 2):  # FP32 face form, FP16 normalised, FP32 assembled coefficients
             params = capi.default_params(precision="mixed", rtol=1e-12, maxit=300, orth=orth, div_tol=1e-8,
                                          mg_half=half)
             u = np.ascontiguousarray(case.ucont.copy())
             gpu_ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
             info, divmax = gpu_ctx.projection_step(gid, params, u, None)
             assert info["converged"] and info["relres"] < 1e-11 and divmax < 1e-8, (half, info, divmax)
-            assert info["mg_half_used"] == bool(half)
+            assert info["mg_half_used"] == (half == 1)
             out[half] = (info, gpu_ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape), u)
-        (i0, phi0, u0), (i1, phi1, u1) = out[0], out[1]
-        assert abs(i1["iterations"] - i0["iterations"]) <= 1, (i0, i1)
+        i0, phi0, u0 = out[0]
         fl = (g.nvert < 0.1)
         fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
-        a, r = phi1[fl] - phi1[fl].mean(), phi0[fl] - phi0[fl].mean()
-        assert np.linalg.norm(a - r) / np.linalg.norm(r) <= 1e-9
-        assert np.abs(u1 - u0).max() <= 1e-9 * np.abs(u0).max()
+        for half in (1, 2):
+            i1, phi1, u1 = out[half]
+            assert abs(i1["iterations"] - i0["iterations"]) <= 1, (i0, i1)
+            a, r = phi1[fl] - phi1[fl].mean(), phi0[fl] - phi0[fl].mean()
+            assert np.linalg.norm(a - r) / np.linalg.norm(r) <= 1e-9
+            assert np.abs(u1 - u0).max() <= 1e-9 * np.abs(u0).max()
     finally:
         gpu_ctx.grid_destroy(gid)
 
@@ -142,7 +144,9 @@ def test_mg_half_rejected_values(gpu_ctx):
     gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
     try:
         gpu_ctx.poisson_lhs(gid)
-        with pytest.raises(capi.VfsError):
-            gpu_ctx.projection_step(gid, capi.default_params(mg_half=2), np.ascontiguousarray(case.ucont.copy()), None)
+        for bad in (-1, 3):
+            with pytest.raises(capi.VfsError):
+                gpu_ctx.projection_step(gid, capi.default_params(mg_half=bad), np.ascontiguousarray(case.ucont.copy()),
+                                        None)
     finally:
         gpu_ctx.grid_destroy(gid)

@@ -90,6 +90,27 @@ def test_operator_apply(gpu_ctx, loaded):
         assert np.abs(got32 - refm).max() <= 1e-5 * np.abs(refm).max()  # FP32 coefficients and arithmetic
 
 
+def test_face_form_operator(gpu_ctx, loaded):
+    """The FP32 face form of an 11-slot level (the multigrid operator as aj
+    times the divergence of face fluxes) is the assembled operator: equal to
+    FP32 rounding against the FP64 coefficients and the FP32 ones."""
+    case, gid, d, mg = loaded
+    rng = np.random.default_rng(9)
+    checked = 0
+    for l in range(case.levels):
+        if gpu_ctx.coef(gid, l, 1).reshape(19, -1)[7:15].any():  # i-j or j-k cross terms: not an 11-slot level
+            continue
+        ld = mg.level_dims(l)
+        x = rng.normal(size=(ld.mz, ld.my, ld.mx))
+        ref = gpu_ctx.apply_op(gid, l, 1, x.astype(np.float32).astype(np.float64))
+        got = gpu_ctx.apply_op(gid, l, 4, x)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), l  # FP32 arithmetic and storage
+        got32 = gpu_ctx.apply_op(gid, l, 2, x)
+        assert np.abs(got - got32).max() <= 1e-5 * np.abs(ref).max(), l
+        checked += 1
+    assert checked == case.levels
+
+
 def test_krylov_product_fp32_operand_exact(gpu_ctx, loaded):
     """The mixed solver's FP64 product on FP32 directions widens each operand
     on the integer pipe; it must equal the FP64 product of the same rounded
@@ -209,17 +230,20 @@ def test_projection_fractional_nvert_bitexact(gpu_ctx):
     gpu_ctx.grid_destroy(gid)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp16_operator"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp16_operator", "mixed_fp32_assembled"])
 @pytest.mark.parametrize("orth", ["cgs", "cgs2"])
 def test_full_step_parity(gpu_ctx, loaded, precision, orth):
-    """mixed: FP32 multigrid on FP32 stencil coefficients (the default);
-    mixed_fp16_operator: on the FP16 diagonal-normalised operator."""
+    """mixed: FP32 multigrid on FP32 stencil coefficients, in face form on
+    11-slot levels (the default); mixed_fp16_operator: on the FP16
+    diagonal-normalised operator; mixed_fp32_assembled: on the 19 assembled
+    FP32 coefficients."""
     case, gid, d, mg = loaded
     g = case.grid
     ref = O.projection_step(g, case.ucont, levels=case.levels, immersed=case.immersed, rtol=1e-13, maxit=400, mg=mg,
                             orth=1 if orth == "cgs" else 2)
     params = capi.default_params(precision=precision.split("_")[0], rtol=1e-12, maxit=300, restart=30, orth=orth,
-                                 div_tol=1e-8, mg_half=1 if precision == "mixed_fp16_operator" else 0)
+                                 div_tol=1e-8,
+                                 mg_half={"mixed_fp16_operator": 1, "mixed_fp32_assembled": 2}.get(precision, 0))
     u = np.ascontiguousarray(case.ucont.copy())
     p = np.zeros(g.nvert.shape)
     info, divmax = gpu_ctx.projection_step(gid, params, u, p)

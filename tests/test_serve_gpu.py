@@ -60,3 +60,42 @@ def test_budget_eviction_and_readmission():
     with capi.Context(0, hbm_budget_bytes=budget) as ctx:
         recs = _run(ctx, streams, _arrivals())
     assert all(r["status"] == 0 and r["divmax"] < 1e-8 for r in recs)
+
+
+def test_per_grid_calls_refuse_a_busy_grid():
+    """While a submitted request is in flight on a grid, the entry points that
+    use the grid's device state return VFS_ERR_BUSY instead of racing with it;
+    once vfs_poll has returned the request they work again."""
+    import numpy as np
+
+    from vfs_v3p2_gb300 import synth
+    case = synth.channel_case(32, 16, 16, seed=43, levels=3)
+    g = case.grid
+    params = capi.default_params(rtol=1e-9, div_tol=1e-8)
+    with capi.Context(0) as ctx:
+        gid = ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+        ctx.poisson_lhs(gid)
+        ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
+        ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
+        ticket = ctx.submit(gid, params)
+        assert ticket is not None
+        calls = [
+            lambda: ctx.poisson_solve(gid, params),
+            lambda: ctx.poisson_lhs(gid),
+            lambda: ctx.set_field(gid, capi.FIELD_UCONT, case.ucont),
+            lambda: ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape),
+            lambda: ctx.poisson_rhs(gid),
+            lambda: ctx.update_pressure(gid),
+            lambda: ctx.projection(gid),
+            lambda: ctx.divergence_max(gid),
+        ]
+        for call in calls:
+            with pytest.raises(capi.VfsError) as e:
+                call()
+            assert e.value.code == capi.VFS_ERR_BUSY
+        res = None
+        while res is None:
+            res = ctx.poll(wait=True)
+        assert res[0] == ticket and res[1] == 0 and res[3] < 1e-8
+        ctx.divergence_max(gid)  # idle again
+        ctx.grid_destroy(gid)

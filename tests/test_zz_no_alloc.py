@@ -67,3 +67,40 @@ def test_noalloc_rejects_oversized_grid(gpu_ctx):
     rc = capi.load().vfs_divergence_max_noalloc(0, 2048, 2048, 2048, 0, 0, 0, p, p, p, p, p, p, 0, err, 256)
     assert rc == capi.VFS_ERR_ARG
     assert b"2^31" in err.value
+
+
+def test_noalloc_periodic_flags_do_not_fill_ghosts(gpu_ctx):
+    """Current behaviour: the periodic flags are accepted but unused.  Like the
+    reference's Divergence (main.c:1279-1349) the check reads each cell's west,
+    south and back faces at index - 1, so with the periodic ghost faces left
+    unfilled the result is the same with and without the flags, and equals
+    the oracle's divergence of those (unfilled) fluxes."""
+    torch = _torch_cuda()
+    import oracle as O
+    case = synth.channel_case(16, 12, 16, seed=32, levels=2)
+    g = case.grid
+    u = case.ucont.copy()
+    u[:, :, 0, 0] = 0.0  # periodic ghost faces left unfilled
+    u[0, :, :, 2] = 0.0
+    d = O.dims_of(g)
+    M = O.form_metrics(d, g.coor)
+    aj = O.metric(M, d, "aj")
+    ref = O.divergence(d, u, aj, g.nvert)
+    mz, my, mx = g.nvert.shape
+    dev = torch.device("cuda", 0)
+    comps = [torch.from_numpy(np.ascontiguousarray(u[..., c]).reshape(-1)).to(dev) for c in range(3)]
+    ajd = torch.from_numpy(np.ascontiguousarray(aj).reshape(-1)).to(dev)
+    nvd = torch.from_numpy(np.ascontiguousarray(g.nvert).reshape(-1)).to(dev)
+    out = torch.full((2,), -1.0, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    err = ctypes.create_string_buffer(256)
+    stream = torch.cuda.current_stream().cuda_stream
+    L = capi.load()
+    for call, flags in enumerate(((1, 0, 1), (0, 0, 0))):
+        rc = L.vfs_divergence_max_noalloc(0, mx, my, mz, *flags, comps[0].data_ptr(), comps[1].data_ptr(),
+                                          comps[2].data_ptr(), ajd.data_ptr(), nvd.data_ptr(),
+                                          out.data_ptr() + 8 * call, stream, err, 256)
+        assert rc == 0, err.value.decode()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert got[0] == got[1] == ref, (got, ref)

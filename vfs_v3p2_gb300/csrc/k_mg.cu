@@ -133,11 +133,14 @@ __device__ __forceinline__ void gather(const Dims& d, const TC* __restrict__ coe
   else stencil_gather<MASK>(d, coef, x, i, j, k, cv, xv);
 }
 
+struct FaceOp;
+
 // Coefficient array of a view in storage type TC: the level's own (TC = T)
 // or its FP16 diagonal-normalised copy (TC = __half).
 template <typename TC, typename T>
 __device__ __forceinline__ const TC* coef_ptr(const OpView<T>& A) {
   if constexpr (std::is_same<TC, __half>::value) return A.hcoef;
+  else if constexpr (std::is_same<TC, FaceOp>::value) return nullptr;
   else return A.coef;
 }
 
@@ -170,6 +173,38 @@ __device__ __forceinline__ TA stencil_clamped(const Dims& d, const TC* __restric
 }
 
 __host__ __forceinline__ bool fits_ch(unsigned mask) { return (mask & ~MASK_CH) == 0u; }
+
+// Storage tag of the FP32 multigrid's face form (OpView::ffi ...): the row
+// is aj times the divergence of six face fluxes (k_face_operator).
+struct FaceOp {};
+
+// Row of the face-form operator at a cell from its 11 stencil values (slot
+// order of the 11-slot set: C E W N S T B TE BE TW BW), its own +i, +j, +k
+// faces, the -i face of its i-1 neighbour, the -j of j-1 and the -k of k-1.
+// Returns aj (A x)_c; a and cn: the row's SP and NP coefficients.
+struct FaceData {
+  float2 fic, fiw, fkc, fkb;  // (normal, cross weight) of the +i faces of c, c-i and the +k faces of c, c-k
+  float gjc, gjs, aj;
+  unsigned cc, cw, cb;        // code bits of c, c-i, c-k
+};
+__device__ __forceinline__ float face_row(const FaceData& f, const float* x) {
+  const float xc = x[CP], xe = x[EP], xw = x[WP], xn = x[NP], xs = x[SP], xt = x[TP], xb = x[BP];
+  const float xte = x[TE], xbe = x[BE], xtw = x[TW], xbw = x[BW];
+  // +i face of c: the pair (C, E) at k+1 / k / k-1
+  const float ce = xc + xe, te = xt + xte, be = xb + xbe;
+  const float Fic = f.fic.x * (xe - xc) + f.fic.y * (((f.cc & 1u) ? ce : te) - ((f.cc & 2u) ? ce : be));
+  // +i face of c-i: the pair (W, C)
+  const float wc = xw + xc, tw = xtw + xt, bw = xbw + xb;
+  const float Fiw = f.fiw.x * (xc - xw) + f.fiw.y * (((f.cw & 1u) ? wc : tw) - ((f.cw & 2u) ? wc : bw));
+  // +k face of c: the pair (C, T) at i+1 / i / i-1
+  const float ct = xc + xt, ete = xe + xte, wtw = xw + xtw;
+  const float Fkc = f.fkc.x * (xt - xc) + f.fkc.y * (((f.cc & 4u) ? ct : ete) - ((f.cc & 8u) ? ct : wtw));
+  // +k face of c-k: the pair (B, C)
+  const float bc = xb + xc, eb = xbe + xe, wb = xbw + xw;
+  const float Fkb = f.fkb.x * (xc - xb) + f.fkb.y * (((f.cb & 4u) ? bc : eb) - ((f.cb & 8u) ? bc : wb));
+  const float Fj = f.gjc * (xn - xc) - f.gjs * (xc - xs);
+  return f.aj * ((Fic - Fiw) + Fj + (Fkc - Fkb));
+}
 
 // ---------------------------------------------------------------------------
 // FP64 outer operator: y = A x, or y = b - A x.
@@ -243,6 +278,41 @@ template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s) {
   if (fits_ch(A.mask)) k_apply_mg<MASK_CH, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
   else k_apply_mg<MASK_ALL, T><<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, b, y);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// y = A x with the FP32 face form (11-slot levels; testing hook).
+__global__ void __launch_bounds__(TX* TY) k_apply_face(OpView<float> A, const float* __restrict__ x,
+                                                       float* __restrict__ y) {
+  TILE_LOOP(A.d) {
+    if (!_in) continue;
+    const Dims d = A.d;
+    const int sy = d.mx, sz = d.mx * d.my;
+    const int c = k * sz + j * sy + i;
+    const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
+    const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
+    const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
+    FaceData f;
+    f.fic = A.ffi[c];
+    f.fiw = A.ffi[c + oiW];
+    f.fkc = A.ffk[c];
+    f.fkb = A.ffk[c + okB];
+    f.gjc = A.ffj[c];
+    f.gjs = A.ffj[c + ojS];
+    f.aj = A.faj[c];
+    f.cc = A.fcode[c];
+    f.cw = A.fcode[c + oiW];
+    f.cb = A.fcode[c + okB];
+    float xv[19];
+    xv[CP] = x[c]; xv[EP] = x[c + oiE]; xv[WP] = x[c + oiW]; xv[NP] = x[c + ojN]; xv[SP] = x[c + ojS];
+    xv[TP] = x[c + okT]; xv[BP] = x[c + okB]; xv[TE] = x[c + okT + oiE]; xv[BE] = x[c + okB + oiE];
+    xv[TW] = x[c + okT + oiW]; xv[BW] = x[c + okB + oiW];
+    y[c] = face_row(f, xv);
+  }
+}
+int launch_apply_face(const OpView<float>& A, const float* x, float* y, cudaStream_t s) {
+  k_apply_face<<<tile_grid(A.d), dim3(TX, TY), 0, s>>>(A, x, y);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -430,6 +500,75 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
   }
 }
 
+// Phase 1 of the sweep on the face form (FP32): U cells per thread batch,
+// every load issued before the arithmetic; writes su, sp, sl of the tile.
+// From a zero guess (ZG) the residual is b and only the j faces and aj are
+// read.  Non-fluid rows (aj = 0) stage zeros.
+template <int U, bool ZG>
+__device__ __forceinline__ void face_phase1(const OpView<float>& A, const float* __restrict__ lf,
+                                            const float* __restrict__ xi, const float* __restrict__ b, float* su,
+                                            float* sp, float* sl, int i0, int k, int TW) {
+  const Dims d = A.d;
+  const int nj = d.my - 2, sy = d.mx, sz = d.mx * d.my;
+  const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
+  for (int base = threadIdx.x; base < TW * nj; base += U * VFS_SMOOTH_NT) {
+    FaceData f[U];
+    float xv[U][11], bb[U], inv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = min(base + u * VFS_SMOOTH_NT, TW * nj - 1);
+      const int il = idx % TW, jl = idx / TW;
+      const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
+      const int c = k * sz + j * sy + i;
+      const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
+      const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
+      f[u].gjc = __ldg(A.ffj + c);
+      f[u].gjs = __ldg(A.ffj + c + ojS);
+      f[u].aj = __ldg(A.faj + c);
+      if (!ZG) {
+        f[u].fic = __ldg(A.ffi + c);
+        f[u].fiw = __ldg(A.ffi + c + oiW);
+        f[u].fkc = __ldg(A.ffk + c);
+        f[u].fkb = __ldg(A.ffk + c + okB);
+        f[u].cc = __ldg(A.fcode + c);
+        f[u].cw = __ldg(A.fcode + c + oiW);
+        f[u].cb = __ldg(A.fcode + c + okB);
+        xv[u][0] = __ldg(xi + c);
+        xv[u][1] = __ldg(xi + c + oiE);
+        xv[u][2] = __ldg(xi + c + oiW);
+        xv[u][3] = __ldg(xi + c + ojN);
+        xv[u][4] = __ldg(xi + c + ojS);
+        xv[u][5] = __ldg(xi + c + okT);
+        xv[u][6] = __ldg(xi + c + okB);
+        xv[u][7] = __ldg(xi + c + okT + oiE);
+        xv[u][8] = __ldg(xi + c + okB + oiE);
+        xv[u][9] = __ldg(xi + c + okT + oiW);
+        xv[u][10] = __ldg(xi + c + okB + oiW);
+      }
+      bb[u] = __ldg(b + c);
+      inv[u] = __ldg(lf + c);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = base + u * VFS_SMOOTH_NT;
+      if (idx >= TW * nj) break;
+      const int jl = idx / TW;
+      const bool live = (i0 + idx % TW <= d.mx - 2) && f[u].aj != 0.f;
+      float x11[19];  // slot-indexed view of the 11 values
+      if (!ZG) {
+        x11[CP] = xv[u][0]; x11[EP] = xv[u][1]; x11[WP] = xv[u][2]; x11[NP] = xv[u][3]; x11[SP] = xv[u][4];
+        x11[TP] = xv[u][5]; x11[BP] = xv[u][6]; x11[TE] = xv[u][7]; x11[BE] = xv[u][8]; x11[TW] = xv[u][9];
+        x11[BW] = xv[u][10];
+      }
+      const float ax = ZG ? 0.f : face_row(f[u], x11);
+      const float a = jl > 0 ? f[u].aj * f[u].gjs : 0.f, cn = jl < nj - 1 ? f[u].aj * f[u].gjc : 0.f;
+      su[idx] = live ? (bb[u] - ax) * inv[u] : 0.f;
+      sp[idx] = live ? a * inv[u] : 0.f;
+      sl[idx] = live ? cn * inv[u] : 0.f;
+    }
+  }
+}
+
 // UU: cells whose loads one thread issues together in phase 1 (2 on levels
 // with fewer than two blocks per SM, where the looser register budget costs
 // no occupancy and halves the serial chain of round trips).
@@ -444,7 +583,8 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
   // NRM: the FP16 diagonal-normalised operator (b is divided by D, non-fluid
   // rows have 1/m = 0 so their delta is 0 without a test)
   constexpr bool NRM = std::is_same<TC, __half>::value;
-  constexpr int PF = NRM ? VFS_SMOOTH_PF_HALF : VFS_SMOOTH_PF;
+  constexpr bool FACE = std::is_same<TC, FaceOp>::value;
+  constexpr int PF = (NRM || FACE) ? VFS_SMOOTH_PF_HALF : VFS_SMOOTH_PF;
   const TC* __restrict__ coef = coef_ptr<TC>(A);
   extern __shared__ unsigned char smraw[];
   const Dims d = A.d;
@@ -504,6 +644,9 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
     // 11-slot levels (half the serial loads per thread); the large 11-slot
     // levels measured faster one cell per thread at 4 blocks per SM.
     smooth_pairs<MASK, T>(A, lf, xi, b, su, sp, sl, i0, k, TW);
+  } else if constexpr (FACE) {
+    static_assert(sizeof(T) == 4 && MASK == MASK_CH, "the face form is the FP32 11-slot operator");
+    face_phase1<UU, ZG>(A, lf, xi, b, su, sp, sl, i0, k, TW);
   } else {
     // Phase 1 in batches of U cells per thread: every load of the batch is
     // issued before any arithmetic (all addresses are interior cells: columns
@@ -714,6 +857,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
       smooth_attrs<MASK_CH, T, __half, false>();
       smooth_attrs<MASK_CH, T, __half, true>();
       smooth_attrs<MASK_ALL, T, __half, true>();
+      smooth_attrs<MASK_CH, T, FaceOp, false>();
     }
     attr = true;
   }
@@ -728,7 +872,10 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   const bool small = sizeof(T) == 4 && solo && (size_t)g.x * g.y < 2 * 152;  // (FP64: spills at two cells)
   bool done = false;
   if constexpr (sizeof(T) == 4) {
-    if (A.hcoef) {
+    if (A.ffi && ch) {
+      smooth_launch<MASK_CH, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+      done = true;
+    } else if (A.hcoef) {
       if (!ch) smooth_launch<MASK_ALL, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
       else if (ncell(A.d) <= (size_t)VFS_SMOOTH_PAIR_MAXN)
         smooth_launch<MASK_CH, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);

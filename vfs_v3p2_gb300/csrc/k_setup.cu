@@ -525,6 +525,86 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
 }
 
 // ---------------------------------------------------------------------------
+// Face form of a level's aj-scaled operator for the FP32 multigrid (levels
+// whose i-j and j-k cross terms vanish: the 11-slot operator).  The assembly
+// above builds every row from six face fluxes, each computed identically by
+// the two cells that share the face (poisson.c:1173-1558: the i+1 branch of
+// cell c and the i-1 branch of cell c+1 test the same cells and walls), so
+//   (A x)_c = F_i(c) - F_i(c-i) + F_j(c) - F_j(c-j) + F_k(c) - F_k(c-k),
+//   F_i(c) = gi (x_E - x_C) + gik (U - L)      (the k cross term of g13)
+//   F_j(c) = gj (x_N - x_C)
+//   F_k(c) = gk (x_T - x_C) + gki (R - Lf)     (the i cross term of g31)
+// with gi = g11, gj = g22, gk = g33 where the face exists (both cells fluid,
+// not a non-periodic wall) and 0 elsewhere, and the cross term's regime
+// folded into its weight (0.25 centred, 0.5 one-sided, 0 none) and two code
+// bits: U is the pair at k+1 (x_T + x_TE) or, one-sided, the centre pair
+// (x_C + x_E); L the pair at k-1 or the centre pair; likewise R / Lf for the
+// pairs at i+1 / i-1 of the k face.  A cell owns its +i, +j, +k faces; the
+// row is scaled by aj.  A row streams 5 FP32 face weights, aj and a code
+// byte (25 bytes) instead of 11 FP32 coefficients (44 bytes).
+// ---------------------------------------------------------------------------
+__global__ void k_face_operator(Dims d, const double* __restrict__ g, const double* __restrict__ nvert,
+                                const double* __restrict__ aj, float2* __restrict__ fi, float2* __restrict__ fk,
+                                float* __restrict__ fj, float* __restrict__ faj, uint8_t* __restrict__ code) {
+  const size_t N = ncell(d);
+  const int mx = d.mx, my = d.my, mz = d.mz, ip = d.ip, jp = d.jp, kp = d.kp;
+  const double *g11 = g, *g13 = g + 2 * N, *g22 = g + 4 * N, *g31 = g + 6 * N, *g33 = g + 8 * N;
+  const double THR = VFS_THR;
+  GRID_LOOP(d) {
+    DECOMP(d, i, j, k);
+    float2 vi = make_float2(0.f, 0.f), vk = make_float2(0.f, 0.f);
+    float vj = 0.f;
+    unsigned cb = 0;
+    const bool row = interior(d, i, j, k) && !(nvert[_t] > THR);
+    if (row) {
+#define NV(ii, jj, kk) nvert[cidx(d, ii, jj, kk)]
+      const size_t c = _t;
+      if (NV(i + 1, j, k) < THR && (i != mx - 2 || ip)) {  // i+1/2 face, poisson.c:1173-1232
+        double s = 0.;
+        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > THR) {
+          if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < THR && k != 1) {
+            s = 0.5;  // backward: U = centre pair
+            cb |= 1u;
+          }
+        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > THR) {
+          if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < THR) {
+            s = 0.5;  // forward: L = centre pair
+            cb |= 2u;
+          }
+        } else {
+          s = 0.25;
+        }
+        vi = make_float2((float)g11[c], (float)(g13[c] * s));
+      }
+      if (NV(i, j + 1, k) < THR && (j != my - 2 || jp)) vj = (float)g22[c];  // j+1/2 face
+      if (NV(i, j, k + 1) < THR && (k != mz - 2 || kp)) {                   // k+1/2 face, poisson.c:1421-1488
+        double s = 0.;
+        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > THR) {
+          if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < THR && i != 1) {
+            s = 0.5;  // backward: R = centre pair
+            cb |= 4u;
+          }
+        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > THR) {
+          if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < THR) {
+            s = 0.5;  // forward: Lf = centre pair
+            cb |= 8u;
+          }
+        } else {
+          s = 0.25;
+        }
+        vk = make_float2((float)g33[c], (float)(g31[c] * s));
+      }
+#undef NV
+    }
+    fi[_t] = vi;
+    fk[_t] = vk;
+    fj[_t] = vj;
+    faj[_t] = row ? (float)aj[_t] : 0.f;
+    code[_t] = (uint8_t)cb;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Multigrid hierarchy.
 // ---------------------------------------------------------------------------
 // Coarse node coordinates = every other fine node (init.c:397-449).
@@ -728,6 +808,12 @@ int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tm
   k_metrics_centred<<<nblk(N), 256, 0, s>>>(d, coor, M, tmp); ++g_launches;
   for (int a = 0; a < 3; a++) k_metrics_mirror<<<nblk(N), 256, 0, s>>>(d, M, a); ++g_launches;
   k_metrics_faces<<<nblk(N), 256, 0, s>>>(d, coor, M); ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
+                         float* fj, float* faj, uint8_t* code, cudaStream_t s) {
+  k_face_operator<<<nblk(ncell(d)), 256, 0, s>>>(d, g, nvert, aj, fi, fk, fj, faj, code); ++g_launches;
   return (int)cudaGetLastError();
 }
 

@@ -139,6 +139,13 @@ struct Level {
   float* rwh = nullptr;     // its restriction weights (levels >= 1)
   float* dinvh = nullptr;   // finest level: 1 / D (input scaling)
   float* dvalh = nullptr;   // coarsest level: D (dense-solve scaling)
+  // face form of the FP32 multigrid operator (11-slot levels, mg_half = 0):
+  // +i / +k faces (normal, cross weight), +j face, aj, cross-term code bits
+  float2* ffi = nullptr;
+  float2* ffk = nullptr;
+  float* ffj = nullptr;
+  float* faj = nullptr;
+  uint8_t* fcode = nullptr;
 };
 
 struct Grid {
@@ -332,6 +339,13 @@ Grid* get_grid(vfs_ctx* ctx, int id) {
   return it == ctx->grids.end() ? nullptr : it->second;
 }
 
+// Entry points that read or write a grid's device state refuse while a
+// submitted request is in flight on it (its job owns the grid's buffers and
+// stream until vfs_poll returns it).
+int check_idle(vfs_ctx* ctx, const Grid* g) {
+  return g->busy ? fail(ctx, VFS_ERR_BUSY, "the grid has a request in flight (vfs_poll it first)") : VFS_OK;
+}
+
 int coarse_n(int n) { return n / 2; }
 
 template <typename T> T* mcoef_of(Level& L);
@@ -368,11 +382,20 @@ template <typename T> const float* dinv_sel(Level& L, bool half);
 template <> const float* dinv_sel<float>(Level& L, bool half) { return half ? L.dinvh : nullptr; }
 template <> const float* dinv_sel<double>(Level&, bool) { return nullptr; }
 template <typename T>
-OpView<T> mgview(Level& L, const int* skip, bool half) {
+OpView<T> mgview(Level& L, const int* skip, bool half, bool face = false) {
   OpView<T> A = mgview<T>(L, skip);
   if (sizeof(T) == 4 && half) A.hcoef = L.hcoef;
+  if (sizeof(T) == 4 && !half && face) {
+    A.ffi = L.ffi;
+    A.ffk = L.ffk;
+    A.ffj = L.ffj;
+    A.faj = L.faj;
+    A.fcode = L.fcode;
+  }
   return A;
 }
+// The FP32 face form runs on levels whose operator fits the 11-slot set.
+bool face_level(const Level& L) { return (L.mask & ~0x7807Fu) == 0u; }
 
 template <typename T>
 int ensure_mg(vfs_ctx* ctx, Grid& g) {
@@ -419,6 +442,7 @@ struct MGCfg {
   int nu1c, nu2c;  // sweeps on the levels below the finest
   int top;         // index of the finest level
   bool half;       // FP16 normalised operator (FP32 multigrid only)
+  bool face;       // FP32 face form on 11-slot levels (FP32 multigrid only)
   bool solo;       // the grid's solve runs alone
   int pre(int l) const { return l == top ? nu1 : nu1c; }
   int post(int l) const { return l == top ? nu2 : nu2c; }
@@ -439,9 +463,11 @@ void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T*
   // x != 0: the coefficient slots (FP16 or T), x, b and 1/m read, x written;
   // from a zero guess: the centre (not with the FP16 operator), SP and NP
   // slots, b and 1/m read, x written
+  // face form: the 5 face weights, aj and the code byte (25 bytes) instead
+  // of the slots; from a zero guess the j faces and aj (8 bytes)
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
-  const double bytes = (double)n_interior(A.d) * (xi ? slot_bytes * popcount(A.mask) + 4.0 * sizeof(T)
-                                                     : slot_bytes * (A.hcoef ? 2 : 3) + 3.0 * sizeof(T));
+  const double op_bytes = A.ffi ? (xi ? 25.0 : 8.0) : (xi ? slot_bytes * popcount(A.mask) : slot_bytes * (A.hcoef ? 2 : 3));
+  const double bytes = (double)n_interior(A.d) * (op_bytes + (xi ? 4.0 : 3.0) * sizeof(T));
   int rc;
   {
     Probed pr(VFS_PROBE_ALL, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
@@ -490,7 +516,8 @@ template <typename T>
 T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, cudaStream_t s) {
   Level& L = g.lev[l];
   const bool half = sizeof(T) == 4 && c.half;
-  OpView<T> A = mgview<T>(L, skip, half);
+  const bool face = sizeof(T) == 4 && !half && c.face && face_level(L);
+  OpView<T> A = mgview<T>(L, skip, half, face);
   T* lf = lf_sel<T>(L, half);
   const int W = level_writes(g, l, c);
   T* bufs[2] = {xa, xb};
@@ -513,8 +540,8 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   int q = 0;
   T* cur = nullptr;
   const bool run_probe = g_probe.kind == VFS_PROBE_SMOOTH && l == g.L - 1;
-  const double sweep_bytes = (double)n_interior(A.d) * ((A.hcoef ? 2.0 : (double)sizeof(T)) * popcount(A.mask) +
-                                                        4.0 * sizeof(T));
+  const double sweep_bytes = (double)n_interior(A.d) * ((A.ffi ? 25.0 : (A.hcoef ? 2.0 : (double)sizeof(T)) *
+                                                                            popcount(A.mask)) + 4.0 * sizeof(T));
   SweepRun run;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
@@ -592,7 +619,8 @@ MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
   sweep_damping(p, c.nu1c, c.wc[0], tmp);
   sweep_damping(p, c.nu2c, tmp, c.wc[1]);
   c.top = top;
-  c.half = p.precision == VFS_MIXED && p.mg_half != 0 && half_ok;
+  c.half = p.precision == VFS_MIXED && p.mg_half == 1 && half_ok;
+  c.face = p.precision == VFS_MIXED && p.mg_half == 0;
   c.solo = false;
   return c;
 }
@@ -789,11 +817,15 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   const unsigned long long n0 = g_launches.load();
   CK(cudaStreamBeginCapture(g.s, cudaStreamCaptureModeThreadLocal));
   issue_iteration<T>(g, p, g.s);
-  CK(cudaStreamEndCapture(g.s, &graph));
+  cudaError_t e = cudaStreamEndCapture(g.s, &graph);
   // captured launches run on replay, not now: count them per replay instead
   g.ig_kernels = g_launches.load() - n0;
   g_launches -= g.ig_kernels;
-  cudaError_t e = cudaGraphInstantiate(&g.ig_exec, graph, 0);
+  if (e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return cuda_fail(ctx, e, "cudaStreamEndCapture");
+  }
+  e = cudaGraphInstantiate(&g.ig_exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
   g.ig_prec = prec;
@@ -901,7 +933,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
     return fail(ctx, VFS_ERR_ARG, "smooth_cols must be 0 (automatic), 8, 16 or 32");
-  if (p->mg_half != 0 && p->mg_half != 1) return fail(ctx, VFS_ERR_ARG, "mg_half must be 0 or 1");
+  if (p->mg_half < 0 || p->mg_half > 2) return fail(ctx, VFS_ERR_ARG, "mg_half must be 0, 1 or 2");
   if (p->nu1 > MAXSWEEP || p->nu2 > MAXSWEEP || p->nu1_coarse > MAXSWEEP || p->nu2_coarse > MAXSWEEP)
     return fail(ctx, VFS_ERR_ARG, "at most 64 smoothing sweeps per level and side");
   if (p->smoother != VFS_SMOOTH_JACOBI && p->smoother != VFS_SMOOTH_CHEBYSHEV)
@@ -1445,6 +1477,7 @@ size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
   b += 19 * 2 * hslot(d) + N * (4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
+  b += N * (8 + 8 + 4 + 4 + 1);               // face form: ffi ffk ffj faj fcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
   return b;
@@ -1614,6 +1647,11 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.rw64, Lv.N);
     if (l > 0) GAB(Lv.pcode, Lv.N);
     GAB(Lv.hcoef, 19 * hslot(Lv.d));
+    GAB(Lv.ffi, Lv.N);
+    GAB(Lv.ffk, Lv.N);
+    GAB(Lv.ffj, Lv.N);
+    GAB(Lv.faj, Lv.N);
+    GAB(Lv.fcode, Lv.N);
     GAB(Lv.lfh, Lv.N);
     GAB(Lv.rwh, Lv.N);
     if (l == L - 1) GAB(Lv.dinvh, Lv.N);
@@ -1764,6 +1802,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   CK(cudaSetDevice(ctx->device));
   const size_t N = ncell(g.d);
@@ -1776,6 +1815,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     Level& Lv = g.lev[l];
     launch_gtensor(Lv.d, Lv.M, gt, g.s);
     launch_assemble(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.coef, Lv.mcoef, Lv.mcoef32, dmask, g.s);
+    launch_face_operator(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.ffi, Lv.ffk, Lv.ffj, Lv.faj, Lv.fcode, g.s);
     CK(cudaMemcpyAsync(&Lv.mask, dmask, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
@@ -1881,6 +1921,7 @@ int vfs_set_field(vfs_ctx* ctx, int grid, int field, const double* host) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || !host) return fail(ctx, VFS_ERR_ARG, "no such grid or null buffer");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   const size_t N = ncell(g.d);
   switch (field) {
@@ -1904,6 +1945,7 @@ int vfs_get_field(vfs_ctx* ctx, int grid, int field, double* host) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || !host) return fail(ctx, VFS_ERR_ARG, "no such grid or null buffer");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   const size_t N = ncell(g.d);
   switch (field) {
@@ -1931,6 +1973,7 @@ int vfs_volume_flux(vfs_ctx* ctx, int grid, double out[4]) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
   launch_volume_flux(F.d, g.immersed ? 1 : 0, g.U(), F.nvert, F.M, g.parts, g.scal, g.s, g.nb8);
@@ -1943,6 +1986,7 @@ int vfs_poisson_rhs(vfs_ctx* ctx, int grid, double dt, double st, double coeff, 
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   if (!(dt > 0.)) return fail(ctx, VFS_ERR_ARG, "dt must be > 0");
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
@@ -1962,6 +2006,7 @@ int vfs_poisson_solve(vfs_ctx* ctx, int grid, const vfs_solve_params* p, vfs_sol
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   vfs_solve_info tmp{};
   int r = do_solve(ctx, *gp, p, info ? info : &tmp);
   if (r) return r;
@@ -1974,6 +2019,7 @@ int vfs_update_pressure(vfs_ctx* ctx, int grid) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
   launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s);
@@ -1985,6 +2031,7 @@ int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
   if (!ctx) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection");
   Level& F = g.lev[g.L - 1];
@@ -2020,6 +2067,7 @@ int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out) {
   if (!ctx || !out) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   Level& F = g.lev[g.L - 1];
   launch_divergence(F.d, g.U(), F.M + F.N * MP_AJ, F.nvert, g.parts, g.scal + 8, g.s, g.nb8);
@@ -2421,6 +2469,7 @@ int vfs_get_metrics(vfs_ctx* ctx, int grid, int level, double* out) {
   if (!ctx || !out) return VFS_ERR_ARG;
   Grid* g = get_grid(ctx, grid);
   if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, g)) return r_;
   Level& L = g->lev[level];
   CK(cudaMemcpy(out, L.M, MP_TOTAL * L.N * sizeof(double), cudaMemcpyDeviceToHost));
   return VFS_OK;
@@ -2430,6 +2479,7 @@ int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out) {
   if (!ctx || !out) return VFS_ERR_ARG;
   Grid* g = get_grid(ctx, grid);
   if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, g)) return r_;
   Level& L = g->lev[level];
   CK(cudaMemcpy(out, L.nvert, L.N * sizeof(double), cudaMemcpyDeviceToHost));
   return VFS_OK;
@@ -2439,6 +2489,7 @@ int vfs_get_coef(vfs_ctx* ctx, int grid, int level, int which, double* out) {
   if (!ctx || !out) return VFS_ERR_ARG;
   Grid* g = get_grid(ctx, grid);
   if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, g)) return r_;
   if (!g->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   Level& L = g->lev[level];
   if (which == 0) CK(cudaMemcpy(out, L.coef, 19 * L.N * sizeof(double), cudaMemcpyDeviceToHost));
@@ -2455,6 +2506,7 @@ int vfs_get_mg_half(vfs_ctx* ctx, int grid, int level, double* coef, double* lf,
   if (!ctx) return VFS_ERR_ARG;
   Grid* g = get_grid(ctx, grid);
   if (!g || level < 0 || level >= g->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, g)) return r_;
   if (!g->lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   Level& L = g->lev[level];
   CK(cudaStreamSynchronize(g->s));
@@ -2484,6 +2536,7 @@ int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, 
   if (!ctx || !x || !y) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || level < 0 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   Level& L = g.lev[level];
@@ -2536,7 +2589,24 @@ int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, 
     cudaFree(dx);
     cudaFree(dy);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
-  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1, 2 or 3");
+  } else if (which == 4) {
+    // the FP32 face form (11-slot levels) applied to x rounded to FP32
+    if (!face_level(L)) return fail(ctx, VFS_ERR_ARG, "the face form needs an 11-slot level");
+    std::vector<float> hx(N), hy(N);
+    for (size_t q = 0; q < N; q++) hx[q] = (float)x[q];
+    float *dx, *dy;
+    CK(cudaMalloc(&dx, N * 4));
+    CK(cudaMalloc(&dy, N * 4));
+    CK(cudaMemcpy(dx, hx.data(), N * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(dy, 0, N * 4));
+    OpView<float> A = mgview<float>(L, nullptr, false, true);
+    launch_apply_face(A, dx, dy, 0);
+    cudaError_t e = cudaMemcpy(hy.data(), dy, N * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
+    for (size_t q = 0; q < N; q++) y[q] = hy[q];
+  } else return fail(ctx, VFS_ERR_ARG, "which must be 0, 1, 2, 3 or 4");
   return VFS_OK;
 }
 
@@ -2544,6 +2614,7 @@ int vfs_mg_restrict(vfs_ctx* ctx, int grid, int level, const double* x, double* 
   if (!ctx || !x || !y) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || level < 1 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   Level &F = g.lev[level], &C = g.lev[level - 1];
   double *dx, *dy;
@@ -2563,6 +2634,7 @@ int vfs_mg_prolong(vfs_ctx* ctx, int grid, int level, const double* x, double* y
   if (!ctx || !x || !y) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || level < 1 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   Level &F = g.lev[level], &C = g.lev[level - 1];
@@ -2608,6 +2680,7 @@ int vfs_mg_smooth(vfs_ctx* ctx, int grid, int level, const double* b, double* x,
   if (!ctx || !x || !b) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp || level < 0 || level >= gp->L) return fail(ctx, VFS_ERR_ARG, "no such grid or level");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   Level& L = g.lev[level];
@@ -2632,6 +2705,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
   if (!ctx || !v || !z || !p) return VFS_ERR_ARG;
   Grid* gp = get_grid(ctx, grid);
   if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
   const size_t N = ncell(g.d);

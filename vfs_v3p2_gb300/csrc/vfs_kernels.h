@@ -24,6 +24,11 @@ int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tm
 int launch_gtensor(const Dims& d, const double* M, double* g, cudaStream_t s);
 int launch_assemble(const Dims& d, const double* g, const double* nvert, const double* aj, double* coef, double* mcoef,
                     float* mcoef32, unsigned* mask, cudaStream_t s);
+// face form of the aj-scaled operator (11-slot levels), FP32: per cell its
+// +i face (g11, k-cross weight), +k face (g33, i-cross weight), +j face
+// (g22), aj, and the one-sided code bits of the two cross terms
+int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
+                         float* fj, float* faj, uint8_t* code, cudaStream_t s);
 int launch_coarsen(const Dims& f, const Dims& c, int si, int sj, int sk, const double* coor_f, const double* nv_f,
                    double* coor_c, double* nv_c, cudaStream_t s);
 int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nv_f, const double* nv_c,
@@ -37,6 +42,8 @@ int launch_dense_inverse(const Dims& d, const double* mcoef, double sigma, doubl
 // y = A x (FP64 accumulate; x FP64 or FP32); r = b - A x when b != nullptr.
 int launch_apply64(const OpView<double>& A, const double* x, const double* b, double* y, cudaStream_t s);
 int launch_apply64_xf(const OpView<double>& A, const float* x, const double* b, double* y, cudaStream_t s);
+// y = A x with the FP32 face form of an 11-slot level (testing hook)
+int launch_apply_face(const OpView<float>& A, const float* x, float* y, cudaStream_t s);
 // multigrid operator apply in precision T (testing hook / residual)
 template <typename T>
 int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream_t s);
