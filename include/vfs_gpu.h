@@ -124,6 +124,12 @@ typedef struct {
   double cheb_hi;     /* upper end of the damped interval (default 2: T^-1 A of a
                          diagonally dominant M-matrix has its spectrum in (0, 2]) */
   double cheb_ratio;  /* cheb_hi over the lower end (default 6) */
+  int proj_exact;     /* projection of a projection step.  0 (the default): on
+                         face weights precomputed with the operator
+                         (vfs_projection_faces: the same products, applied with
+                         FMAs; within 1e-14 relative of the reference's
+                         operation order).  1: the reference's operation order
+                         bit for bit (vfs_projection). */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every
@@ -202,6 +208,16 @@ int vfs_update_pressure(vfs_ctx* ctx, int grid);
 /* Projection (poisson.c:2122-2470) on the resident Ucont, then Contra2Cart
  * (rhs.c:52-190) into the resident Ucat. */
 int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff);
+
+/* The same projection on per-face weights formed once by vfs_poisson_lhs:
+ * every regime choice of Projection (poisson.c:2221-2363: faces touching
+ * nvert skipped; each cross derivative centred, one-sided or absent) depends
+ * on the grid only, so it is folded into the weights (dot product times the
+ * face Jacobian times 0.25, 0.5 or 0) and two code bits per cross term.  The
+ * update is U -= (wN dphi_n + wA dphi_A + wB dphi_B) dt st / coeff with FMAs:
+ * about half the FP64 operations of the reference's order, no nvert reads,
+ * equal to vfs_projection within 1e-14 relative.  Then Contra2Cart. */
+int vfs_projection_faces(vfs_ctx* ctx, int grid, double dt, double st, double coeff);
 
 /* Divergence (main.c:1244-1390): max |div U| * aj over the fluid. */
 int vfs_divergence_max(vfs_ctx* ctx, int grid, double* out);
@@ -294,7 +310,8 @@ int vfs_get_level_nvert(vfs_ctx* ctx, int grid, int level, double* out);
  * the aj-scaled FP64 operator applied to x rounded to FP32 (the Krylov
  * product of the mixed-precision solve). */
 int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, double* y);
-/* One multigrid preconditioner application z = M^{-1} v on the finest level. */
+/* One multigrid preconditioner application z = M^{-1} v on the finest level,
+ * issued as the iterations of a lone solve issue it. */
 int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_params* p, const double* v, double* z);
 /* MyRestriction of level `level` (>= 1) to level-1, MyInterpolation of level-1
  * to `level` (overwrite), in FP64. */

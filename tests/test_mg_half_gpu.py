@@ -150,3 +150,25 @@ def test_mg_half_rejected_values(gpu_ctx):
                                         None)
     finally:
         gpu_ctx.grid_destroy(gid)
+
+
+def test_face_form_vcycle_matches_assembled(gpu_ctx):
+    """One FP32 V-cycle with the face form of the 11-slot levels (mg_half 0)
+    against the same V-cycle on the assembled FP32 coefficients (mg_half 2):
+    the same operator up to FP32 rounding, so the outputs agree closely."""
+    case = synth.c2_sphere(scale=4)
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    try:
+        gpu_ctx.poisson_lhs(gid)
+        rng = np.random.default_rng(3)
+        v = rng.normal(size=g.nvert.shape)
+        fl = (g.nvert < 0.1)
+        fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
+        v[~fl] = 0.0
+        z = {h: gpu_ctx.apply_precond(gid, capi.VFS_MIXED, capi.default_params(precision="mixed", mg_half=h), v)
+             for h in (0, 2)}
+        assert np.isfinite(z[0]).all()
+        assert np.abs(z[0] - z[2]).max() <= 1e-4 * np.abs(z[2]).max()
+    finally:
+        gpu_ctx.grid_destroy(gid)

@@ -230,6 +230,71 @@ def test_projection_fractional_nvert_bitexact(gpu_ctx):
     gpu_ctx.grid_destroy(gid)
 
 
+def _faces_vs_reference(gpu_ctx, gid, d, M, nv, u, phi, dt, st, coeff):
+    """vfs_projection_faces against the oracle's Projection (the reference's
+    operation order) for the same phi: equal to rounding, every face the
+    reference leaves alone unchanged bit for bit."""
+    u_ref = u.copy()
+    O.projection(d, M, nv, phi, u_ref, dt=dt, st=st, coeff=coeff)
+    gpu_ctx.set_field(gid, capi.FIELD_UCONT, u)
+    gpu_ctx.L.vfs_set_field(gpu_ctx.h, gid, capi.FIELD_PHI, capi.dptr(phi))
+    gpu_ctx.projection(gid, dt=dt, st=st, coeff=coeff, faces=True)
+    u_got = gpu_ctx.get_field(gid, capi.FIELD_UCONT, u.shape)
+    # per component: FMAs and the pair sums' order against the reference's
+    # left-to-right sums, relative to the flux and its correction
+    scale = np.abs(u).max() + np.abs(u_ref - u).max()
+    assert np.abs(u_got - u_ref).max() <= 1e-14 * scale
+    untouched = u_ref == u
+    assert np.array_equal(u_got[untouched], u[untouched])
+    dv = O.divergence(d, u_ref, O.metric(M, d, "aj"), nv)
+    dg = gpu_ctx.divergence_max(gid)
+    assert abs(dg - dv) <= 1e-12 * max(dv, 1e-300) + 1e-14 * scale
+
+
+def test_projection_faces_matches_reference_order(gpu_ctx, loaded):
+    case, gid, d, mg = loaded
+    g = case.grid
+    M = O.form_metrics(d, g.coor)
+    rng = np.random.default_rng(81)
+    for dt, st, coeff in ((0.04, 1.0, 1.0), (0.013, 0.5, 1.5)):
+        phi = rng.normal(size=g.nvert.shape) * 10.0
+        O.phi_finish(d, g.nvert, phi)
+        _faces_vs_reference(gpu_ctx, gid, d, M, g.nvert, case.ucont.copy(), phi, dt, st, coeff)
+
+
+@pytest.mark.parametrize("kind", ["fractional", "walled", "terrain"])
+def test_projection_faces_other_grids(gpu_ctx, kind):
+    """The face-weight projection on grids whose regime choices differ from
+    the channel's: fractional nvert (the FP64 nvert tests), walls on every
+    side (no periodic seam) and the stretched terrain grid."""
+    if kind == "terrain":
+        case = synth.c3_terrain(scale=8)
+        g = case.grid
+        nv = g.nvert
+    else:
+        case = synth.channel_case(32, 16, 16, seed=15, spheres=[(math.pi, 0.0, math.pi / 2, 0.6)], sigma=0.5,
+                                  levels=3)
+        g = case.grid
+        nv = g.nvert * 0.35 if kind == "fractional" else g.nvert
+    desc_periodic = kind != "walled"
+    if desc_periodic:
+        gid = gpu_ctx.grid_create(g.coor, nv, case.levels, case.immersed)
+        d = O.dims_of(g)
+    else:
+        gid = gpu_ctx.grid_create(g.coor, nv, case.levels, case.immersed, periodic=(0, 0, 0))
+        mz, my, mx = nv.shape
+        d = O.Dims(mx, my, mz, 0, 0, 0)
+    try:
+        gpu_ctx.poisson_lhs(gid)
+        M = O.form_metrics(d, g.coor)
+        rng = np.random.default_rng(82)
+        phi = rng.normal(size=nv.shape)
+        O.phi_finish(d, nv, phi)
+        _faces_vs_reference(gpu_ctx, gid, d, M, nv, case.ucont.copy(), phi, 0.04, 1.0, 1.0)
+    finally:
+        gpu_ctx.grid_destroy(gid)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp16_operator", "mixed_fp32_assembled"])
 @pytest.mark.parametrize("orth", ["cgs", "cgs2"])
 def test_full_step_parity(gpu_ctx, loaded, precision, orth):

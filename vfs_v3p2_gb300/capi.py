@@ -65,7 +65,7 @@ class SolveParams(ctypes.Structure):
                 ("omega", ctypes.c_double), ("warm_start", ctypes.c_int), ("div_tol", ctypes.c_double),
                 ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
                 ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int), ("smoother", ctypes.c_int),
-                ("cheb_hi", ctypes.c_double), ("cheb_ratio", ctypes.c_double)]
+                ("cheb_hi", ctypes.c_double), ("cheb_ratio", ctypes.c_double), ("proj_exact", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -113,6 +113,7 @@ SIGNATURES = {
     "vfs_poisson_solve": ([_P, _I, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo)], _I),
     "vfs_update_pressure": ([_P, _I], _I),
     "vfs_projection": ([_P, _I, _D, _D, _D], _I),
+    "vfs_projection_faces": ([_P, _I, _D, _D, _D], _I),
     "vfs_divergence_max": ([_P, _I, _DP], _I),
     "vfs_divergence_max_noalloc": ([_I, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, ctypes.c_char_p, _I], _I),
     "vfs_projection_step": ([_P, _I, _DP, _DP, _D, _D, _D, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveInfo),
@@ -318,8 +319,9 @@ class Context:
     def update_pressure(self, g: int):
         self.check(self.L.vfs_update_pressure(self.h, g))
 
-    def projection(self, g: int, dt=0.04, st=1.0, coeff=1.0):
-        self.check(self.L.vfs_projection(self.h, g, dt, st, coeff))
+    def projection(self, g: int, dt=0.04, st=1.0, coeff=1.0, faces: bool = False):
+        fn = self.L.vfs_projection_faces if faces else self.L.vfs_projection
+        self.check(fn(self.h, g, dt, st, coeff))
 
     def divergence_max(self, g: int) -> float:
         v = ctypes.c_double()

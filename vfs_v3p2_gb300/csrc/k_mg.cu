@@ -205,6 +205,38 @@ __device__ __forceinline__ float face_row(const FaceData& f, const float* x) {
   const float Fj = f.gjc * (xn - xc) - f.gjs * (xc - xs);
   return f.aj * ((Fic - Fiw) + Fj + (Fkc - Fkb));
 }
+// The face data and the 11 stencil values of interior cell (i, j, k), every
+// load issued before any arithmetic (periodic wraps as in stencil_gather).
+__device__ __forceinline__ void face_gather(const OpView<float>& A, const float* __restrict__ x, int i, int j, int k,
+                                            FaceData& f, float* xv) {
+  const Dims d = A.d;
+  const int sy = d.mx, sz = d.mx * d.my;
+  const int c = k * sz + j * sy + i;
+  const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
+  const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
+  const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
+  f.fic = __ldg(A.ffi + c);
+  f.fiw = __ldg(A.ffi + c + oiW);
+  f.fkc = __ldg(A.ffk + c);
+  f.fkb = __ldg(A.ffk + c + okB);
+  f.gjc = __ldg(A.ffj + c);
+  f.gjs = __ldg(A.ffj + c + ojS);
+  f.aj = __ldg(A.faj + c);
+  f.cc = __ldg(A.fcode + c);
+  f.cw = __ldg(A.fcode + c + oiW);
+  f.cb = __ldg(A.fcode + c + okB);
+  xv[CP] = __ldg(x + c);
+  xv[EP] = __ldg(x + c + oiE);
+  xv[WP] = __ldg(x + c + oiW);
+  xv[NP] = __ldg(x + c + ojN);
+  xv[SP] = __ldg(x + c + ojS);
+  xv[TP] = __ldg(x + c + okT);
+  xv[BP] = __ldg(x + c + okB);
+  xv[TE] = __ldg(x + c + okT + oiE);
+  xv[BE] = __ldg(x + c + okB + oiE);
+  xv[TW] = __ldg(x + c + okT + oiW);
+  xv[BW] = __ldg(x + c + okB + oiW);
+}
 
 // ---------------------------------------------------------------------------
 // FP64 outer operator: y = A x, or y = b - A x.
@@ -287,28 +319,10 @@ __global__ void __launch_bounds__(TX* TY) k_apply_face(OpView<float> A, const fl
                                                        float* __restrict__ y) {
   TILE_LOOP(A.d) {
     if (!_in) continue;
-    const Dims d = A.d;
-    const int sy = d.mx, sz = d.mx * d.my;
-    const int c = k * sz + j * sy + i;
-    const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
-    const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
-    const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
     FaceData f;
-    f.fic = A.ffi[c];
-    f.fiw = A.ffi[c + oiW];
-    f.fkc = A.ffk[c];
-    f.fkb = A.ffk[c + okB];
-    f.gjc = A.ffj[c];
-    f.gjs = A.ffj[c + ojS];
-    f.aj = A.faj[c];
-    f.cc = A.fcode[c];
-    f.cw = A.fcode[c + oiW];
-    f.cb = A.fcode[c + okB];
     float xv[19];
-    xv[CP] = x[c]; xv[EP] = x[c + oiE]; xv[WP] = x[c + oiW]; xv[NP] = x[c + ojN]; xv[SP] = x[c + ojS];
-    xv[TP] = x[c + okT]; xv[BP] = x[c + okB]; xv[TE] = x[c + okT + oiE]; xv[BE] = x[c + okB + oiE];
-    xv[TW] = x[c + okT + oiW]; xv[BW] = x[c + okB + oiW];
-    y[c] = face_row(f, xv);
+    face_gather(A, x, i, j, k, f, xv);
+    y[cidx(A.d, i, j, k)] = face_row(f, xv);
   }
 }
 int launch_apply_face(const OpView<float>& A, const float* x, float* y, cudaStream_t s) {
@@ -507,17 +521,17 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
 template <int U, bool ZG>
 __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float* __restrict__ lf,
                                             const float* __restrict__ xi, const float* __restrict__ b, float* su,
-                                            float* sp, float* sl, int i0, int k, int TW) {
+                                            float* sp, float* sl, int i0, int k, int tw) {
   const Dims d = A.d;
   const int nj = d.my - 2, sy = d.mx, sz = d.mx * d.my;
   const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
-  for (int base = threadIdx.x; base < TW * nj; base += U * VFS_SMOOTH_NT) {
+  for (int base = threadIdx.x; base < tw * nj; base += U * VFS_SMOOTH_NT) {
     FaceData f[U];
     float xv[U][11], bb[U], inv[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int idx = min(base + u * VFS_SMOOTH_NT, TW * nj - 1);
-      const int il = idx % TW, jl = idx / TW;
+      const int idx = min(base + u * VFS_SMOOTH_NT, tw * nj - 1);
+      const int il = idx % tw, jl = idx / tw;
       const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
       const int c = k * sz + j * sy + i;
       const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
@@ -551,10 +565,10 @@ __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float*
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int idx = base + u * VFS_SMOOTH_NT;
-      if (idx >= TW * nj) break;
-      const int jl = idx / TW;
-      const bool live = (i0 + idx % TW <= d.mx - 2) && f[u].aj != 0.f;
-      float x11[19];  // slot-indexed view of the 11 values
+      if (idx >= tw * nj) break;
+      const int jl = idx / tw;
+      const bool live = (i0 + idx % tw <= d.mx - 2) && f[u].aj != 0.f;
+      float x11[19];  // slot-indexed view of the 11 values (TE, BE, TW, BW: the stencil slots)
       if (!ZG) {
         x11[CP] = xv[u][0]; x11[EP] = xv[u][1]; x11[WP] = xv[u][2]; x11[NP] = xv[u][3]; x11[SP] = xv[u][4];
         x11[TP] = xv[u][5]; x11[BP] = xv[u][6]; x11[TE] = xv[u][7]; x11[BE] = xv[u][8]; x11[TW] = xv[u][9];
@@ -1098,10 +1112,17 @@ __global__ void __launch_bounds__(256, VFS_STENCIL_MINB) k_resrestrict_tiled(OpV
     const T bv = b[fc];
     T ax = T(0);
     if (x) {
-      TC cv[19];
-      T xv[19];
-      gather<MASK>(f, coef, x, fic, fjc, fk, cv, xv);
-      ax = row_dot<MASK, T>(cv, xv);
+      if constexpr (std::is_same<TC, FaceOp>::value) {
+        FaceData fd;
+        float xv[19];
+        face_gather(A, x, fic, fjc, fk, fd, xv);
+        ax = face_row(fd, xv);
+      } else {
+        TC cv[19];
+        T xv[19];
+        gather<MASK>(f, coef, x, fic, fjc, fk, cv, xv);
+        ax = row_dot<MASK, T>(cv, xv);
+      }
     }
     const T rr = (bv - ax) * w;
     sr[kk][ty][ii] = (w != T(0) && fi <= f.mx - 2 && fj <= f.my - 2) ? rr : T(0);
@@ -1144,7 +1165,11 @@ int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T
                              const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
   bool done = false;
   if constexpr (sizeof(T) == 4) {
-    if (A.hcoef) {
+    if (A.ffi && fits_ch(A.mask) && !si && !sj && !sk) {
+      dim3 g((c.mx - 2 + 31) / 32, (c.my - 2 + 3) / 4, c.mz - 2);
+      k_resrestrict_tiled<MASK_CH, T, FaceOp><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+      done = true;
+    } else if (A.hcoef) {
       launch_resrestrict_tc<T, __half>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc, s);
       done = true;
     }

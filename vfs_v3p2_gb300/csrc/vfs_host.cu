@@ -153,6 +153,8 @@ struct Grid {
   int L = 1, si = 0, sj = 0, sk = 0, immersed = 0;
   Level lev[MAXLEV];
   double* pd = nullptr;
+  double* pw = nullptr;     // projection face weights (9, see launch_proj_weights)
+  uint16_t* pc = nullptr;   // projection cross-term codes
   double* minv = nullptr;   // per-cell inverse metric / 2 (9, row-major), Contra2Cart
   uint8_t* nb8 = nullptr;   // nvert as bytes when all are integers in [0, 127], else null
   uint8_t* nb8_buf = nullptr;  // storage behind nb8
@@ -556,8 +558,10 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   {
     // the slots, x, b and the restriction weights read; the coarse right-hand
     // side and the cleared coarse x written
+    const bool face_rr = A.ffi && !g.si && !g.sj && !g.sk;  // the face form's restriction (tiled form only)
     Probed pr(VFS_PROBE_ALL, s, "k_resrestrict", l,
-              nf * (slot_bytes * popcount(A.mask) + 3.0 * sizeof(T)) + 2.0 * n_interior(C.d) * sizeof(T));
+              nf * ((face_rr ? 25.0 : slot_bytes * popcount(A.mask)) + 3.0 * sizeof(T)) +
+                  2.0 * n_interior(C.d) * sizeof(T));
     dbg("residual_restrict", l,
         launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0],
                                     s),
@@ -629,12 +633,14 @@ MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
 // with_input == false: the finest-level input buffer already holds T(v).
 template <typename T>
 int precond(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, const double* v, T* z, T* tmp, const int* skip,
-            cudaStream_t s, bool with_input = true) {
+            cudaStream_t s, bool with_input = true, bool solo = false) {
   Level& F = g.lev[g.L - 1];
   T* bf = bbuf<T>(F);
-  const float* dinv = dinv_sel<T>(F, mgcfg(p, g.L - 1, g.half_ok).half);
+  MGCfg mc = mgcfg(p, g.L - 1, g.half_ok);
+  mc.solo = solo;
+  const float* dinv = dinv_sel<T>(F, mc.half);
   if (with_input) dbg("scale_in", g.L - 1, launch_scale_in<T>(F.d, nullptr, v, bf, skip, s, dinv), s);
-  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mgcfg(p, g.L - 1, g.half_ok), skip, s);
+  T* res = vcycle<T>(g, g.L - 1, bf, z, tmp, mc, skip, s);
   if (res != z) CK(cudaMemcpyAsync(z, res, F.N * sizeof(T), cudaMemcpyDeviceToDevice, s));
   return VFS_OK;
 }
@@ -929,6 +935,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (!(p->omega > 0. && p->omega < 2.)) return fail(ctx, VFS_ERR_ARG, "omega must be in (0, 2)");
   if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
+  if (p->proj_exact != 0 && p->proj_exact != 1) return fail(ctx, VFS_ERR_ARG, "proj_exact must be 0 or 1");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
@@ -969,8 +976,8 @@ int transfer_slabs(size_t ncells) {
   return (int)std::max<size_t>(1, std::min<size_t>(8, b >> 22));
 }
 
-int step_post(Grid& g, double dt, double st, double coeff, double* u_out = nullptr, double* p_out = nullptr,
-              bool p_in_pending = false);
+int step_post(Grid& g, double dt, double st, double coeff, bool exact, double* u_out = nullptr,
+              double* p_out = nullptr, bool p_in_pending = false);
 
 struct Job {
   Grid* g = nullptr;
@@ -1124,7 +1131,7 @@ int job_check_eval(vfs_ctx* ctx, Job& J) {
     }
     CK(cudaEventRecord(g.t1, s));
     if (J.post) {
-      const int rp = step_post(g, J.dt, J.st, J.coeff, J.u_out, J.p_out, J.p_in_pending);
+      const int rp = step_post(g, J.dt, J.st, J.coeff, J.p.proj_exact != 0, J.u_out, J.p_out, J.p_in_pending);
       J.p_in_pending = false;
       if (rp) return job_fail(ctx, J, cuda_fail(ctx, (cudaError_t)rp, "step outputs"));
       CK(cudaMemcpyAsync(g.hv + 2, g.scal + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1479,7 +1486,7 @@ size_t level_bytes(const Dims& d, bool finest) {
   b += 19 * 2 * hslot(d) + N * (4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
   b += N * (8 + 8 + 4 + 4 + 1);               // face form: ffi ffk ffj faj fcode
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
-  if (finest) b += N * 8 * (9 + 9 + 3 + 3 + 3 + 3 + 3) + N;           // pd minv u ustar p phi b ucat aos nb8
+  if (finest) b += N * 8 * (9 + 9 + 9 + 3 + 3 + 3 + 3 + 3) + N * 3;  // pd pw minv u ustar p phi b ucat aos, nb8 pc
   return b;
 }
 
@@ -1509,6 +1516,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->nu1_coarse = -1;
   p->nu2_coarse = -1;
   p->mg_half = 0;
+  p->proj_exact = 0;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -1660,6 +1668,8 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
   const size_t N = ncell(d);
   GAB(tmp, 9 * N);
   GAB(g.pd, 9 * N);
+  GAB(g.pw, 9 * N);
+  GAB(g.pc, N);
   GAB(g.minv, 9 * N);
   GAB(g.u, 3 * N);
   GAB(g.ustar, 3 * N);
@@ -1830,6 +1840,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
                                  g.lev[l - 1].mcoef, g.lev[l].rwh, g.s);
   Level& F = g.lev[g.L - 1];
   launch_proj_dots(F.d, F.M, g.pd, g.s);
+  launch_proj_weights(F.d, g.pd, F.M, F.nvert, g.pw, g.pc, g.s);
   unsigned range = 0;
   CK(cudaMemcpyAsync(&range, dmask + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
   CK(cudaStreamSynchronize(g.s));
@@ -2041,6 +2052,20 @@ int vfs_projection(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
   return VFS_OK;
 }
 
+int vfs_projection_faces(vfs_ctx* ctx, int grid, double dt, double st, double coeff) {
+  if (!ctx) return VFS_ERR_ARG;
+  Grid* gp = get_grid(ctx, grid);
+  if (!gp) return fail(ctx, VFS_ERR_ARG, "no such grid");
+  if (int r_ = check_idle(ctx, gp)) return r_;
+  Grid& g = *gp;
+  if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs must run before the projection");
+  Level& F = g.lev[g.L - 1];
+  launch_projection_fast(F.d, g.pw, g.pc, g.phi, dt, st, coeff, g.U(), g.s);
+  launch_contra2cart(F.d, g.minv, F.nvert, g.U(), g.ucat, g.s);
+  CK(cudaStreamSynchronize(g.s));
+  return VFS_OK;
+}
+
 int vfs_divergence_max_noalloc(int device, int mx, int my, int mz, int i_periodic, int j_periodic, int k_periodic,
                                const double* ucont_x, const double* ucont_y, const double* ucont_z, const double* aj,
                                const double* nvert, double* out, void* stream, char* err, int err_len) {
@@ -2110,7 +2135,8 @@ void step_pre(Grid& g, double dt, double st, double coeff) {
 // Contra2Cart and the divergence check); the main stream then waits for the
 // copies.  p_in_pending: the pressure upload of the step (on the copy
 // stream, overlapping the solve) must land before the update.
-int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double* p_out, bool p_in_pending) {
+int step_post(Grid& g, double dt, double st, double coeff, bool exact, double* u_out, double* p_out,
+              bool p_in_pending) {
   Level& F = g.lev[g.L - 1];
   const size_t N = ncell(g.d);
   cudaError_t e = cudaSuccess;
@@ -2125,16 +2151,22 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     dbg("update_pressure", 0, launch_update_pressure(F.d, F.nvert, g.phi, g.p, g.s), g.s);
   }
   // projection: the 9 metric products, 3 face Jacobians, nvert bytes (or
-  // doubles) and phi read, U read and written
-  const double proj_b = 9 * 8.0 + 24.0 + (g.nb8 ? 1.0 : 8.0) + 8.0 + 48.0;
+  // doubles) and phi read, U read and written; on face weights: the 9
+  // weights, the code and phi read, U read and written
+  const double proj_b = exact ? 9 * 8.0 + 24.0 + (g.nb8 ? 1.0 : 8.0) + 8.0 + 48.0 : 9 * 8.0 + 2.0 + 8.0 + 48.0;
+  const char* proj_name = exact ? "k_projection" : "k_projection_fast";
+  auto project = [&](int k0, int k1) {
+    return exact ? launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s, k0, k1)
+                 : launch_projection_fast(F.d, g.pw, g.pc, g.phi, dt, st, coeff, g.U(), g.s, k0, k1);
+  };
   if (p_out) {
     ok(cudaEventRecord(g.ev_p, g.s));
     ok(cudaStreamWaitEvent(g.cs, g.ev_p, 0));
     ok(cudaMemcpyAsync(p_out, g.p, N * sizeof(double), cudaMemcpyDeviceToHost, g.cs));
   }
   if (!u_out) {
-    Probed pr(VFS_PROBE_ALL, g.s, "k_projection", g.L - 1, Nd * proj_b);
-    dbg("projection", 0, launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s), g.s);
+    Probed pr(VFS_PROBE_ALL, g.s, proj_name, g.L - 1, Nd * proj_b);
+    dbg("projection", 0, project(0, -1), g.s);
   } else {
     // Interior planes in slabs: a slab is projected and converted to AoS on
     // the step stream and goes down on the copy stream while the next one
@@ -2156,9 +2188,8 @@ int step_post(Grid& g, double dt, double st, double coeff, double* u_out, double
     for (int q = 0; q < S; q++) {
       const int k0 = 1 + (int)((long long)inner * q / S), k1 = 1 + (int)((long long)inner * (q + 1) / S);
       {
-        Probed pr(VFS_PROBE_ALL, g.s, "k_projection", g.L - 1, (double)(k1 - k0) * P * proj_b);
-        dbg("projection", 0,
-            launch_projection(F.d, g.pd, F.M, F.nvert, g.nb8, g.phi, dt, st, coeff, g.U(), g.s, k0, k1), g.s);
+        Probed pr(VFS_PROBE_ALL, g.s, proj_name, g.L - 1, (double)(k1 - k0) * P * proj_b);
+        dbg("projection", 0, project(k0, k1), g.s);
       }
       to_aos(k0, k1);
       ok(cudaEventRecord(g.ev_u, g.s));
@@ -2719,7 +2750,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     float* dz = nullptr;
     if (!r && cudaMalloc(&dz, N * 4) != cudaSuccess) r = VFS_ERR_NOMEM;
     if (!r) cudaMemsetAsync(dz, 0, N * 4, g.s);
-    if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s);
+    if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s, true, true);
     if (!r) {
       std::vector<float> hz(N);
       cudaStreamSynchronize(g.s);
@@ -2732,7 +2763,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     double* dz = nullptr;
     if (!r && cudaMalloc(&dz, N * 8) != cudaSuccess) r = VFS_ERR_NOMEM;
     if (!r) cudaMemsetAsync(dz, 0, N * 8, g.s);
-    if (!r) r = precond<double>(ctx, g, *p, dv, dz, F.x64[1], nullptr, g.s);
+    if (!r) r = precond<double>(ctx, g, *p, dv, dz, F.x64[1], nullptr, g.s, true, true);
     if (!r) {
       cudaStreamSynchronize(g.s);
       cudaMemcpy(z, dz, N * 8, cudaMemcpyDeviceToHost);

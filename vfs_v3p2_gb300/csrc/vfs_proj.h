@@ -39,6 +39,13 @@ int launch_proj_dots(const Dims& d, const double* M, double* pd, cudaStream_t s)
 int launch_projection(const Dims& d, const double* pd, const double* M, const double* nvert, const uint8_t* nb8,
                       const double* phi, double dt, double st, double coeff, const Ucont& u, cudaStream_t s,
                       int k0 = 0, int k1 = -1);
+// The same projection on face weights and cross-term codes precomputed by
+// launch_proj_weights (pw [9][N], pc [N]): FMAs, no nvert tests; equal to
+// the reference's operation order to rounding (<= 1e-14 relative).
+int launch_proj_weights(const Dims& d, const double* pd, const double* M, const double* nvert, double* pw, uint16_t* pc,
+                        cudaStream_t s);
+int launch_projection_fast(const Dims& d, const double* pw, const uint16_t* pc, const double* phi, double dt, double st,
+                           double coeff, const Ucont& u, cudaStream_t s, int k0 = 0, int k1 = -1);
 // periodic ghost sync of the Ucont components on planes [k0, k1)
 int launch_ucont_ghosts(const Dims& d, const Ucont& u, int k0, int k1, cudaStream_t s);
 // minv: per-cell inverse of the metric matrix [csi; eta; zet] (9 doubles,
