@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import shlex
 import shutil
 import subprocess
 import sys
@@ -42,7 +43,10 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC, "-I", os.path.join(ROOT, "include")] + ARCH
+    # VFS_NVCC_FLAGS: extra nvcc flags (compile-time tuning knobs such as
+    # -DVFS_SMOOTH_PF_FACE=2; rebuild with --force after changing it)
+    extra = shlex.split(os.environ.get("VFS_NVCC_FLAGS", ""))
+    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", SRC, "-I", os.path.join(ROOT, "include")] + ARCH + extra
 
 
 def _compile(unit: str, extra, verbose: bool):

@@ -368,7 +368,8 @@ int launch_apply_face(const OpView<float>& A, const float* x, float* y, cudaStre
 #define VFS_SMOOTH_PF 1  // phase-1 rows prefetched into L2 this many iterations ahead (0: off), FP32 operator
 #endif
 #ifndef VFS_SMOOTH_PF_HALF
-#define VFS_SMOOTH_PF_HALF 0  // the same for the FP16 operator (measured: the prefetches cost more than they save)
+#define VFS_SMOOTH_PF_HALF 0  // the same for the FP16 operator and the face form (measured: the prefetches cost more
+                              // than they save; face form 55.4 -> 78 us per finest sweep one to three row bands ahead)
 #endif
 #ifndef VFS_SMOOTH_MINBLK
 #define VFS_SMOOTH_MINBLK 152  // automatic tile: narrow while a sweep has fewer blocks (one per SM)
