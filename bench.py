@@ -339,9 +339,11 @@ def run_batch(args, dist, local, ws):
         ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
         ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
         ids.append(gid)
-    tuned = None
-    if not args.no_tune:
-        plist, tuned = autotune.tuned_params_batch(ctx, ids, cases, base)
+    tuned, tune_s = None, 0.0
+    if not args.no_tune:  # every grid tuned alone (its smoothing schedule), before the timed steps
+        t0 = time.perf_counter()
+        plist, tuned = autotune.tuned_params_grids(ctx, ids, cases, base)
+        tune_s = time.perf_counter() - t0
     else:
         plist = [base] * len(ids)
     for _ in range(args.warmup):
@@ -395,6 +397,7 @@ def run_batch(args, dist, local, ws):
                        "measures": "batched pressure projection steps/s (64 uneven grids, one graph launch per "
                                    "FGMRES iteration), mixed FP32-MG/FP64-FGMRES",
                        "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": not args.no_tune,
+                       "autotune_s": tune_s,
                        "mg_operator": OPERATOR[base.mg_half],
                        "timer": "host wall clock around synchronous batch calls (results on the host)",
                        "parallelism": f"replicas x{ws}"},
@@ -422,9 +425,11 @@ def run_serve(args, dist, local, ws):
     ctx = capi.Context(local, hbm_budget_bytes=120 * 10**9, max_inflight=16)
     params = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400,
                                  restart=args.restart, warm_start=1)
-    tuned = None
-    if not args.no_tune:  # per size class, single-grid latency objective
-        plist, tuned = autotune.tuned_params(ctx, [s.case for s in streams], params)
+    tuned, tune_s = None, 0.0
+    if not args.no_tune:  # every stream's grid tuned alone, single-grid latency objective
+        t0 = time.perf_counter()
+        plist, tuned = autotune.tuned_params_cases(ctx, [s.case for s in streams], params)
+        tune_s = time.perf_counter() - t0
         for s, p in zip(streams, plist):
             s.params = p
     srv = serve.Server(ctx, streams, params)
@@ -476,7 +481,7 @@ def run_serve(args, dist, local, ws):
                                    "continuous batching), mixed FP32-MG/FP64-FGMRES",
                        "requests": len(recs), "hbm_budget_gb": 120, "max_inflight": 16,
                        "mg_operator": OPERATOR[params.mg_half], "rtol": args.rtol,
-                       "div_tol": args.div_tol, "autotuned": not args.no_tune,
+                       "div_tol": args.div_tol, "autotuned": not args.no_tune, "autotune_s": tune_s,
                        "timer": "host wall clock, first arrival to last result",
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * summ["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -521,8 +526,9 @@ def smoother_config(args) -> dict:
 
 def compact_single(args, dist, local, ws, config):
     """Mixed and plain FP64 steps/s of one single-grid workload (U* resident,
-    the headline's stopping rule and smoother), for the default line."""
-    from vfs_v3p2_gb300 import capi
+    the headline's stopping rule; the smoothing schedule the autotuner picks
+    for the grid, the same in both precisions), for the default line."""
+    from vfs_v3p2_gb300 import autotune, capi
     a = argparse.Namespace(**vars(args))
     a.config, a.grid, a.scale = config, None, 1
     case = make_case(a)
@@ -533,9 +539,14 @@ def compact_single(args, dist, local, ws, config):
     ctx.set_field(gid, capi.FIELD_USTAR, case.ucont)
     ctx.set_field(gid, capi.FIELD_P, np.zeros(g.nvert.shape))
     out = {"workload": WORKLOAD[config], "grid": case.name, "mg_levels": case.levels}
+    base = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400)
+    t0 = time.perf_counter()
+    cand, _ = autotune.tune_resident(ctx, gid, case, base, steps=2)
+    out["autotuned"] = {**autotune.candidate_entry(cand), "autotune_s": time.perf_counter() - t0}
+    autotune.apply_candidate(base, cand)
     K = 20
     for prec in ("mixed", "fp64"):
-        params = capi.default_params(precision=prec, rtol=args.rtol, div_tol=args.div_tol, maxit=400)
+        params = autotune.with_precision(base, capi.VFS_MIXED if prec == "mixed" else capi.VFS_FP64)
         for _ in range(3):
             ctx.projection_step(gid, params)
         barrier(dist)
@@ -556,25 +567,29 @@ def compact_single(args, dist, local, ws, config):
 
 
 def compact_workloads(args, dist, local, ws):
-    """The channel, batched and served workloads in short runs (default
-    solver parameters, no autotuning), so that one default bench line records
-    every configuration; --config batch / serve give the full runs."""
+    """The channel, batched and served workloads in short runs, so that one
+    default bench line records every configuration; --config batch / serve
+    give the full runs.  Every grid runs the smoothing schedule the autotuner
+    picks for it (tuned once, before the timed steps; the FP64 runs use the
+    same schedules)."""
     out = {"channel_64x64x64": compact_single(args, dist, local, ws, "channel")}
     b = argparse.Namespace(**vars(args))
-    b.steps, b.warmup, b.no_tune, b.no_fp64, b.scale = 3, 1, True, False, 1
+    b.steps, b.warmup, b.no_tune, b.no_fp64, b.scale = 3, 1, False, False, 1
     bl = run_batch(b, dist, local, ws)
     out["batch_64_grids"] = {"workload": WORKLOAD["batch"], "value": bl["value"], "unit": "solves/s",
                              "steps": bl["steps"], "latency_ms": bl["latency_ms"], "divmax": bl["divmax"],
-                             "iterations": bl["iterations"], "autotuned": False,
+                             "iterations": bl["iterations"], "autotuned": True,
+                             "autotune_s": bl["config"]["autotune_s"],
                              "fp64_batched": bl["fp64"]["batched"]["value"],
                              "mixed_over_fp64_batched": bl["fp64"]["mixed_batched_over_fp64_batched"],
                              "fp64_divmax": bl["fp64"]["batched"]["divmax"]}
     v = argparse.Namespace(**vars(args))
-    v.requests, v.warmup, v.no_tune, v.no_fp64, v.scale = 200, 1, True, False, 1
+    v.requests, v.warmup, v.no_tune, v.no_fp64, v.scale = 200, 1, False, False, 1
     sl = run_serve(v, dist, local, ws)
     out["serve_16_streams"] = {"workload": WORKLOAD["serve"], "value": sl["value"], "unit": "solves/s",
                                "requests": sl["steps"], "rate_req_s": v.rate, "latency_ms": sl["latency_ms"],
-                               "divmax": sl["divmax"], "failed": sl["failed"], "autotuned": False,
+                               "divmax": sl["divmax"], "failed": sl["failed"], "autotuned": True,
+                               "autotune_s": sl["config"]["autotune_s"],
                                "fp64_latency_ms": sl["fp64"]["latency_ms"], "fp64_divmax": sl["fp64"]["divmax"],
                                "capacity_solves_per_s": sl["fp64"]["capacity_solves_per_s"]}
     return out

@@ -28,6 +28,7 @@ def test_candidate_roundtrip(cand):
     assert p.omega == pytest.approx(cand[2])
     assert p.nu1_coarse == p.nu2_coarse == cand[4]
     assert p.smoother == autotune.SMOOTHERS[cand[5]]
+    assert p.cheb_ratio == pytest.approx(cand[6])
     # untouched: the caller's tolerances and warm start
     assert (p.rtol, p.div_tol, p.warm_start) == (1e-7, 1e-8, 1)
     assert autotune.entry_candidate(autotune.candidate_entry(cand)) == cand
@@ -40,7 +41,7 @@ def test_candidate_roundtrip(cand):
 
 def test_entry_without_smoother_is_jacobi():
     e = {"nu1": 3, "nu2": 3, "omega": 0.9, "smooth_cols": 0, "nu_coarse": 5}
-    assert autotune.entry_candidate(e) == (3, 3, 0.9, 0, 5, "jacobi")
+    assert autotune.entry_candidate(e) == (3, 3, 0.9, 0, 5, "jacobi", 6.0)
 
 
 def test_with_precision_keeps_settings():

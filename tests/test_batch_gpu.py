@@ -127,3 +127,24 @@ def test_autotune_batch_objective(gpu_ctx):
     finally:
         for gid in ids:
             gpu_ctx.grid_destroy(gid)
+
+
+def test_autotune_per_grid(gpu_ctx):
+    """Every grid tuned alone: each picks a candidate of the list, and the
+    batch with the per-grid schedules converges to the divergence target."""
+    from vfs_v3p2_gb300 import autotune
+    cases = _cases()[:3]
+    ids = _load(gpu_ctx, cases)
+    try:
+        for gid, c in zip(ids, cases):
+            _reset(gpu_ctx, gid, c)
+        base = capi.default_params(rtol=1e-9, div_tol=1e-8)
+        plist, table = autotune.tuned_params_grids(gpu_ctx, ids, cases, base, steps=1)
+        assert set(table) == {c.name for c in cases}
+        for e in table.values():
+            assert autotune.entry_candidate(e) in autotune.CANDIDATES and e["ms_per_step"] < float("inf")
+        infos, dm = gpu_ctx.projection_step_batch(ids, plist)
+        assert all(i["converged"] for i in infos) and (dm < 1e-8).all()
+    finally:
+        for gid in ids:
+            gpu_ctx.grid_destroy(gid)
