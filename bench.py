@@ -72,6 +72,8 @@ def parse():
                     help="multigrid operator storage: FP32 face form on 11-slot levels (0), FP16 normalised by "
                          "the diagonal (1), FP32 assembled coefficients (2); FP32 arithmetic in every case")
     ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--mg-grouped", type=int, default=0, choices=[0, 1],
+                    help="batch: V-cycles as grouped launches over same-size grids (1) or each grid's own (0)")
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -331,7 +333,8 @@ def run_batch(args, dist, local, ws):
     sc = max(1, args.scale)
     cases = synth.c4_batch(64, seed=1004, lo=(32 // sc, 32 // sc, 32 // sc), hi=(192 // sc, 96 // sc, 96 // sc))
     ctx = capi.Context(local)
-    base = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400, restart=args.restart)
+    base = capi.default_params(precision="mixed", rtol=args.rtol, div_tol=args.div_tol, maxit=400, restart=args.restart,
+                               mg_grouped=args.mg_grouped)
     ids = []
     for c in cases:
         gid = ctx.grid_create(c.grid.coor, c.grid.nvert, c.levels, c.immersed)
@@ -397,7 +400,7 @@ def run_batch(args, dist, local, ws):
                        "measures": "batched pressure projection steps/s (64 uneven grids, one graph launch per "
                                    "FGMRES iteration), mixed FP32-MG/FP64-FGMRES",
                        "rtol": args.rtol, "div_tol": args.div_tol, "autotuned": not args.no_tune,
-                       "autotune_s": tune_s,
+                       "autotune_s": tune_s, "mg_grouped": args.mg_grouped,
                        "mg_operator": OPERATOR[base.mg_half],
                        "timer": "host wall clock around synchronous batch calls (results on the host)",
                        "parallelism": f"replicas x{ws}"},

@@ -130,6 +130,18 @@ typedef struct {
                          FMAs; within 1e-14 relative of the reference's
                          operation order).  1: the reference's operation order
                          bit for bit (vfs_projection). */
+  int mg_grouped;     /* batched solves (vfs_projection_step_batch): 1: the
+                         V-cycles of the grids that allow it (full coarsening,
+                         not the FP16 operator) run as grouped launches: grids
+                         of one precision, level count and size class (cell
+                         count within a factor of two) share one chain of
+                         launches, operation i of each grid's V-cycle in one
+                         launch per kernel with a table of one item per grid,
+                         bit for bit the per-grid launches' results.  0 (the
+                         default): each grid's own launches, each grid a branch
+                         of the tick's graph, which measured faster on GB300
+                         (64-grid batch: 801 against 683 solves/s).  Single
+                         solves and served requests ignore it. */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

@@ -2,8 +2,10 @@
 all grids of the batch) against the same steps run one grid at a time.
 
 Each grid's kernels and their order are the same in both modes; only the
-launch grouping differs, so pressure, phi and the corrected fluxes must agree
-bit for bit, and every solve must reach max |div u| < 1e-8."""
+launch grouping differs (and with mg_grouped = 1 the V-cycles of same-size
+grids run as grouped launches, operation i of every V-cycle in one launch
+with a table of per-grid items), so pressure, phi and the corrected fluxes
+must agree bit for bit, and every solve must reach max |div u| < 1e-8."""
 import numpy as np
 import pytest
 
@@ -145,6 +147,41 @@ def test_autotune_per_grid(gpu_ctx):
             assert autotune.entry_candidate(e) in autotune.CANDIDATES and e["ms_per_step"] < float("inf")
         infos, dm = gpu_ctx.projection_step_batch(ids, plist)
         assert all(i["converged"] for i in infos) and (dm < 1e-8).all()
+    finally:
+        for gid in ids:
+            gpu_ctx.grid_destroy(gid)
+
+
+@pytest.mark.parametrize("members", ["uniform", "mixed_kinds"])
+def test_grouped_vcycles_equal_per_grid_launches(gpu_ctx, members):
+    """mg_grouped 1 (grouped V-cycles) against 0 (each grid's own launches)
+    on the same batch, bit for bit; with mixed_kinds the batch also holds
+    grids that are not grouped (the FP16 operator) and FP64 grids, whose
+    grouped stages run separately."""
+    cases = _cases()
+    ids = _load(gpu_ctx, cases)
+    try:
+        out = {}
+        for grouped in (0, 1):
+            plist = []
+            for q in range(len(cases)):
+                prec, half = "mixed", 0
+                if members == "mixed_kinds":
+                    prec = "fp64" if q % 3 == 2 else "mixed"
+                    half = 1 if q % 3 == 1 else 0
+                plist.append(capi.default_params(precision=prec, rtol=1e-9, div_tol=1e-8, mg_half=half,
+                                                 mg_grouped=grouped, cheb_ratio=6.0 + 4 * (q % 2)))
+            for gid, c in zip(ids, cases):
+                _reset(gpu_ctx, gid, c)
+            infos, dm = gpu_ctx.projection_step_batch(ids, plist)
+            assert all(i["converged"] for i in infos) and (dm < 1e-8).all()
+            out[grouped] = ([i["iterations"] for i in infos], dm.copy(),
+                            [_fields(gpu_ctx, gid, c) for gid, c in zip(ids, cases)])
+        assert out[0][0] == out[1][0]
+        assert np.array_equal(out[0][1], out[1][1])
+        for f0, f1 in zip(out[0][2], out[1][2]):
+            for a, b in zip(f0, f1):
+                assert np.array_equal(a, b)
     finally:
         for gid in ids:
             gpu_ctx.grid_destroy(gid)

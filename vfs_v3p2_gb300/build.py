@@ -26,6 +26,7 @@ UNITS = {
     "k_setup.cu": ["--fmad=false"],
     "k_proj.cu": ["--fmad=false"],
     "k_mg.cu": [],
+    "k_group.cu": [],
     "k_krylov.cu": [],
     "vfs_host.cu": [],
 }

@@ -22,6 +22,8 @@
 #include <string>
 #include <vector>
 
+#include "mg_group.h"
+#include "mg_tiles.cuh"
 #include "vfs_common.cuh"
 #include "vfs_gpu.h"
 #include "vfs_kernels.h"
@@ -735,16 +737,27 @@ int fg_start(vfs_ctx* ctx, Fgmres& f, double atol, bool warm) {
 // nv: the host's count of basis columns (column j + 1), for the probe's
 // byte counts only (-1 when unknown, e.g. while capturing).
 template <typename T>
+void issue_krylov(Grid& g, const vfs_solve_params& p, cudaStream_t s, int nv = -1);
+
+template <typename T>
 void issue_iteration(Grid& g, const vfs_solve_params& p, cudaStream_t s, int nv = -1) {
+  Level& F = g.lev[g.L - 1];
+  MGCfg mc = mgcfg(p, g.L - 1, g.half_ok);
+  mc.solo = g.solo;
+  vcycle<T>(g, g.L - 1, bbuf<T>(F), xbuf<T>(F)[0], xbuf<T>(F)[1], mc, &g.st->done, s);
+  issue_krylov<T>(g, p, s, nv);
+}
+
+// The iteration after its V-cycle (whose result is in the finest level's
+// first buffer): w = A z, Gram-Schmidt, Arnoldi close, status copy.
+template <typename T>
+void issue_krylov(Grid& g, const vfs_solve_params& p, cudaStream_t s, int nv) {
   const size_t N = ncell(g.d);
   const double nvb = nv > 0 ? nv : 1, Nd = (double)N;
   const int* skip = &g.st->done;
   Level& F = g.lev[g.L - 1];
   T* zt = xbuf<T>(F)[0];
-  MGCfg mc = mgcfg(p, g.L - 1, g.half_ok);
-  mc.solo = g.solo;
-  const float* dinv = dinv_sel<T>(F, mc.half);
-  vcycle<T>(g, g.L - 1, bbuf<T>(F), zt, xbuf<T>(F)[1], mc, skip, s);
+  const float* dinv = dinv_sel<T>(F, mgcfg(p, g.L - 1, g.half_ok).half);
   {
     // the FP64 slots, z read; w and the Z column written
     Probed pr(VFS_PROBE_APPLY64, s, "k_apply64_krylov", g.L - 1,
@@ -936,6 +949,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (!(p->div_tol >= 0.)) return fail(ctx, VFS_ERR_ARG, "div_tol must be >= 0");
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   if (p->proj_exact != 0 && p->proj_exact != 1) return fail(ctx, VFS_ERR_ARG, "proj_exact must be 0 or 1");
+  if (p->mg_grouped != 0 && p->mg_grouped != 1) return fail(ctx, VFS_ERR_ARG, "mg_grouped must be 0 or 1");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
@@ -1270,10 +1284,218 @@ struct BatchGraph {
   cudaGraphExec_t exec = nullptr;
   std::vector<Job*> members;
   unsigned long long kernels = 0;
+  std::vector<void*> tables;  // work-item tables of the grouped launches (every capture's, freed at the end)
+  std::vector<cudaEvent_t> stage_done;  // end of each group's stages within a tick
   ~BatchGraph() {
     if (exec) cudaGraphExecDestroy(exec);
+    for (void* t : tables) cudaFree(t);
+    for (cudaEvent_t e : stage_done) cudaEventDestroy(e);
   }
 };
+
+// ---------------------------------------------------------------------------
+// Grouped V-cycles (mg_group.h): the V-cycle of each member whose solve
+// allows it (mg_grouped = 1, full coarsening, not the FP16 operator) is
+// recorded as an operation list that mirrors vcycle() (same buffers, same
+// damping, same tiles); operation i of every list runs in stage i, one
+// launch per kernel instantiation present in the stage, each with a table
+// of one item per grid.  The tick graph runs the stages on the batch stream
+// and then each member's Krylov part on its own stream.
+// ---------------------------------------------------------------------------
+enum GOpKind { GOP_SMOOTH, GOP_RESTRICT, GOP_PROLONG, GOP_PROLONG_ADD, GOP_GEMV };
+template <typename T>
+struct GOp {
+  int kind, lev;
+  const T* x;
+  const T* b;
+  T* y;
+  T* y2;
+  double w;
+};
+
+template <typename T>
+T* group_ops(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, std::vector<GOp<T>>& ops) {
+  Level& L = g.lev[l];
+  const int W = level_writes(g, l, c);
+  T* bufs[2] = {xa, xb};
+  if (((W - 1) & 1) == 1) std::swap(bufs[0], bufs[1]);
+  if (l == 0) {
+    if (binv<T>(L)) {
+      ops.push_back(GOp<T>{GOP_GEMV, 0, nullptr, b, bufs[0], nullptr, 0.});
+      return bufs[0];
+    }
+    T* cur = nullptr;
+    for (int q = 0; q < c.ncoarse; q++) {
+      T* o = bufs[q & 1];
+      ops.push_back(GOp<T>{GOP_SMOOTH, 0, cur, b, o, nullptr, c.omega_c});
+      cur = o;
+    }
+    return cur;
+  }
+  int q = 0;
+  T* cur = nullptr;
+  for (; q < c.pre(l); q++) {
+    T* o = bufs[q & 1];
+    ops.push_back(GOp<T>{GOP_SMOOTH, l, cur, b, o, nullptr, c.w(l, 0, q)});
+    cur = o;
+  }
+  Level& C = g.lev[l - 1];
+  T** xc = xbuf<T>(C);
+  ops.push_back(GOp<T>{GOP_RESTRICT, l, cur, b, bbuf<T>(C), xc[0], 0.});
+  T* ec = group_ops<T>(g, l - 1, bbuf<T>(C), xc[0], xc[1], c, ops);
+  if (!cur) {
+    cur = bufs[q & 1];
+    q++;
+    ops.push_back(GOp<T>{GOP_PROLONG, l, ec, nullptr, cur, nullptr, 0.});
+  } else {
+    ops.push_back(GOp<T>{GOP_PROLONG_ADD, l, ec, nullptr, cur, nullptr, 0.});
+  }
+  for (int r = 0; r < c.post(l); r++, q++) {
+    T* o = bufs[q & 1];
+    ops.push_back(GOp<T>{GOP_SMOOTH, l, cur, b, o, nullptr, c.w(l, 1, r)});
+    cur = o;
+  }
+  return cur;
+}
+
+// The item of one operation on one grid: its kernel, tiles and shared memory.
+template <typename T>
+void group_item(Grid& g, const GOp<T>& op, const MGCfg& c, const int* skip, int* kind, GroupItem<T>* it, int* blocks,
+                size_t* smem) {
+  Level& L = g.lev[op.lev];
+  const bool face = sizeof(T) == 4 && c.face && face_level(L);
+  const bool ch = face_level(L);  // the 11-slot set
+  GroupItem<T> t{};
+  t.A = mgview<T>(L, skip, false, face);
+  t.skip = skip;
+  t.x = op.x;
+  t.b = op.b;
+  t.y = op.y;
+  t.y2 = op.y2;
+  t.w = (T)op.w;
+  *smem = 0;
+  const int ni = L.d.mx - 2, nj = L.d.my - 2, nk = L.d.mz - 2;
+  switch (op.kind) {
+    case GOP_SMOOTH: {
+      t.lf = lf_sel<T>(L, false);
+      t.tw = smooth_tw<T>(ni, nj, nk, c.cols);
+      t.gx = (ni + t.tw - 1) / t.tw;
+      t.gy = nk;
+      *blocks = t.gx * nk;
+      *smem = (size_t)3 * t.tw * nj * sizeof(T);
+      const int zg = op.x ? 0 : 1;
+      *kind = (face ? GK_SMOOTH_FACE : ch ? GK_SMOOTH_CH : GK_SMOOTH_ALL) + zg;
+      break;
+    }
+    case GOP_RESTRICT: {
+      Level& C = g.lev[op.lev - 1];
+      t.rw = rw_sel<T>(L, false);
+      t.c = C.d;
+      t.nvc = C.nvert;
+      t.gx = (C.d.mx - 2 + 31) / 32;
+      t.gy = (C.d.my - 2 + 3) / 4;
+      *blocks = t.gx * t.gy * (C.d.mz - 2);
+      *kind = face ? GK_RESTRICT_FACE : ch ? GK_RESTRICT_CH : GK_RESTRICT_ALL;
+      break;
+    }
+    case GOP_PROLONG:
+    case GOP_PROLONG_ADD: {
+      Level& C = g.lev[op.lev - 1];
+      t.c = C.d;
+      t.pcode = L.pcode;
+      t.add = op.kind == GOP_PROLONG_ADD;
+      t.gx = (ni + 31) / 32;
+      t.gy = (nj + 7) / 8;
+      *blocks = t.gx * t.gy * ((nk + 3) / 4);
+      *kind = GK_PROLONG;
+      break;
+    }
+    default: {  // GOP_GEMV
+      t.Binv = binv<T>(L);
+      t.n = L.nco;
+      *blocks = (L.nco + 7) / 8;
+      *smem = (size_t)L.nco * sizeof(T);
+      *kind = GK_GEMV;
+      break;
+    }
+  }
+  *it = t;
+}
+
+struct GroupLaunch {
+  int kind, nitems, nblocks;
+  size_t off, smem;  // first item in the table, dynamic shared memory
+};
+
+// The stages of the grouped V-cycles of `jobs` (all of multigrid precision
+// T): their launches and the item table (host side).
+template <typename T>
+void group_plan(std::vector<Job*>& jobs, std::vector<GroupLaunch>& launches, std::vector<GroupItem<T>>& table) {
+  std::vector<std::vector<GOp<T>>> lists(jobs.size());
+  std::vector<MGCfg> cfg(jobs.size());
+  size_t stages = 0;
+  for (size_t q = 0; q < jobs.size(); q++) {
+    Grid& g = *jobs[q]->g;
+    Level& F = g.lev[g.L - 1];
+    cfg[q] = mgcfg(jobs[q]->p, g.L - 1, g.half_ok);
+    group_ops<T>(g, g.L - 1, bbuf<T>(F), xbuf<T>(F)[0], xbuf<T>(F)[1], cfg[q], lists[q]);
+    stages = std::max(stages, lists[q].size());
+  }
+  for (size_t i = 0; i < stages; i++) {
+    std::vector<GroupItem<T>> bucket[GK_COUNT];
+    int nb[GK_COUNT] = {0};
+    size_t sm[GK_COUNT] = {0};
+    for (size_t q = 0; q < jobs.size(); q++) {
+      if (i >= lists[q].size()) continue;
+      Grid& g = *jobs[q]->g;
+      int kind = 0, blocks = 0;
+      size_t smem = 0;
+      GroupItem<T> it;
+      group_item<T>(g, lists[q][i], cfg[q], &g.st->done, &kind, &it, &blocks, &smem);
+      it.start = nb[kind];
+      nb[kind] += blocks;
+      sm[kind] = std::max(sm[kind], smem);
+      bucket[kind].push_back(it);
+    }
+    for (int k = 0; k < GK_COUNT; k++) {
+      if (bucket[k].empty()) continue;
+      launches.push_back(GroupLaunch{k, (int)bucket[k].size(), nb[k], table.size(), sm[k]});
+      table.insert(table.end(), bucket[k].begin(), bucket[k].end());
+    }
+  }
+}
+
+// Grids grouped together: the same multigrid precision, number of levels
+// and interior cell count to within a factor of two (so that a stage's
+// launches do not wait long on one grid's larger tiles).
+std::string group_key(const Job& J) {
+  const Grid& g = *J.g;
+  const double cells = (double)n_interior(g.d);
+  return std::to_string(J.mixed() ? 4 : 8) + ":" + std::to_string(g.L) + ":" +
+         std::to_string((int)std::lround(std::log2(std::max(cells, 1.))));
+}
+
+// Members whose V-cycle may run grouped.
+bool groupable(const Job& J) {
+  const Grid& g = *J.g;
+  return J.p.mg_grouped != 0 && !g.si && !g.sj && !g.sk && !mgcfg(J.p, g.L - 1, g.half_ok).half;
+}
+
+// Uploads a grouped plan's table (a device buffer owned by bg) and returns
+// its device address.
+template <typename T>
+int group_upload(vfs_ctx* ctx, cudaStream_t s0, const std::vector<GroupItem<T>>& table, BatchGraph& bg,
+                 const GroupItem<T>** out) {
+  *out = nullptr;
+  if (table.empty()) return VFS_OK;
+  void* d = nullptr;
+  CK(cudaMalloc(&d, table.size() * sizeof(GroupItem<T>)));
+  bg.tables.push_back(d);
+  CK(cudaMemcpyAsync(d, table.data(), table.size() * sizeof(GroupItem<T>), cudaMemcpyHostToDevice, s0));
+  CK(cudaStreamSynchronize(s0));  // the host table goes out of scope
+  *out = (const GroupItem<T>*)d;
+  return VFS_OK;
+}
 
 int batch_capture(vfs_ctx* ctx, cudaStream_t s0, cudaEvent_t fork, std::vector<cudaEvent_t>& joins,
                   std::vector<Job*>& members, BatchGraph& bg) {
@@ -1286,18 +1508,77 @@ int batch_capture(vfs_ctx* ctx, cudaStream_t s0, cudaEvent_t fork, std::vector<c
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     joins.push_back(e);
   }
+  // grouped V-cycles: groups, plans and tables before the capture
+  std::map<std::string, std::vector<size_t>> groups;
+  std::vector<char> grouped(members.size(), 0);
+  for (size_t q = 0; q < members.size(); q++) {
+    if (!groupable(*members[q])) continue;
+    grouped[q] = 1;
+    groups[group_key(*members[q])].push_back(q);
+  }
+  struct Plan {
+    std::vector<size_t> idx;
+    bool f32;
+    std::vector<GroupLaunch> launches;
+    const GroupItem<float>* d32 = nullptr;
+    const GroupItem<double>* d64 = nullptr;
+  };
+  std::vector<Plan> plans;
+  for (auto& kv : groups) {
+    Plan P;
+    P.idx = kv.second;
+    std::vector<Job*> js;
+    for (size_t q : P.idx) js.push_back(members[q]);
+    P.f32 = js[0]->mixed();
+    if (P.f32) {
+      std::vector<GroupItem<float>> t;
+      group_plan<float>(js, P.launches, t);
+      if (int r = group_upload<float>(ctx, s0, t, bg, &P.d32)) return r;
+    } else {
+      std::vector<GroupItem<double>> t;
+      group_plan<double>(js, P.launches, t);
+      if (int r = group_upload<double>(ctx, s0, t, bg, &P.d64)) return r;
+    }
+    plans.push_back(std::move(P));
+  }
+  while (bg.stage_done.size() < plans.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    bg.stage_done.push_back(e);
+  }
   const unsigned long long n0 = g_launches.load();
   cudaGraph_t graph = nullptr;
   CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(fork, s0);
+  // members not grouped: their whole iteration on their own streams
   for (size_t q = 0; q < members.size(); q++) {
+    if (grouped[q]) continue;
     Grid& g = *members[q]->g;
     cudaStreamWaitEvent(g.s, fork, 0);
     if (members[q]->mixed()) issue_iteration<float>(g, members[q]->p, g.s);
     else issue_iteration<double>(g, members[q]->p, g.s);
     cudaEventRecord(joins[q], g.s);
-    cudaStreamWaitEvent(s0, joins[q], 0);
   }
+  // each group: its V-cycle stages on its first member's stream, then every
+  // member's Krylov part on the member's own stream
+  for (size_t k = 0; k < plans.size(); k++) {
+    const Plan& P = plans[k];
+    cudaStream_t gs = members[P.idx[0]]->g->s;
+    cudaStreamWaitEvent(gs, fork, 0);
+    for (const GroupLaunch& gl : P.launches) {
+      if (P.f32) launch_group<float>(gl.kind, P.d32 + gl.off, gl.nitems, gl.nblocks, gl.smem, gs);
+      else launch_group<double>(gl.kind, P.d64 + gl.off, gl.nitems, gl.nblocks, gl.smem, gs);
+    }
+    cudaEventRecord(bg.stage_done[k], gs);
+    for (size_t q : P.idx) {
+      Grid& g = *members[q]->g;
+      cudaStreamWaitEvent(g.s, bg.stage_done[k], 0);
+      if (members[q]->mixed()) issue_krylov<float>(g, members[q]->p, g.s);
+      else issue_krylov<double>(g, members[q]->p, g.s);
+      cudaEventRecord(joins[q], g.s);
+    }
+  }
+  for (size_t q = 0; q < members.size(); q++) cudaStreamWaitEvent(s0, joins[q], 0);
   cudaError_t e = cudaStreamEndCapture(s0, &graph);
   bg.kernels = g_launches.load() - n0;
   g_launches -= bg.kernels;
@@ -1517,6 +1798,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->nu2_coarse = -1;
   p->mg_half = 0;
   p->proj_exact = 0;
+  p->mg_grouped = 0;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
