@@ -547,7 +547,8 @@ def compact_single(args, dist, local, ws, config):
     cand, _ = autotune.tune_resident(ctx, gid, case, base, steps=2)
     out["autotuned"] = {**autotune.candidate_entry(cand), "autotune_s": time.perf_counter() - t0}
     autotune.apply_candidate(base, cand)
-    K = 20
+    K = 20 if g.nvert.size < 2**24 else 5
+    phis = {}
     for prec in ("mixed", "fp64"):
         params = autotune.with_precision(base, capi.VFS_MIXED if prec == "mixed" else capi.VFS_FP64)
         for _ in range(3):
@@ -563,19 +564,27 @@ def compact_single(args, dist, local, ws, config):
         t = allmax(dist, ctx.elapsed(0, 1))
         out[prec] = {"value": ws * K / (t / 1e3), "unit": "solves/s", "iterations": statistics.mean(its),
                      "divmax": max(dms), "steps": K}
+        phis[prec] = ctx.get_field(gid, capi.FIELD_PHI, g.nvert.shape)
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    # the two solutions of the same step (fluid interior, means removed)
+    fl = g.nvert < 0.1
+    fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = False, False, False, False, False, False
+    a = phis["mixed"][fl] - phis["mixed"][fl].mean()
+    r = phis["fp64"][fl] - phis["fp64"][fl].mean()
+    out["phi_rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(a - r) / np.linalg.norm(r))
     ctx.grid_destroy(gid)
     ctx.close()
     return out
 
 
 def compact_workloads(args, dist, local, ws):
-    """The channel, batched and served workloads in short runs, so that one
-    default bench line records every configuration; --config batch / serve
+    """The channel, terrain, batched and served workloads in short runs, so
+    that one default bench line records every configuration; --config batch / serve
     give the full runs.  Every grid runs the smoothing schedule the autotuner
     picks for it (tuned once, before the timed steps; the FP64 runs use the
     same schedules)."""
-    out = {"channel_64x64x64": compact_single(args, dist, local, ws, "channel")}
+    out = {"channel_64x64x64": compact_single(args, dist, local, ws, "channel"),
+           "terrain_512x256x256": compact_single(args, dist, local, ws, "terrain")}
     b = argparse.Namespace(**vars(args))
     b.steps, b.warmup, b.no_tune, b.no_fp64, b.scale = 3, 1, False, False, 1
     bl = run_batch(b, dist, local, ws)
