@@ -72,6 +72,8 @@ def parse():
                     help="multigrid operator storage: FP32 face form on 11-slot levels (0), FP16 normalised by "
                          "the diagonal (1), FP32 assembled coefficients (2); FP32 arithmetic in every case")
     ap.add_argument("--restart", type=int, default=30)
+    ap.add_argument("--mg-tma", type=int, default=0, choices=[0, 1],
+                    help="finest face-form sweeps on the tensor-copy kernel (1) or the register-staged one (0)")
     ap.add_argument("--mg-grouped", type=int, default=0, choices=[0, 1],
                     help="batch: V-cycles as grouped launches over same-size grids (1) or each grid's own (0)")
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
@@ -99,7 +101,7 @@ def make_case(args):
 
 
 # storage of the FP32 multigrid's level operators (vfs_solve_params.mg_half)
-OPERATOR = {0: "fp32 (face form on 11-slot levels: 3 face weights + 2 cross weights + aj + code byte per cell)",
+OPERATOR = {0: "fp32 (face form on 11-slot levels: 3 face weights + 2 cross weights + aj carrying 4 code bits per cell)",
             1: "fp16 diagonal-normalised, row sums kept (fp32 arithmetic)",
             2: "fp32 assembled coefficients (11 or 19 slots)"}
 
@@ -634,7 +636,7 @@ def main():
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
-                                mg_half=args.mg_half)
+                                mg_half=args.mg_half, mg_tma=args.mg_tma)
     other = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
@@ -739,6 +741,8 @@ def main():
     avg_ms = pms / plaunch if plaunch else None
     achieved = alg / (avg_ms / 1e3) / 1e9 if plaunch else None
     kname = {0: "k_smooth<float, FaceOp>", 1: "k_smooth<float, __half>", 2: "k_smooth<float, float>"}[args.mg_half]
+    if args.mg_half == 0 and args.mg_tma:
+        kname = "k_smooth_tma"
     traffic = ncu_traffic(kname + ":" + case.name)
     roof = {"kernel": kname + " (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
@@ -778,7 +782,7 @@ def main():
                        "measures": "pressure projection steps/s with U* resident, mixed FP32-MG/FP64-FGMRES",
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
                        "restart": args.restart, "orth": args.orth, **smoother_config(args),
-                       "mg_operator": OPERATOR[args.mg_half],
+                       "mg_operator": OPERATOR[args.mg_half], "mg_tma": args.mg_tma,
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},

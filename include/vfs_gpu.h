@@ -101,9 +101,10 @@ typedef struct {
                    i-k ones only (the 11-slot operator: channel and sphere
                    grids) in face form: per cell its three faces' FP32
                    weights (g11, g22, g33 and the cross weights with the
-                   one-sided regime folded in), aj and a code byte, the row
+                   one-sided regime folded in) and aj carrying the regime
+                   code bits in its four low mantissa bits, the row
                    being aj times the divergence of the face fluxes (a sweep
-                   streams 41 instead of 60 bytes per cell); elsewhere the 19
+                   streams 40 instead of 60 bytes per cell); elsewhere the 19
                    assembled FP32 coefficients.  2: the assembled FP32
                    coefficients on every level.  1: FP16 normalised by the
                    diagonal, with an FP16 centre-slot correction that keeps
@@ -142,6 +143,15 @@ typedef struct {
                          of the tick's graph, which measured faster on GB300
                          (64-grid batch: 801 against 683 solves/s).  Single
                          solves and served requests ignore it. */
+  int mg_tma;         /* 1: the finest level's sweeps on the FP32 face form
+                         (levels of at least 2^20 interior cells with even mx
+                         and my) run the tensor-copy kernel: one block per SM,
+                         a producer thread copying 16-row bands of x, the face
+                         weights, b and 1/m into a shared-memory ring
+                         (cp.async.bulk.tensor, mbarrier completion) while
+                         eight warps form residuals, solve columns and write;
+                         bit for bit the other kernel's results.  0 (the
+                         default): the register-staged kernel. */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

@@ -46,12 +46,12 @@ def test_probe_all_records_a_step(gpu_ctx):
         top = case.levels - 1
         assert sum(1 for r in recs if r[0] == "k_apply64_krylov") == its
         assert sum(1 for r in recs if r[0] == "k_smooth (zero guess)" and r[1] == top) == its
-        # a finest full sweep streams the face form (5 FP32 face weights, aj
-        # and a code byte: 25 bytes), x, b and 1/m and writes x
+        # a finest full sweep streams the face form (5 FP32 face weights and
+        # aj with the code bits: 24 bytes), x, b and 1/m and writes x
         ni, nj, nk = g.ni, g.nj, g.nk
         sweeps = [r for r in recs if r[0] == "k_smooth" and r[1] == top]
         assert len(sweeps) == its * (params.nu1 + params.nu2 - 1)
-        assert all(r[3] == ni * nj * nk * (25 + 16) for r in sweeps)
+        assert all(r[3] == ni * nj * nk * (24 + 16) for r in sweeps)
         assert all(r[2] > 0 for r in recs if r[3] > 0)
     finally:
         gpu_ctx.grid_destroy(gid)
@@ -79,7 +79,7 @@ def test_probe_smooth_counts_real_sweeps(gpu_ctx):
         n, ms, by = gpu_ctx.probe_end()
         sweeps = info["iterations"] * (params.nu1 - 1 + params.nu2)
         assert n == sweeps and ms > 0
-        assert by == sweeps * g.ni * g.nj * g.nk * (25 + 16)  # face form (25 bytes), x, b, 1/m read, x written
+        assert by == sweeps * g.ni * g.nj * g.nk * (24 + 16)  # face form (24 bytes), x, b, 1/m read, x written
         runs = gpu_ctx.probe_records(2 * info["iterations"])
         assert all(r[0] == "k_smooth (run)" for r in runs)
     finally:

@@ -27,6 +27,7 @@ UNITS = {
     "k_proj.cu": ["--fmad=false"],
     "k_mg.cu": [],
     "k_group.cu": [],
+    "k_smooth_tma.cu": [],
     "k_krylov.cu": [],
     "vfs_host.cu": [],
 }

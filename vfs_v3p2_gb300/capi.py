@@ -66,7 +66,7 @@ class SolveParams(ctypes.Structure):
                 ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
                 ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int), ("smoother", ctypes.c_int),
                 ("cheb_hi", ctypes.c_double), ("cheb_ratio", ctypes.c_double), ("proj_exact", ctypes.c_int),
-                ("mg_grouped", ctypes.c_int)]
+                ("mg_grouped", ctypes.c_int), ("mg_tma", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):

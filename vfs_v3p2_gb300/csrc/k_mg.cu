@@ -13,6 +13,7 @@
 #include <type_traits>
 
 #include "mg_tiles.cuh"
+#include "mg_tma.h"
 #include "vfs_common.cuh"
 #include "vfs_kernels.h"
 #include "vfs_proj.h"
@@ -150,7 +151,16 @@ static void smooth_launch(bool small, dim3 g, size_t sm, cudaStream_t s, const O
 
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols,
-                  bool solo) {
+                  bool solo, bool tma) {
+  if constexpr (sizeof(T) == 4) {
+    // the tensor-copy sweep; a configuration it cannot take (its launch
+    // refused before running) falls back to the register-staged one
+    if (tma && A.ffi && xi && fits_ch(A.mask) &&
+        (size_t)(A.d.mx - 2) * (A.d.my - 2) * (A.d.mz - 2) >= (size_t)VFS_TMA_MINCELLS &&
+        smooth_tma_stages(A.d) > 0 && smooth_tma_err() &&
+        launch_smooth_tma(A, lf, xi, b, xo, omega, smooth_tma_err(), s) == (int)cudaSuccess)
+      return (int)cudaSuccess;
+  }
   static bool attr = false;
   if (!attr) {
     smooth_attrs<MASK_CH, T, T, false>();
@@ -529,7 +539,7 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
 
 #define INST(T)                                                                                                        \
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
-  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int, bool);            \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int, bool, bool);      \
   template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
   template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const T*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \

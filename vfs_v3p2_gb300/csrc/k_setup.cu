@@ -540,12 +540,15 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
 // bits: U is the pair at k+1 (x_T + x_TE) or, one-sided, the centre pair
 // (x_C + x_E); L the pair at k-1 or the centre pair; likewise R / Lf for the
 // pairs at i+1 / i-1 of the k face.  A cell owns its +i, +j, +k faces; the
-// row is scaled by aj.  A row streams 5 FP32 face weights, aj and a code
-// byte (25 bytes) instead of 11 FP32 coefficients (44 bytes).
+// row is scaled by aj.  The four code bits ride in the low mantissa bits of
+// the FP32 aj (a relative change of at most 2^-19 of aj; the bits are
+// cleared before aj is used), so a row streams 5 FP32 face weights and aj
+// (24 bytes) instead of 11 FP32 coefficients (44 bytes), as FP32 arrays
+// only (no byte array, whose rows a tensor copy could not tile).
 // ---------------------------------------------------------------------------
 __global__ void k_face_operator(Dims d, const double* __restrict__ g, const double* __restrict__ nvert,
                                 const double* __restrict__ aj, float2* __restrict__ fi, float2* __restrict__ fk,
-                                float* __restrict__ fj, float* __restrict__ faj, uint8_t* __restrict__ code) {
+                                float* __restrict__ fj, float* __restrict__ faj) {
   const size_t N = ncell(d);
   const int mx = d.mx, my = d.my, mz = d.mz, ip = d.ip, jp = d.jp, kp = d.kp;
   const double *g11 = g, *g13 = g + 2 * N, *g22 = g + 4 * N, *g31 = g + 6 * N, *g33 = g + 8 * N;
@@ -599,8 +602,7 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
     fi[_t] = vi;
     fk[_t] = vk;
     fj[_t] = vj;
-    faj[_t] = row ? (float)aj[_t] : 0.f;
-    code[_t] = (uint8_t)cb;
+    faj[_t] = row ? __int_as_float((__float_as_int((float)aj[_t]) & ~0xF) | (int)cb) : 0.f;
   }
 }
 
@@ -812,8 +814,8 @@ int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tm
 }
 
 int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
-                         float* fj, float* faj, uint8_t* code, cudaStream_t s) {
-  k_face_operator<<<nblk(ncell(d)), 256, 0, s>>>(d, g, nvert, aj, fi, fk, fj, faj, code); ++g_launches;
+                         float* fj, float* faj, cudaStream_t s) {
+  k_face_operator<<<nblk(ncell(d)), 256, 0, s>>>(d, g, nvert, aj, fi, fk, fj, faj); ++g_launches;
   return (int)cudaGetLastError();
 }
 

@@ -182,6 +182,9 @@ struct FaceData {
   float gjc, gjs, aj;
   unsigned cc, cw, cb;        // code bits of c, c-i, c-k
 };
+// aj of the face form with its code bits cleared, and the code bits.
+__device__ __forceinline__ float face_aj(float v) { return __int_as_float(__float_as_int(v) & ~0xF); }
+__device__ __forceinline__ unsigned face_code(float v) { return (unsigned)__float_as_int(v) & 0xFu; }
 __device__ __forceinline__ float face_row(const FaceData& f, const float* x) {
   const float xc = x[CP], xe = x[EP], xw = x[WP], xn = x[NP], xs = x[SP], xt = x[TP], xb = x[BP];
   const float xte = x[TE], xbe = x[BE], xtw = x[TW], xbw = x[BW];
@@ -216,10 +219,7 @@ __device__ __forceinline__ void face_gather(const OpView<float>& A, const float*
   f.fkb = __ldg(A.ffk + c + okB);
   f.gjc = __ldg(A.ffj + c);
   f.gjs = __ldg(A.ffj + c + ojS);
-  f.aj = __ldg(A.faj + c);
-  f.cc = __ldg(A.fcode + c);
-  f.cw = __ldg(A.fcode + c + oiW);
-  f.cb = __ldg(A.fcode + c + okB);
+  const float ajc = __ldg(A.faj + c), ajw = __ldg(A.faj + c + oiW), ajb = __ldg(A.faj + c + okB);
   xv[CP] = __ldg(x + c);
   xv[EP] = __ldg(x + c + oiE);
   xv[WP] = __ldg(x + c + oiW);
@@ -231,6 +231,10 @@ __device__ __forceinline__ void face_gather(const OpView<float>& A, const float*
   xv[BE] = __ldg(x + c + okB + oiE);
   xv[TW] = __ldg(x + c + okT + oiW);
   xv[BW] = __ldg(x + c + okB + oiW);
+  f.aj = face_aj(ajc);
+  f.cc = face_code(ajc);
+  f.cw = face_code(ajw);
+  f.cb = face_code(ajb);
 }
 
 
@@ -442,15 +446,14 @@ __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float*
       const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
       f[u].gjc = __ldg(A.ffj + c);
       f[u].gjs = __ldg(A.ffj + c + ojS);
-      f[u].aj = __ldg(A.faj + c);
+      f[u].aj = __ldg(A.faj + c);  // code bits still set: split below
       if (!ZG) {
         f[u].fic = __ldg(A.ffi + c);
         f[u].fiw = __ldg(A.ffi + c + oiW);
         f[u].fkc = __ldg(A.ffk + c);
         f[u].fkb = __ldg(A.ffk + c + okB);
-        f[u].cc = __ldg(A.fcode + c);
-        f[u].cw = __ldg(A.fcode + c + oiW);
-        f[u].cb = __ldg(A.fcode + c + okB);
+        f[u].cw = face_code(__ldg(A.faj + c + oiW));
+        f[u].cb = face_code(__ldg(A.faj + c + okB));
         xv[u][0] = __ldg(xi + c);
         xv[u][1] = __ldg(xi + c + oiE);
         xv[u][2] = __ldg(xi + c + oiW);
@@ -471,6 +474,8 @@ __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float*
       const int idx = base + u * VFS_SMOOTH_NT;
       if (idx >= tw * nj) break;
       const int jl = idx / tw;
+      f[u].cc = face_code(f[u].aj);
+      f[u].aj = face_aj(f[u].aj);
       const bool live = (i0 + idx % tw <= d.mx - 2) && f[u].aj != 0.f;
       float x11[19];  // slot-indexed view of the 11 values (TE, BE, TW, BW: the stencil slots)
       if (!ZG) {

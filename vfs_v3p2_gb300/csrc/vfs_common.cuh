@@ -95,14 +95,14 @@ struct OpView {
   const __half* hcoef = nullptr;  // [19][hslot], FP16 diagonal-normalised (nullable)
   // face form of the FP32 multigrid operator (11-slot levels, nullable): per
   // cell the +i face (g11, k-cross weight), +k face (g33, i-cross weight), +j
-  // face (g22), aj, and the cross terms' one-sided code bits (bit 0: the
-  // i face's upper pair is the centre pair, bit 1: its lower pair; bits 2, 3
-  // the same for the k face's pairs at i+1 / i-1)
+  // face (g22), and aj with the cross terms' one-sided code bits in its four
+  // low mantissa bits (bit 0: the i face's upper pair is the centre pair,
+  // bit 1: its lower pair; bits 2, 3 the same for the k face's pairs at
+  // i+1 / i-1)
   const float2* ffi = nullptr;
   const float2* ffk = nullptr;
   const float* ffj = nullptr;
   const float* faj = nullptr;
-  const uint8_t* fcode = nullptr;
 };
 
 __device__ __forceinline__ bool skipped(const int* f) { return f && *(volatile const int*)f; }

@@ -24,6 +24,7 @@
 
 #include "mg_group.h"
 #include "mg_tiles.cuh"
+#include "mg_tma.h"
 #include "vfs_common.cuh"
 #include "vfs_gpu.h"
 #include "vfs_kernels.h"
@@ -147,7 +148,6 @@ struct Level {
   float2* ffk = nullptr;
   float* ffj = nullptr;
   float* faj = nullptr;
-  uint8_t* fcode = nullptr;
 };
 
 struct Grid {
@@ -198,7 +198,7 @@ struct Grid {
   int* comp = nullptr;   // finest-level region labels (device), when ncomp > 1
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
   int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
-  int ig_smoother = -1;
+  int ig_smoother = -1, ig_tma = -1;
   double ig_cheb_hi = 0., ig_cheb_ratio = 0.;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
@@ -394,7 +394,6 @@ OpView<T> mgview(Level& L, const int* skip, bool half, bool face = false) {
     A.ffk = L.ffk;
     A.ffj = L.ffj;
     A.faj = L.faj;
-    A.fcode = L.fcode;
   }
   return A;
 }
@@ -448,6 +447,7 @@ struct MGCfg {
   bool half;       // FP16 normalised operator (FP32 multigrid only)
   bool face;       // FP32 face form on 11-slot levels (FP32 multigrid only)
   bool solo;       // the grid's solve runs alone
+  bool tma;        // the finest face-form sweeps run the tensor-copy kernel
   int pre(int l) const { return l == top ? nu1 : nu1c; }
   int post(int l) const { return l == top ? nu2 : nu2c; }
 };
@@ -463,19 +463,19 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
 void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols, bool solo,
-                   cudaStream_t s) {
+                   cudaStream_t s, bool tma = false) {
   // x != 0: the coefficient slots (FP16 or T), x, b and 1/m read, x written;
   // from a zero guess: the centre (not with the FP16 operator), SP and NP
   // slots, b and 1/m read, x written
-  // face form: the 5 face weights, aj and the code byte (25 bytes) instead
+  // face form: the 5 face weights and aj with the code bits (24 bytes) instead
   // of the slots; from a zero guess the j faces and aj (8 bytes)
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
-  const double op_bytes = A.ffi ? (xi ? 25.0 : 8.0) : (xi ? slot_bytes * popcount(A.mask) : slot_bytes * (A.hcoef ? 2 : 3));
+  const double op_bytes = A.ffi ? (xi ? 24.0 : 8.0) : (xi ? slot_bytes * popcount(A.mask) : slot_bytes * (A.hcoef ? 2 : 3));
   const double bytes = (double)n_interior(A.d) * (op_bytes + (xi ? 4.0 : 3.0) * sizeof(T));
   int rc;
   {
     Probed pr(VFS_PROBE_ALL, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
-    rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo);
+    rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo, tma);
   }
   dbg("smooth", l, rc, s);
 }
@@ -544,13 +544,13 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   int q = 0;
   T* cur = nullptr;
   const bool run_probe = g_probe.kind == VFS_PROBE_SMOOTH && l == g.L - 1;
-  const double sweep_bytes = (double)n_interior(A.d) * ((A.ffi ? 25.0 : (A.hcoef ? 2.0 : (double)sizeof(T)) *
+  const double sweep_bytes = (double)n_interior(A.d) * ((A.ffi ? 24.0 : (A.hcoef ? 2.0 : (double)sizeof(T)) *
                                                                             popcount(A.mask)) + 4.0 * sizeof(T));
   SweepRun run;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
     if (cur) run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s, c.tma && l == c.top);
     cur = o;
   }
   run.close();
@@ -562,7 +562,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     // side and the cleared coarse x written
     const bool face_rr = A.ffi && !g.si && !g.sj && !g.sk;  // the face form's restriction (tiled form only)
     Probed pr(VFS_PROBE_ALL, s, "k_resrestrict", l,
-              nf * ((face_rr ? 25.0 : slot_bytes * popcount(A.mask)) + 3.0 * sizeof(T)) +
+              nf * ((face_rr ? 24.0 : slot_bytes * popcount(A.mask)) + 3.0 * sizeof(T)) +
                   2.0 * n_interior(C.d) * sizeof(T));
     dbg("residual_restrict", l,
         launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0],
@@ -585,7 +585,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
     run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s, c.tma && l == c.top);
     cur = o;
   }
   run.close();
@@ -628,6 +628,7 @@ MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
   c.half = p.precision == VFS_MIXED && p.mg_half == 1 && half_ok;
   c.face = p.precision == VFS_MIXED && p.mg_half == 0;
   c.solo = false;
+  c.tma = p.mg_tma != 0;
   return c;
 }
 
@@ -824,7 +825,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
       g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse &&
       g.ig_half == p.mg_half && g.ig_solo == (int)g.solo && g.ig_smoother == p.smoother &&
-      g.ig_cheb_hi == p.cheb_hi && g.ig_cheb_ratio == p.cheb_ratio) {
+      g.ig_cheb_hi == p.cheb_hi && g.ig_cheb_ratio == p.cheb_ratio && g.ig_tma == p.mg_tma) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -860,6 +861,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_smoother = p.smoother;
   g.ig_cheb_hi = p.cheb_hi;
   g.ig_cheb_ratio = p.cheb_ratio;
+  g.ig_tma = p.mg_tma;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -950,6 +952,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   if (p->proj_exact != 0 && p->proj_exact != 1) return fail(ctx, VFS_ERR_ARG, "proj_exact must be 0 or 1");
   if (p->mg_grouped != 0 && p->mg_grouped != 1) return fail(ctx, VFS_ERR_ARG, "mg_grouped must be 0 or 1");
+  if (p->mg_tma != 0 && p->mg_tma != 1) return fail(ctx, VFS_ERR_ARG, "mg_tma must be 0 or 1");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
@@ -1205,6 +1208,9 @@ int job_post_eval(vfs_ctx* ctx, Job& J) {
   }
   // with the step's divergence measured, div_limited reports the outcome
   if (J.post && J.p.div_tol > 0.) J.info.div_limited = J.divmax > J.p.div_tol ? 1 : 0;
+  // a bounded wait of the tensor-copy sweep that ran out leaves garbage
+  if (J.p.mg_tma && smooth_tma_take_error())
+    return job_fail(ctx, J, fail(ctx, VFS_ERR_CUDA, "tensor-copy sweep: a bounded wait ran out"));
   J.phase = J_DONE;
   return VFS_OK;
 }
@@ -1765,7 +1771,7 @@ size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
   b += 19 * 2 * hslot(d) + N * (4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
-  b += N * (8 + 8 + 4 + 4 + 1);               // face form: ffi ffk ffj faj fcode
+  b += N * (8 + 8 + 4 + 4);                   // face form: ffi ffk ffj faj (with the code bits)
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 9 + 3 + 3 + 3 + 3 + 3) + N * 3;  // pd pw minv u ustar p phi b ucat aos, nb8 pc
   return b;
@@ -1799,6 +1805,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->mg_half = 0;
   p->proj_exact = 0;
   p->mg_grouped = 0;
+  p->mg_tma = 0;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -1941,7 +1948,6 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.ffk, Lv.N);
     GAB(Lv.ffj, Lv.N);
     GAB(Lv.faj, Lv.N);
-    GAB(Lv.fcode, Lv.N);
     GAB(Lv.lfh, Lv.N);
     GAB(Lv.rwh, Lv.N);
     if (l == L - 1) GAB(Lv.dinvh, Lv.N);
@@ -2107,7 +2113,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     Level& Lv = g.lev[l];
     launch_gtensor(Lv.d, Lv.M, gt, g.s);
     launch_assemble(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.coef, Lv.mcoef, Lv.mcoef32, dmask, g.s);
-    launch_face_operator(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.ffi, Lv.ffk, Lv.ffj, Lv.faj, Lv.fcode, g.s);
+    launch_face_operator(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.ffi, Lv.ffk, Lv.ffj, Lv.faj, g.s);
     CK(cudaMemcpyAsync(&Lv.mask, dmask, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
@@ -3033,6 +3039,10 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     if (!r && cudaMalloc(&dz, N * 4) != cudaSuccess) r = VFS_ERR_NOMEM;
     if (!r) cudaMemsetAsync(dz, 0, N * 4, g.s);
     if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s, true, true);
+    if (!r && p->mg_tma) {
+      cudaStreamSynchronize(g.s);
+      if (smooth_tma_take_error()) r = fail(ctx, VFS_ERR_CUDA, "tensor-copy sweep: a bounded wait ran out");
+    }
     if (!r) {
       std::vector<float> hz(N);
       cudaStreamSynchronize(g.s);

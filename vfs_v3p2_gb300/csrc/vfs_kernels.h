@@ -26,9 +26,10 @@ int launch_assemble(const Dims& d, const double* g, const double* nvert, const d
                     float* mcoef32, unsigned* mask, cudaStream_t s);
 // face form of the aj-scaled operator (11-slot levels), FP32: per cell its
 // +i face (g11, k-cross weight), +k face (g33, i-cross weight), +j face
-// (g22), aj, and the one-sided code bits of the two cross terms
+// (g22), and aj with the one-sided code bits of the two cross terms in its
+// four low mantissa bits
 int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
-                         float* fj, float* faj, uint8_t* code, cudaStream_t s);
+                         float* fj, float* faj, cudaStream_t s);
 int launch_coarsen(const Dims& f, const Dims& c, int si, int sj, int sk, const double* coor_f, const double* nv_f,
                    double* coor_c, double* nv_c, cudaStream_t s);
 int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nv_f, const double* nv_c,
@@ -51,9 +52,11 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // lf = precomputed y-line Thomas pivots 1/m_j (N of T)
 // solo: this grid's solve has the GPU to itself (allows the low-occupancy
 // variant on small levels)
+// tma: on the face form, sweeps of levels of at least VFS_TMA_MINCELLS
+// interior cells whose extents qualify run the tensor-copy kernel
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s,
-                 int cols = 0, bool solo = false);
+                 int cols = 0, bool solo = false, bool tma = false);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
 // FP16 diagonal-normalised copy of a level's aj-scaled operator (hidx layout), with
