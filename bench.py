@@ -72,8 +72,8 @@ def parse():
                     help="multigrid operator storage: FP32 face form on 11-slot levels (0), FP16 normalised by "
                          "the diagonal (1), FP32 assembled coefficients (2); FP32 arithmetic in every case")
     ap.add_argument("--restart", type=int, default=30)
-    ap.add_argument("--mg-tma", type=int, default=0, choices=[0, 1],
-                    help="finest face-form sweeps on the tensor-copy kernel (1) or the register-staged one (0)")
+    ap.add_argument("--mg-stage", type=int, default=0, choices=[0, 1],
+                    help="finest face-form sweeps staged in registers (0) or by tensor-memory copies (1)")
     ap.add_argument("--mg-grouped", type=int, default=0, choices=[0, 1],
                     help="batch: V-cycles as grouped launches over same-size grids (1) or each grid's own (0)")
     ap.add_argument("--orth", default="cgs", choices=["cgs", "cgs2"], help="Gram-Schmidt of the Arnoldi step")
@@ -636,7 +636,7 @@ def main():
     mixed = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
-                                mg_half=args.mg_half, mg_tma=args.mg_tma)
+                                mg_half=args.mg_half, mg_stage=args.mg_stage)
     other = capi.default_params(precision="mixed", rtol=args.rtol, nu1=nu1, nu2=nu2, restart=args.restart,
                                 div_tol=args.div_tol, maxit=400, orth=args.orth, **smooth,
                                 nu1_coarse=nuc[0], nu2_coarse=nuc[1], smooth_cols=args.smooth_cols,
@@ -741,8 +741,10 @@ def main():
     avg_ms = pms / plaunch if plaunch else None
     achieved = alg / (avg_ms / 1e3) / 1e9 if plaunch else None
     kname = {0: "k_smooth<float, FaceOp>", 1: "k_smooth<float, __half>", 2: "k_smooth<float, float>"}[args.mg_half]
-    if args.mg_half == 0 and args.mg_tma:
-        kname = "k_smooth_tma"
+    if args.mg_half == 0:
+        # the face form's full-width sweeps run the warp-row kernel (30-column
+        # tiles), or with --mg-stage 1 the tensor-copy one
+        kname = "k_smooth_tma" if args.mg_stage else "k_smooth_w<2>"
     traffic = ncu_traffic(kname + ":" + case.name)
     roof = {"kernel": kname + " (finest-level y-line sweep, x != 0)", "bound": "hbm", "achieved": achieved,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
@@ -782,7 +784,7 @@ def main():
                        "measures": "pressure projection steps/s with U* resident, mixed FP32-MG/FP64-FGMRES",
                        "mg_levels": case.levels, "rtol": args.rtol, "div_tol": args.div_tol, "nu": [nu1, nu2], "nu_coarse": nuc,
                        "restart": args.restart, "orth": args.orth, **smoother_config(args),
-                       "mg_operator": OPERATOR[args.mg_half], "mg_tma": args.mg_tma,
+                       "mg_operator": OPERATOR[args.mg_half], "mg_stage": args.mg_stage,
                        "l2": "working set > L2 (129 MB) per step", "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "latency_ms": {"p50": float(np.percentile(per_ms, 50)), "p99": float(np.percentile(per_ms, 99))},

@@ -143,15 +143,18 @@ typedef struct {
                          of the tick's graph, which measured faster on GB300
                          (64-grid batch: 801 against 683 solves/s).  Single
                          solves and served requests ignore it. */
-  int mg_tma;         /* 1: the finest level's sweeps on the FP32 face form
-                         (levels of at least 2^20 interior cells with even mx
-                         and my) run the tensor-copy kernel: one block per SM,
-                         a producer thread copying 16-row bands of x, the face
-                         weights, b and 1/m into a shared-memory ring
-                         (cp.async.bulk.tensor, mbarrier completion) while
-                         eight warps form residuals, solve columns and write;
-                         bit for bit the other kernel's results.  0 (the
-                         default): the register-staged kernel. */
+  int mg_stage;       /* How the finest level's sweeps on the FP32 face form
+                         (levels of at least 2^20 interior cells) stage their
+                         operands; both choices give the same results bit for
+                         bit.  0 (the default): in registers, four blocks per
+                         SM.  1: tensor-memory copies (mx and my even): one
+                         block per SM, a producer thread copying 16-row bands
+                         of x, the face weights, b and 1/m into a shared-
+                         memory ring (cp.async.bulk.tensor, mbarrier
+                         completion) while eight warps form residuals, solve
+                         columns and write; measured slower on GB300 (the
+                         copies alone take as long as the register-staged
+                         sweep). */
 } vfs_solve_params;
 /* The outer FGMRES iterates on the aj-scaled system (aj A) phi = aj b, the
  * form the reference's multigrid path assembles (poisson == -1 scales every

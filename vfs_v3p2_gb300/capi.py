@@ -66,7 +66,7 @@ class SolveParams(ctypes.Structure):
                 ("orth", ctypes.c_int), ("smooth_cols", ctypes.c_int), ("nu1_coarse", ctypes.c_int),
                 ("nu2_coarse", ctypes.c_int), ("mg_half", ctypes.c_int), ("smoother", ctypes.c_int),
                 ("cheb_hi", ctypes.c_double), ("cheb_ratio", ctypes.c_double), ("proj_exact", ctypes.c_int),
-                ("mg_grouped", ctypes.c_int), ("mg_tma", ctypes.c_int)]
+                ("mg_grouped", ctypes.c_int), ("mg_stage", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -211,7 +211,10 @@ def sweep_damping(params: SolveParams, finest: bool, post: bool) -> np.ndarray:
 def default_params(**kw) -> SolveParams:
     p = SolveParams()
     load().vfs_default_params(ctypes.byref(p))
+    names = {f[0] for f in SolveParams._fields_}
     for k, v in kw.items():
+        if k not in names:
+            raise AttributeError(f"vfs_solve_params has no field {k!r}")
         if k == "precision" and isinstance(v, str):
             v = {"fp64": VFS_FP64, "mixed": VFS_MIXED}[v]
         if k == "orth" and isinstance(v, str):

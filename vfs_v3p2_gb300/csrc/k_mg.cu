@@ -13,7 +13,7 @@
 #include <type_traits>
 
 #include "mg_tiles.cuh"
-#include "mg_tma.h"
+#include "mg_stage.h"
 #include "vfs_common.cuh"
 #include "vfs_kernels.h"
 #include "vfs_proj.h"
@@ -123,6 +123,15 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
   smooth_tile<MASK, T, TC, PAIR, UU, ZG>(A, lf, xi, b, xo, omega, TW, blockIdx.x, blockIdx.y, smraw);
 }
 
+// The face-form sweep with warp-row neighbours (smooth_tile_w): 30-column tiles.
+template <int U>
+__global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
+    k_smooth_w(OpView<float> A, const float* __restrict__ lf, const float* __restrict__ xi,
+               const float* __restrict__ b, float* __restrict__ xo, float omega) {
+  if (skipped(A.skip)) return;
+  extern __shared__ unsigned char smraw[];
+  smooth_tile_w<U>(A, lf, xi, b, xo, omega, blockIdx.x, blockIdx.y, smraw);
+}
 template <unsigned MASK, typename T, typename TC, bool PAIR, int UU, bool ZG>
 static void smooth_attrs1() {
   cudaFuncSetAttribute(k_smooth<MASK, T, TC, PAIR, UU, ZG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -151,12 +160,12 @@ static void smooth_launch(bool small, dim3 g, size_t sm, cudaStream_t s, const O
 
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s, int cols,
-                  bool solo, bool tma) {
+                  bool solo, int stage) {
   if constexpr (sizeof(T) == 4) {
     // the tensor-copy sweep; a configuration it cannot take (its launch
     // refused before running) falls back to the register-staged one
-    if (tma && A.ffi && xi && fits_ch(A.mask) &&
-        (size_t)(A.d.mx - 2) * (A.d.my - 2) * (A.d.mz - 2) >= (size_t)VFS_TMA_MINCELLS &&
+    if (stage == STAGE_TMA && A.ffi && xi && fits_ch(A.mask) &&
+        (size_t)(A.d.mx - 2) * (A.d.my - 2) * (A.d.mz - 2) >= (size_t)VFS_STAGE_MINCELLS &&
         smooth_tma_stages(A.d) > 0 && smooth_tma_err() &&
         launch_smooth_tma(A, lf, xi, b, xo, omega, smooth_tma_err(), s) == (int)cudaSuccess)
       return (int)cudaSuccess;
@@ -175,7 +184,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
   const int tw = smooth_tw<T>(ni, nj, nk, cols);
-  const size_t sm = (size_t)3 * tw * nj * sizeof(T);
+  const size_t sm = smooth_smem<T>(tw, nj);
   dim3 g((ni + tw - 1) / tw, nk);
   const bool ch = fits_ch(A.mask);
   // two-cell batches only when the sweep has the GPU to itself (one grid
@@ -184,7 +193,17 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
   const bool small = sizeof(T) == 4 && solo && (size_t)g.x * g.y < 2 * 152;  // (FP64: spills at two cells)
   bool done = false;
   if constexpr (sizeof(T) == 4) {
-    if (A.ffi && ch) {
+    if (A.ffi && ch && xi && cols == 0 && tw == 32 && !small && VFS_SMOOTH_W_U > 0) {
+      // automatic full-width tiles on the face form: the warp-row sweep
+      static bool wattr = false;
+      if (!wattr) {
+        cudaFuncSetAttribute(k_smooth_w<VFS_SMOOTH_W_U>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        wattr = true;
+      }
+      const dim3 gw((ni + SMOOTH_W_TW - 1) / SMOOTH_W_TW, nk);
+      k_smooth_w<VFS_SMOOTH_W_U><<<gw, VFS_SMOOTH_NT, smooth_smem<float>(32, nj), s>>>(A, lf, xi, b, xo, omega);
+      done = true;
+    } else if (A.ffi && ch) {
       smooth_launch<MASK_CH, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
       done = true;
     } else if (A.hcoef) {
@@ -539,7 +558,7 @@ int launch_scale_in(const Dims& d, const double* aj, const double* v, T* out, co
 
 #define INST(T)                                                                                                        \
   template int launch_apply_mg<T>(const OpView<T>&, const T*, const T*, T*, cudaStream_t);                            \
-  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int, bool, bool);      \
+  template int launch_smooth<T>(const OpView<T>&, const T*, const T*, const T*, T*, T, cudaStream_t, int, bool, int);      \
   template int launch_line_factors<T>(const Dims&, const double*, T*, cudaStream_t);                                  \
   template int launch_residual_restrict<T>(const OpView<T>&, const T*, const T*, const T*, const Dims&,           \
                                            const double*, int, int, int, T*, T*, cudaStream_t);                       \

@@ -42,7 +42,7 @@
 #include <cuda.h>
 
 #include "mg_tiles.cuh"
-#include "mg_tma.h"
+#include "mg_stage.h"
 #include "vfs_kernels.h"
 
 namespace vfs {

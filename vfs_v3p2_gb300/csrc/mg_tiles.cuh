@@ -422,6 +422,12 @@ __device__ __forceinline__ void line_solve(T* su, const T* sp, const T* sl, int 
   }
 }
 
+// Shared memory of a sweep tile: su, sp, sl (TW x nj each).
+template <typename T>
+__host__ __device__ inline size_t smooth_smem(int tw, int nj) {
+  return (size_t)3 * tw * nj * sizeof(T);
+}
+
 // Phase 1 of the sweep on the face form (FP32): U cells per thread batch,
 // every load issued before the arithmetic; writes su, sp, sl of the tile.
 // From a zero guess (ZG) the residual is b and only the j faces and aj are
@@ -726,6 +732,123 @@ __device__ __forceinline__ void smooth_tile(const OpView<T>& A, const T* __restr
     const T x0 = xi ? __ldg(xi + c) : T(0);
     const T v = x0 + omega * su[idx];
     if (i0 + il <= d.mx - 2) xo[c] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The face-form sweep with warp-row neighbours (x != 0).  A warp's 32 lanes
+// hold 32 consecutive columns of one row (i0 - 1 .. i0 + 30): lanes 1..30
+// are the tile's cells, lanes 0 and 31 their -i and +i halo.  Every lane
+// loads x of planes k, k + 1, k - 1, its +i face and aj; a cell's E, W, TE,
+// TW, BE, BW values, its -i face and the code bits of its i - 1 neighbour
+// are its neighbour lanes' (warp shuffles), so a cell keeps 17 loaded values
+// in registers instead of 24, and VFS_SMOOTH_W_U cells' loads fit in flight
+// per thread at the register budget of four blocks per SM.  The halo lanes
+// carry the periodic wrap (lane 0 of the first tile holds column mx - 2,
+// the lane past the last interior column holds column 1).  Inputs and
+// arithmetic per cell are face_phase1's, so results are bit for bit the
+// one-cell-per-thread sweep's.  Tiles are VFS_SMOOTH_W_TW = 30 columns
+// wide; the line arrays keep 32 columns (the halo lanes' stay zero).
+// ---------------------------------------------------------------------------
+#ifndef VFS_SMOOTH_W_U
+#define VFS_SMOOTH_W_U 2  // rows (cells) whose loads one thread issues together
+#endif
+constexpr int SMOOTH_W_TW = 30;
+
+template <int U>
+__device__ __forceinline__ void smooth_tile_w(const OpView<float>& A, const float* __restrict__ lf,
+                                              const float* __restrict__ xi, const float* __restrict__ b,
+                                              float* __restrict__ xo, float omega, int bx, int by,
+                                              unsigned char* smraw) {
+  static_assert(VFS_SMOOTH_NT == 256, "eight warps per block");
+  const Dims d = A.d;
+  const int nj = d.my - 2, sy = d.mx, sz = d.mx * d.my;
+  const int k = 1 + by, i0 = 1 + SMOOTH_W_TW * bx;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* su = (float*)smraw;  // [nj][32]
+  float* sp = su + 32 * nj;
+  float* sl = sp + 32 * nj;
+  // the lane's column, periodic wraps folded in, clamped past the ghost column
+  int il = i0 - 1 + lane;
+  if (d.ip && il == 0) il = d.mx - 2;
+  else if (d.ip && il == d.mx - 1) il = 1;
+  il = min(il, d.mx - 1);
+  const bool comp = lane >= 1 && lane <= SMOOTH_W_TW && i0 - 1 + lane <= d.mx - 2;  // the lane is a cell
+  const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
+  const int pk = k * sz + il;
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  for (int jb = warp; jb < nj; jb += 8 * U) {
+    float xc[U], xn[U], xs[U], xt[U], xb[U], gjc[U], gjs[U], ajr[U], ajb[U], bb[U], inv[U];
+    float2 fic[U], fkc[U], fkb[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int j = 1 + min(jb + 8 * u, nj - 1);
+      const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
+      const int c = pk + j * sy;
+      xc[u] = __ldg(xi + c);
+      xt[u] = __ldg(xi + c + okT);
+      xb[u] = __ldg(xi + c + okB);
+      fic[u] = __ldg(A.ffi + c);
+      ajr[u] = __ldg(A.faj + c);
+      xn[u] = comp ? __ldg(xi + c + ojN) : 0.f;
+      xs[u] = comp ? __ldg(xi + c + ojS) : 0.f;
+      fkc[u] = comp ? __ldg(A.ffk + c) : make_float2(0.f, 0.f);
+      fkb[u] = comp ? __ldg(A.ffk + c + okB) : make_float2(0.f, 0.f);
+      gjc[u] = comp ? __ldg(A.ffj + c) : 0.f;
+      gjs[u] = comp ? __ldg(A.ffj + c + ojS) : 0.f;
+      ajb[u] = comp ? __ldg(A.faj + c + okB) : 0.f;
+      bb[u] = comp ? __ldg(b + c) : 0.f;
+      inv[u] = comp ? __ldg(lf + c) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int jl = jb + 8 * u;
+      FaceData f;
+      float x11[19];
+      x11[CP] = xc[u];
+      x11[EP] = __shfl_down_sync(FULL, xc[u], 1);
+      x11[WP] = __shfl_up_sync(FULL, xc[u], 1);
+      x11[NP] = xn[u];
+      x11[SP] = xs[u];
+      x11[TP] = xt[u];
+      x11[BP] = xb[u];
+      x11[TE] = __shfl_down_sync(FULL, xt[u], 1);
+      x11[TW] = __shfl_up_sync(FULL, xt[u], 1);
+      x11[BE] = __shfl_down_sync(FULL, xb[u], 1);
+      x11[BW] = __shfl_up_sync(FULL, xb[u], 1);
+      f.fic = fic[u];
+      f.fiw.x = __shfl_up_sync(FULL, fic[u].x, 1);
+      f.fiw.y = __shfl_up_sync(FULL, fic[u].y, 1);
+      const float ajw = __shfl_up_sync(FULL, ajr[u], 1);
+      if (jl >= nj) continue;  // warp-uniform
+      f.fkc = fkc[u];
+      f.fkb = fkb[u];
+      f.gjc = gjc[u];
+      f.gjs = gjs[u];
+      f.aj = face_aj(ajr[u]);
+      f.cc = face_code(ajr[u]);
+      f.cw = face_code(ajw);
+      f.cb = face_code(ajb[u]);
+      const bool live = comp && f.aj != 0.f;
+      const float ax = face_row(f, x11);
+      const float a = jl > 0 ? f.aj * f.gjs : 0.f, cn = jl < nj - 1 ? f.aj * f.gjc : 0.f;
+      const int idx = jl * 32 + lane;
+      su[idx] = live ? (bb[u] - ax) * inv[u] : 0.f;
+      sp[idx] = live ? a * inv[u] : 0.f;
+      sl[idx] = live ? cn * inv[u] : 0.f;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) line_solve<float>(su, sp, sl, nj, 32, threadIdx.x);
+  __syncthreads();
+  constexpr int U3 = VFS_SMOOTH_U3;
+#pragma unroll U3
+  for (int idx = threadIdx.x; idx < 32 * nj; idx += VFS_SMOOTH_NT) {
+    const int l = idx & 31, jl = idx >> 5;
+    const int i = min(i0 - 1 + l, d.mx - 2);
+    const int c = k * sz + (1 + jl) * sy + i;
+    const float v = __ldg(xi + c) + omega * su[idx];
+    if (l >= 1 && l <= SMOOTH_W_TW && i0 - 1 + l <= d.mx - 2) xo[c] = v;
   }
 }
 

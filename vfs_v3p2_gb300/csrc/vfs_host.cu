@@ -24,7 +24,7 @@
 
 #include "mg_group.h"
 #include "mg_tiles.cuh"
-#include "mg_tma.h"
+#include "mg_stage.h"
 #include "vfs_common.cuh"
 #include "vfs_gpu.h"
 #include "vfs_kernels.h"
@@ -198,7 +198,7 @@ struct Grid {
   int* comp = nullptr;   // finest-level region labels (device), when ncomp > 1
   cudaGraphExec_t ig_exec = nullptr;  // captured Arnoldi iteration
   int ig_prec = -1, ig_nu1 = -1, ig_nu2 = -1, ig_orth = -1, ig_cols = -1, ig_nu1c = -2, ig_nu2c = -2, ig_half = -1, ig_solo = -1;
-  int ig_smoother = -1, ig_tma = -1;
+  int ig_smoother = -1, ig_stage = -1;
   double ig_cheb_hi = 0., ig_cheb_ratio = 0.;
   unsigned long long ig_kernels = 0;  // kernels per replay
   double ig_omega = 0.;
@@ -447,7 +447,7 @@ struct MGCfg {
   bool half;       // FP16 normalised operator (FP32 multigrid only)
   bool face;       // FP32 face form on 11-slot levels (FP32 multigrid only)
   bool solo;       // the grid's solve runs alone
-  bool tma;        // the finest face-form sweeps run the tensor-copy kernel
+  int stage;       // how the finest face-form sweeps stage their operands (SweepStage)
   int pre(int l) const { return l == top ? nu1 : nu1c; }
   int post(int l) const { return l == top ? nu2 : nu2c; }
 };
@@ -463,7 +463,7 @@ size_t n_interior(const Dims& d) { return (size_t)(d.mx - 2) * (d.my - 2) * (d.m
 // b, the line pivots 1/m and writes x: (slots + 4) words per interior cell.
 template <typename T>
 void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, int cols, bool solo,
-                   cudaStream_t s, bool tma = false) {
+                   cudaStream_t s, int stage = STAGE_REGS) {
   // x != 0: the coefficient slots (FP16 or T), x, b and 1/m read, x written;
   // from a zero guess: the centre (not with the FP16 operator), SP and NP
   // slots, b and 1/m read, x written
@@ -475,7 +475,7 @@ void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T*
   int rc;
   {
     Probed pr(VFS_PROBE_ALL, s, xi ? "k_smooth" : "k_smooth (zero guess)", l, bytes);
-    rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo, tma);
+    rc = launch_smooth<T>(A, lf, xi, b, xo, omega, s, cols, solo, stage);
   }
   dbg("smooth", l, rc, s);
 }
@@ -550,7 +550,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
     if (cur) run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s, c.tma && l == c.top);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 0, q), c.cols, c.solo, s, l == c.top ? c.stage : STAGE_REGS);
     cur = o;
   }
   run.close();
@@ -585,7 +585,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   for (int r = 0; r < c.post(l); r++, q++) {
     T* o = bufs[q & 1];
     run.add(run_probe, s, sweep_bytes);
-    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s, c.tma && l == c.top);
+    smooth_probed<T>(l, A, lf, cur, b, o, (T)c.w(l, 1, r), c.cols, c.solo, s, l == c.top ? c.stage : STAGE_REGS);
     cur = o;
   }
   run.close();
@@ -628,7 +628,7 @@ MGCfg mgcfg(const vfs_solve_params& p, int top, bool half_ok = true) {
   c.half = p.precision == VFS_MIXED && p.mg_half == 1 && half_ok;
   c.face = p.precision == VFS_MIXED && p.mg_half == 0;
   c.solo = false;
-  c.tma = p.mg_tma != 0;
+  c.stage = p.mg_stage;
   return c;
 }
 
@@ -825,7 +825,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   if (g.ig_exec && g.ig_prec == prec && g.ig_nu1 == p.nu1 && g.ig_nu2 == p.nu2 && g.ig_omega == p.omega &&
       g.ig_orth == p.orth && g.ig_cols == p.smooth_cols && g.ig_nu1c == p.nu1_coarse && g.ig_nu2c == p.nu2_coarse &&
       g.ig_half == p.mg_half && g.ig_solo == (int)g.solo && g.ig_smoother == p.smoother &&
-      g.ig_cheb_hi == p.cheb_hi && g.ig_cheb_ratio == p.cheb_ratio && g.ig_tma == p.mg_tma) {
+      g.ig_cheb_hi == p.cheb_hi && g.ig_cheb_ratio == p.cheb_ratio && g.ig_stage == p.mg_stage) {
     *out = g.ig_exec;
     return VFS_OK;
   }
@@ -861,7 +861,7 @@ int iteration_graph(vfs_ctx* ctx, Grid& g, const vfs_solve_params& p, cudaGraphE
   g.ig_smoother = p.smoother;
   g.ig_cheb_hi = p.cheb_hi;
   g.ig_cheb_ratio = p.cheb_ratio;
-  g.ig_tma = p.mg_tma;
+  g.ig_stage = p.mg_stage;
   *out = g.ig_exec;
   return VFS_OK;
 }
@@ -952,7 +952,7 @@ int check_params(vfs_ctx* ctx, const vfs_solve_params* p) {
   if (p->precision != VFS_FP64 && p->precision != VFS_MIXED) return fail(ctx, VFS_ERR_ARG, "unknown precision");
   if (p->proj_exact != 0 && p->proj_exact != 1) return fail(ctx, VFS_ERR_ARG, "proj_exact must be 0 or 1");
   if (p->mg_grouped != 0 && p->mg_grouped != 1) return fail(ctx, VFS_ERR_ARG, "mg_grouped must be 0 or 1");
-  if (p->mg_tma != 0 && p->mg_tma != 1) return fail(ctx, VFS_ERR_ARG, "mg_tma must be 0 or 1");
+  if (p->mg_stage != STAGE_REGS && p->mg_stage != STAGE_TMA) return fail(ctx, VFS_ERR_ARG, "mg_stage must be 0 or 1");
   if (p->orth != VFS_ORTH_CGS && p->orth != VFS_ORTH_CGS2)
     return fail(ctx, VFS_ERR_ARG, "orth must be VFS_ORTH_CGS or VFS_ORTH_CGS2");
   if (p->smooth_cols != 0 && p->smooth_cols != 8 && p->smooth_cols != 16 && p->smooth_cols != 32)
@@ -1209,7 +1209,7 @@ int job_post_eval(vfs_ctx* ctx, Job& J) {
   // with the step's divergence measured, div_limited reports the outcome
   if (J.post && J.p.div_tol > 0.) J.info.div_limited = J.divmax > J.p.div_tol ? 1 : 0;
   // a bounded wait of the tensor-copy sweep that ran out leaves garbage
-  if (J.p.mg_tma && smooth_tma_take_error())
+  if (J.p.mg_stage == STAGE_TMA && smooth_tma_take_error())
     return job_fail(ctx, J, fail(ctx, VFS_ERR_CUDA, "tensor-copy sweep: a bounded wait ran out"));
   J.phase = J_DONE;
   return VFS_OK;
@@ -1388,7 +1388,7 @@ void group_item(Grid& g, const GOp<T>& op, const MGCfg& c, const int* skip, int*
       t.gx = (ni + t.tw - 1) / t.tw;
       t.gy = nk;
       *blocks = t.gx * nk;
-      *smem = (size_t)3 * t.tw * nj * sizeof(T);
+      *smem = smooth_smem<T>(t.tw, nj);
       const int zg = op.x ? 0 : 1;
       *kind = (face ? GK_SMOOTH_FACE : ch ? GK_SMOOTH_CH : GK_SMOOTH_ALL) + zg;
       break;
@@ -1805,7 +1805,7 @@ void vfs_default_params(vfs_solve_params* p) {
   p->mg_half = 0;
   p->proj_exact = 0;
   p->mg_grouped = 0;
-  p->mg_tma = 0;
+  p->mg_stage = STAGE_REGS;
 }
 
 int vfs_create(const vfs_config* cfg, vfs_ctx** out) {
@@ -3027,6 +3027,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
   if (int r_ = check_idle(ctx, gp)) return r_;
   Grid& g = *gp;
   if (!g.lhs) return fail(ctx, VFS_ERR_STATE, "vfs_poisson_lhs has not run");
+  if (int r_ = check_params(ctx, p)) return r_;
   const size_t N = ncell(g.d);
   Level& F = g.lev[g.L - 1];
   double* dv;
@@ -3039,7 +3040,7 @@ int vfs_apply_precond(vfs_ctx* ctx, int grid, int precision, const vfs_solve_par
     if (!r && cudaMalloc(&dz, N * 4) != cudaSuccess) r = VFS_ERR_NOMEM;
     if (!r) cudaMemsetAsync(dz, 0, N * 4, g.s);
     if (!r) r = precond<float>(ctx, g, *p, dv, dz, F.x32[1], nullptr, g.s, true, true);
-    if (!r && p->mg_tma) {
+    if (!r && p->mg_stage == STAGE_TMA) {
       cudaStreamSynchronize(g.s);
       if (smooth_tma_take_error()) r = fail(ctx, VFS_ERR_CUDA, "tensor-copy sweep: a bounded wait ran out");
     }

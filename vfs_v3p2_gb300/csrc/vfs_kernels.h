@@ -52,11 +52,12 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // lf = precomputed y-line Thomas pivots 1/m_j (N of T)
 // solo: this grid's solve has the GPU to itself (allows the low-occupancy
 // variant on small levels)
-// tma: on the face form, sweeps of levels of at least VFS_TMA_MINCELLS
-// interior cells whose extents qualify run the tensor-copy kernel
+// stage: on the face form, sweeps of levels of at least VFS_STAGE_MINCELLS
+// interior cells run the kernel that stages operands this way (SweepStage:
+// registers or tensor-memory copies)
 template <typename T>
 int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* xo, T omega, cudaStream_t s,
-                 int cols = 0, bool solo = false, bool tma = false);
+                 int cols = 0, bool solo = false, int stage = 0);
 template <typename T>
 int launch_line_factors(const Dims& d, const double* mcoef, T* lf, cudaStream_t s);
 // FP16 diagonal-normalised copy of a level's aj-scaled operator (hidx layout), with
