@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 def _cases():
     return {
-        # mx = 258 (mx mod 4 = 2), 126 rows = 7 full 16-row bands + 14, 9 full 14-row bands
+        # mx = 258 (mx mod 4 = 2), 128 rows = 8 full 16-row bands
         "sphere_256x128x128": (synth.c2_sphere(), (1, 0, 1)),
         # mx = 256 (mx mod 4 = 0), a partial last tile (254 = 7 x 32 + 30), partial bands (66 = 4 x 16 + 2 = 4 x 14 + 10)
         "channel_254x66x64": (synth.channel_case(254, 66, 64, seed=71, levels=2), (1, 0, 1)),

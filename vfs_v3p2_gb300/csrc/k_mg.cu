@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(VFS_SMOOTH_NT, PAIR ? VFS_SMOOTH_MINB_HALF : (
 
 // The face-form sweep with warp-row neighbours (smooth_tile_w): 30-column tiles.
 template <int U>
-__global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_MINB)
+__global__ void __launch_bounds__(VFS_SMOOTH_NT, VFS_SMOOTH_W_MINB)
     k_smooth_w(OpView<float> A, const float* __restrict__ lf, const float* __restrict__ xi,
                const float* __restrict__ b, float* __restrict__ xo, float omega) {
   if (skipped(A.skip)) return;

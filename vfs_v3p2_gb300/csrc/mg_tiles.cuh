@@ -753,6 +753,9 @@ __device__ __forceinline__ void smooth_tile(const OpView<T>& A, const T* __restr
 #ifndef VFS_SMOOTH_W_U
 #define VFS_SMOOTH_W_U 2  // rows (cells) whose loads one thread issues together
 #endif
+#ifndef VFS_SMOOTH_W_MINB
+#define VFS_SMOOTH_W_MINB 4  // resident blocks per SM its register budget allows (4: 64 registers)
+#endif
 constexpr int SMOOTH_W_TW = 30;
 
 template <int U>
