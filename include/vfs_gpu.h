@@ -358,6 +358,13 @@ int vfs_grid_components(vfs_ctx* ctx, int grid, int* finest, int* coarsest);
  * post != 0 for the post-sweeps.  n must equal that side's sweep count.
  * VFS_ERR_ARG for invalid parameters. */
 int vfs_sweep_damping(const vfs_solve_params* p, int finest, int post, double* w, int n);
+/* Test hook of the tensor-copy sweep (mg_stage = 1): from the next launch on,
+ * its producer leaves out the 1/m copies of band `band` of every block (-1,
+ * the default: none), so that band's bounded wait (about 0.2 s) runs out;
+ * the solve or preconditioner call then fails with VFS_ERR_CUDA ("a bounded
+ * wait ran out") and the context stays usable.  Process-wide; returns
+ * VFS_OK. */
+int vfs_debug_tma_drop(int band);
 
 /* ---- serving: continuous batching of projection steps ----
  * A request is one projection step of one grid (the simulation stream's

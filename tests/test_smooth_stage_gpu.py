@@ -111,3 +111,33 @@ def test_warp_row_sweep_bitexact(gpu_ctx, name):
         assert np.array_equal(z[0], z[32]), np.abs(z[0] - z[32]).max()
     finally:
         gpu_ctx.grid_destroy(gid)
+
+
+def test_tma_bounded_wait_reports_and_recovers(gpu_ctx):
+    """A tensor-copy sweep whose copies never all arrive (the test hook
+    leaves out one band's 1/m copies in every block) ends its bounded wait
+    after about 0.2 s: the call fails with VFS_ERR_CUDA and the reason, and
+    the context stays usable -- the next call gives the register sweep's
+    result bit for bit."""
+    case = synth.channel_case(128, 64, 128, seed=77, levels=3)
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, case.levels, case.immersed)
+    lib = capi.load()
+    try:
+        gpu_ctx.poisson_lhs(gid)
+        rng = np.random.default_rng(78)
+        v = rng.normal(size=g.nvert.shape)
+        v[~_fluid(g.nvert)] = 0.0
+        p1 = capi.default_params(precision="mixed", mg_stage=1)
+        assert lib.vfs_debug_tma_drop(0) == 0
+        try:
+            with pytest.raises(capi.VfsError) as e:
+                gpu_ctx.apply_precond(gid, capi.VFS_MIXED, p1, v)
+        finally:
+            lib.vfs_debug_tma_drop(-1)
+        assert e.value.code == 2 and "bounded wait" in str(e.value)
+        z1 = gpu_ctx.apply_precond(gid, capi.VFS_MIXED, p1, v)
+        z0 = gpu_ctx.apply_precond(gid, capi.VFS_MIXED, capi.default_params(precision="mixed"), v)
+        assert np.isfinite(z0).all() and np.array_equal(z1, z0)
+    finally:
+        gpu_ctx.grid_destroy(gid)

@@ -148,6 +148,7 @@ SIGNATURES = {
     "vfs_grid_components": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "vfs_probe_record": ([_P, _I, ctypes.c_char_p, _I, ctypes.POINTER(_I), _DP, _DP], _I),
     "vfs_sweep_damping": ([ctypes.POINTER(SolveParams), _I, _I, _DP, _I], _I),
+    "vfs_debug_tma_drop": ([_I], _I),
     "vfs_host_register": ([_P, ctypes.c_ulonglong], _I),
     "vfs_host_unregister": ([_P], _I),
     "vfs_host_alloc": ([ctypes.POINTER(_P), ctypes.c_ulonglong], _I),

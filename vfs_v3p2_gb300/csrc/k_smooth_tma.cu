@@ -34,11 +34,15 @@
 //
 // Every mbarrier wait is bounded (about 0.2 s of clock cycles); a wait that
 // runs out records an error in *err and raises the block's abort flag, after
-// which the other waits return at once; the block carries on through the
-// same barriers (its results are then garbage, and the host reports the
-// error), so that no thread is left waiting on another; before exiting, one
-// consumer waits again (bounded, whatever the flag) for the last copies
-// issued.
+// which the other waits return at once and the producer issues no further
+// band (so a stage whose phase did not complete is never armed again); the
+// consumers carry on through the same barriers (their results are then
+// garbage, and the host reports the error), so that no thread is left
+// waiting on another.  Before the block exits, one thread waits again
+// (bounded, whatever the flag) for the last band issued on each stage, so no
+// copy is still writing the block's shared memory.  drop >= 0 (a test hook)
+// leaves out the 1/m copies of the block's band number drop, so that band's
+// wait runs out.
 #include <cuda.h>
 
 #include "mg_tiles.cuh"
@@ -115,10 +119,10 @@ struct TmaMaps {
 __global__ void __launch_bounds__(TMA_NT, 1)
     k_smooth_tma(const __grid_constant__ TmaMaps maps, OpView<float> A, const float* __restrict__ lf,
                  const float* __restrict__ xi, const float* __restrict__ b, float* __restrict__ xo, float omega,
-                 int stages, int* err) {
+                 int stages, int* err, int drop) {
   if (skipped(A.skip)) return;
   extern __shared__ __align__(128) unsigned char smraw[];
-  __shared__ int abort_flag;
+  __shared__ int abort_flag, n_issued;
   volatile int* abort = &abort_flag;
   const Dims d = A.d;
   const int nj = d.my - 2, ni = d.mx - 2, nk = d.mz - 2;
@@ -133,6 +137,7 @@ __global__ void __launch_bounds__(TMA_NT, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     abort_flag = 0;
+    n_issued = 0;
     for (int s = 0; s < stages; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], TMA_NCONS / 32);
@@ -142,143 +147,153 @@ __global__ void __launch_bounds__(TMA_NT, 1)
   __syncthreads();
 
   if (warp == TMA_NCONS / 32) {
-    // producer: one lane issues the copies of every (tile, band) in order
-    if (lane != 0) return;
+    // producer: one lane issues the copies of every (tile, band) in order,
+    // until the abort flag is raised
+    if (lane == 0) {
+      long long q = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+        const int bx = t % gx, k = 1 + t / gx;
+        const int kb = (k == 1 && d.kp) ? d.mz - 2 : k - 1, kt = (k == d.mz - 2 && d.kp) ? 1 : k + 1;
+        const int c0 = bx * TMA_TW;  // column i0 - 1
+        for (int band = 0; band < nb; band++, q++) {
+          const int s = (int)(q % stages);
+          const unsigned use = (unsigned)(q / stages);
+          if (*abort) stop = true;
+          else if (use > 0) mbar_wait(&empty[s], (use - 1) & 1, err, 1, abort);
+          if (stop || *abort) {
+            stop = true;
+            break;
+          }
+          unsigned char* st = ring + (size_t)s * TMA_STAGE;
+          mbar_expect_tx(&full[s], TMA_TX);
+          const int pr = band * (TMA_R / 2);  // first row pair: rows 16 band, 16 band + 1 (= b0 - 1, b0)
+          const int b0 = 1 + band * TMA_R;
+          auto pair4 = [&](int slot, const CUtensorMap* m, int plane) {
+            unsigned char* dst = st + slot * TMA_A4;
+            tma_load3(dst, m, c0, pr, plane, &full[s]);                             // even rows
+            tma_load3(dst + TMA_HALF, m, d.mx + c0 - shift, pr, plane, &full[s]);  // odd rows
+          };
+          pair4(S_XB, &maps.x, kb);
+          pair4(S_XC, &maps.x, k);
+          pair4(S_XT, &maps.x, kt);
+          pair4(S_FJ, &maps.fj, k);
+          pair4(S_AJ, &maps.aj, k);
+          pair4(S_AJB, &maps.aj, kb);
+          pair4(S_B, &maps.b, k);
+          if (q != drop) pair4(S_LF, &maps.lf, k);
+          unsigned char* e8 = st + 8 * TMA_A4;
+          tma_load3(e8, &maps.fi, c0, b0, k, &full[s]);
+          tma_load3(e8 + TMA_A8, &maps.fk, c0, b0, k, &full[s]);
+          tma_load3(e8 + 2 * TMA_A8, &maps.fk, c0, b0, kb, &full[s]);
+        }
+      }
+      n_issued = (int)q;  // bands whose copies were issued
+    }
+  } else {
+    // consumers: 8 warps; a band's 16 rows x 32 columns are two cells per
+    // thread, rows 1 + warp and 9 + warp of the band's staged rows, column
+    // 1 + lane of the staged columns.  A cell's place in a stage is the same in
+    // every band, so its byte offsets are formed once.
+    const int il = lane;
+    // byte offset of staged row r (0 .. 17 from the band's first row) and
+    // staged column e (0 .. 39 from column i0 - 1) in a 4-byte array's slot
+    auto off4 = [&](int r, int e) -> int { return (r & 1) * TMA_HALF + ((r >> 1) * TMA_BW + e + (r & 1) * shift) * 4; };
+    int o4[2][5];   // per cell: C E W N S in a 4-byte slot (the same for every array and plane)
+    int o8[2][2];   // per cell: 8-byte (i), (i - 1) of rows 1..16
+    for (int u = 0; u < 2; u++) {
+      const int r = 1 + warp + 8 * u, e = 1 + il;
+      o4[u][0] = off4(r, e);
+      o4[u][1] = off4(r, e + 1);
+      o4[u][2] = off4(r, e - 1);
+      o4[u][3] = off4(r + 1, e);
+      o4[u][4] = off4(r - 1, e);
+      o8[u][0] = ((r - 1) * TMA_BW + e) * 8;
+      o8[u][1] = ((r - 1) * TMA_BW + e - 1) * 8;
+    }
     long long q = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const int bx = t % gx, k = 1 + t / gx;
-      const int kb = (k == 1 && d.kp) ? d.mz - 2 : k - 1, kt = (k == d.mz - 2 && d.kp) ? 1 : k + 1;
-      const int c0 = bx * TMA_TW;  // column i0 - 1
+      const int i0 = 1 + bx * TMA_TW;
+      const int i = min(i0 + il, d.mx - 2);
+      const bool col_in = i0 + il <= d.mx - 2;
       for (int band = 0; band < nb; band++, q++) {
         const int s = (int)(q % stages);
-        const unsigned use = (unsigned)(q / stages);
-        if (use > 0) mbar_wait(&empty[s], (use - 1) & 1, err, 1, abort);
-        unsigned char* st = ring + (size_t)s * TMA_STAGE;
-        mbar_expect_tx(&full[s], TMA_TX);
-        const int pr = band * (TMA_R / 2);  // first row pair: rows 16 band, 16 band + 1 (= b0 - 1, b0)
-        const int b0 = 1 + band * TMA_R;
-        auto pair4 = [&](int slot, const CUtensorMap* m, int plane) {
-          unsigned char* dst = st + slot * TMA_A4;
-          tma_load3(dst, m, c0, pr, plane, &full[s]);                             // even rows
-          tma_load3(dst + TMA_HALF, m, d.mx + c0 - shift, pr, plane, &full[s]);  // odd rows
-        };
-        pair4(S_XB, &maps.x, kb);
-        pair4(S_XC, &maps.x, k);
-        pair4(S_XT, &maps.x, kt);
-        pair4(S_FJ, &maps.fj, k);
-        pair4(S_AJ, &maps.aj, k);
-        pair4(S_AJB, &maps.aj, kb);
-        pair4(S_B, &maps.b, k);
-        pair4(S_LF, &maps.lf, k);
-        unsigned char* e8 = st + 8 * TMA_A4;
-        tma_load3(e8, &maps.fi, c0, b0, k, &full[s]);
-        tma_load3(e8 + TMA_A8, &maps.fk, c0, b0, k, &full[s]);
-        tma_load3(e8 + 2 * TMA_A8, &maps.fk, c0, b0, kb, &full[s]);
-      }
-    }
-    return;
-  }
-
-  // consumers: 8 warps; a band's 16 rows x 32 columns are two cells per
-  // thread, rows 1 + warp and 9 + warp of the band's staged rows, column
-  // 1 + lane of the staged columns.  A cell's place in a stage is the same in
-  // every band, so its byte offsets are formed once.
-  const int il = lane;
-  // byte offset of staged row r (0 .. 17 from the band's first row) and
-  // staged column e (0 .. 39 from column i0 - 1) in a 4-byte array's slot
-  auto off4 = [&](int r, int e) -> int { return (r & 1) * TMA_HALF + ((r >> 1) * TMA_BW + e + (r & 1) * shift) * 4; };
-  int o4[2][12];  // per cell: C E W N S (plane k) | C E W (plane kt) | C E W (plane kb) | S row of ffj
-  int o8[2][2];   // per cell: 8-byte (i), (i - 1) of rows 1..16
-  for (int u = 0; u < 2; u++) {
-    const int r = 1 + warp + 8 * u, e = 1 + il;
-    o4[u][0] = off4(r, e);
-    o4[u][1] = off4(r, e + 1);
-    o4[u][2] = off4(r, e - 1);
-    o4[u][3] = off4(r + 1, e);
-    o4[u][4] = off4(r - 1, e);
-    o8[u][0] = ((r - 1) * TMA_BW + e) * 8;
-    o8[u][1] = ((r - 1) * TMA_BW + e - 1) * 8;
-  }
-  long long q = 0;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int bx = t % gx, k = 1 + t / gx;
-    const int i0 = 1 + bx * TMA_TW;
-    const int i = min(i0 + il, d.mx - 2);
-    const bool col_in = i0 + il <= d.mx - 2;
-    for (int band = 0; band < nb; band++, q++) {
-      const int s = (int)(q % stages);
-      mbar_wait(&full[s], (unsigned)((q / stages) & 1), err, 2, abort);
-      const unsigned char* st = ring + (size_t)s * TMA_STAGE;
-      auto ld4 = [&](int slot, int off) -> float { return *(const float*)(st + slot * TMA_A4 + off); };
-      auto ld8 = [&](int slot, int off) -> float2 { return *(const float2*)(st + 8 * TMA_A4 + slot * TMA_A8 + off); };
-#pragma unroll
-      for (int u = 0; u < 2; u++) {
-        const int jl = band * TMA_R + warp + 8 * u;  // row index within the tile (j = 1 + jl)
-        if (jl >= nj) continue;
-        const int j = 1 + jl;
-        FaceData f;
-        float x11[19];
-        float bb, inv;
-        const bool seam = (d.ip && (i == 1 || i == d.mx - 2)) || (d.jp && (j == 1 || j == d.my - 2));
-        if (seam) {
-          face_gather(A, xi, i, j, k, f, x11);
-          const int c = cidx(d, i, j, k);
-          bb = __ldg(b + c);
-          inv = __ldg(lf + c);
-        } else {
-          const int oc = o4[u][0], oe = o4[u][1], ow = o4[u][2], on = o4[u][3], os = o4[u][4];
-          const float ajc = ld4(S_AJ, oc), ajw = ld4(S_AJ, ow), ajb = ld4(S_AJB, oc);
-          f.fic = ld8(0, o8[u][0]);
-          f.fiw = ld8(0, o8[u][1]);
-          f.fkc = ld8(1, o8[u][0]);
-          f.fkb = ld8(2, o8[u][0]);
-          f.gjc = ld4(S_FJ, oc);
-          f.gjs = ld4(S_FJ, os);
-          f.aj = face_aj(ajc);
-          f.cc = face_code(ajc);
-          f.cw = face_code(ajw);
-          f.cb = face_code(ajb);
-          x11[CP] = ld4(S_XC, oc);
-          x11[EP] = ld4(S_XC, oe);
-          x11[WP] = ld4(S_XC, ow);
-          x11[NP] = ld4(S_XC, on);
-          x11[SP] = ld4(S_XC, os);
-          x11[TP] = ld4(S_XT, oc);
-          x11[BP] = ld4(S_XB, oc);
-          x11[TE] = ld4(S_XT, oe);
-          x11[BE] = ld4(S_XB, oe);
-          x11[TW] = ld4(S_XT, ow);
-          x11[BW] = ld4(S_XB, ow);
-          bb = ld4(S_B, oc);
-          inv = ld4(S_LF, oc);
+        mbar_wait(&full[s], (unsigned)((q / stages) & 1), err, 2, abort);
+        const unsigned char* st = ring + (size_t)s * TMA_STAGE;
+        auto ld4 = [&](int slot, int off) -> float { return *(const float*)(st + slot * TMA_A4 + off); };
+        auto ld8 = [&](int slot, int off) -> float2 { return *(const float2*)(st + 8 * TMA_A4 + slot * TMA_A8 + off); };
+  #pragma unroll
+        for (int u = 0; u < 2; u++) {
+          const int jl = band * TMA_R + warp + 8 * u;  // row index within the tile (j = 1 + jl)
+          if (jl >= nj) continue;
+          const int j = 1 + jl;
+          FaceData f;
+          float x11[19];
+          float bb, inv;
+          const bool seam = (d.ip && (i == 1 || i == d.mx - 2)) || (d.jp && (j == 1 || j == d.my - 2));
+          if (seam) {
+            face_gather(A, xi, i, j, k, f, x11);
+            const int c = cidx(d, i, j, k);
+            bb = __ldg(b + c);
+            inv = __ldg(lf + c);
+          } else {
+            const int oc = o4[u][0], oe = o4[u][1], ow = o4[u][2], on = o4[u][3], os = o4[u][4];
+            const float ajc = ld4(S_AJ, oc), ajw = ld4(S_AJ, ow), ajb = ld4(S_AJB, oc);
+            f.fic = ld8(0, o8[u][0]);
+            f.fiw = ld8(0, o8[u][1]);
+            f.fkc = ld8(1, o8[u][0]);
+            f.fkb = ld8(2, o8[u][0]);
+            f.gjc = ld4(S_FJ, oc);
+            f.gjs = ld4(S_FJ, os);
+            f.aj = face_aj(ajc);
+            f.cc = face_code(ajc);
+            f.cw = face_code(ajw);
+            f.cb = face_code(ajb);
+            x11[CP] = ld4(S_XC, oc);
+            x11[EP] = ld4(S_XC, oe);
+            x11[WP] = ld4(S_XC, ow);
+            x11[NP] = ld4(S_XC, on);
+            x11[SP] = ld4(S_XC, os);
+            x11[TP] = ld4(S_XT, oc);
+            x11[BP] = ld4(S_XB, oc);
+            x11[TE] = ld4(S_XT, oe);
+            x11[BE] = ld4(S_XB, oe);
+            x11[TW] = ld4(S_XT, ow);
+            x11[BW] = ld4(S_XB, ow);
+            bb = ld4(S_B, oc);
+            inv = ld4(S_LF, oc);
+          }
+          const bool live = col_in && f.aj != 0.f;
+          const float ax = face_row(f, x11);
+          const float a = jl > 0 ? f.aj * f.gjs : 0.f, cn = jl < nj - 1 ? f.aj * f.gjc : 0.f;
+          const int idx = jl * TMA_TW + il;
+          su[idx] = live ? (bb - ax) * inv : 0.f;
+          sp[idx] = live ? a * inv : 0.f;
+          sl[idx] = live ? cn * inv : 0.f;
         }
-        const bool live = col_in && f.aj != 0.f;
-        const float ax = face_row(f, x11);
-        const float a = jl > 0 ? f.aj * f.gjs : 0.f, cn = jl < nj - 1 ? f.aj * f.gjc : 0.f;
-        const int idx = jl * TMA_TW + il;
-        su[idx] = live ? (bb - ax) * inv : 0.f;
-        sp[idx] = live ? a * inv : 0.f;
-        sl[idx] = live ? cn * inv : 0.f;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s]);
+      consumers_sync();
+      if (tid < TMA_TW) line_solve<float>(su, sp, sl, nj, TMA_TW, tid);
+      consumers_sync();
+      for (int idx = tid; idx < TMA_TW * nj; idx += TMA_NCONS) {
+        const int jl = idx / TMA_TW, ic = min(i0 + idx % TMA_TW, d.mx - 2);
+        const int c = cidx(d, ic, 1 + jl, k);
+        const float v = __ldg(xi + c) + omega * su[idx];
+        if (i0 + idx % TMA_TW <= d.mx - 2) xo[c] = v;
+      }
+      consumers_sync();  // the next tile restages su, sp, sl
     }
-    consumers_sync();
-    if (tid < TMA_TW) line_solve<float>(su, sp, sl, nj, TMA_TW, tid);
-    consumers_sync();
-    for (int idx = tid; idx < TMA_TW * nj; idx += TMA_NCONS) {
-      const int jl = idx / TMA_TW, ic = min(i0 + idx % TMA_TW, d.mx - 2);
-      const int c = cidx(d, ic, 1 + jl, k);
-      const float v = __ldg(xi + c) + omega * su[idx];
-      if (i0 + idx % TMA_TW <= d.mx - 2) xo[c] = v;
-    }
-    consumers_sync();  // the next tile restages su, sp, sl
   }
+  __syncthreads();
   // every copy issued has landed before the block exits (immediate unless a
-  // wait above ran out)
+  // wait above ran out): the last band issued on each stage
   if (tid == 0) {
-    for (long long r = (q > stages ? q - stages : 0); r < q; r++)
-      mbar_wait(&full[(int)(r % stages)], (unsigned)((r / stages) & 1), err, 4, abort, false);
+    const int n = n_issued;
+    for (int r = n > stages ? n - stages : 0; r < n; r++)
+      mbar_wait(&full[r % stages], (unsigned)((r / stages) & 1), err, 4, abort, false);
   }
 }
 
@@ -324,6 +339,9 @@ static bool map8(EncodeTiled enc, CUtensorMap* m, const void* base, const Dims& 
 }
 
 __device__ int g_tma_err = 0;
+static int g_tma_drop = -1;  // test hook: band whose 1/m copies are left out (-1: none)
+
+void smooth_tma_drop(int band) { g_tma_drop = band; }
 
 int* smooth_tma_err() {
   static int* p = nullptr;
@@ -392,7 +410,7 @@ int launch_smooth_tma(const OpView<float>& A, const float* lf, const float* xi, 
   }
   const int ntiles = ((d.mx - 2 + TMA_TW - 1) / TMA_TW) * (d.mz - 2);
   const int grid = std::max(1, std::min(nsm, ntiles));
-  k_smooth_tma<<<grid, TMA_NT, smem, s>>>(m, A, lf, xi, b, xo, omega, stages, err);
+  k_smooth_tma<<<grid, TMA_NT, smem, s>>>(m, A, lf, xi, b, xo, omega, stages, err, g_tma_drop);
   ++g_launches;
   return (int)cudaGetLastError();
 }

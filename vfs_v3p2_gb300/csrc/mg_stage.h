@@ -31,4 +31,9 @@ int launch_smooth_tma(const OpView<float>& A, const float* lf, const float* xi, 
 int* smooth_tma_err();
 int smooth_tma_take_error();
 
+// Test hook: later launches leave out the 1/m copies of band `band` of every
+// block (-1: none), so that band's bounded wait runs out and the sweep
+// reports it.
+void smooth_tma_drop(int band);
+
 }  // namespace vfs

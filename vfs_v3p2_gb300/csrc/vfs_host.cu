@@ -2980,6 +2980,11 @@ int vfs_grid_components(vfs_ctx* ctx, int grid, int* finest, int* coarsest) {
   return VFS_OK;
 }
 
+int vfs_debug_tma_drop(int band) {
+  smooth_tma_drop(band < 0 ? -1 : band);
+  return VFS_OK;
+}
+
 int vfs_sweep_damping(const vfs_solve_params* p, int finest, int post, double* w, int n) {
   if (!p || !w || n < 0) return VFS_ERR_ARG;
   if (p->nu1 < 0 || p->nu2 < 0 || p->nu1 > MAXSWEEP || p->nu2 > MAXSWEEP || p->nu1_coarse < -1 ||
