@@ -60,7 +60,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_group_gemv(const GroupItem<T>* __restrict__ items, int n) {
   const GroupItem<T>& it = group_item(items, n);
   if (skipped(it.skip)) return;
-  extern __shared__ unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   gemv_tile<T>(it.A.d, it.Binv, it.n, it.b, it.y, (const T*)nullptr, blockIdx.x - it.start, (T*)smraw);
 }
 

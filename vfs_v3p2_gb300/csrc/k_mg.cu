@@ -520,7 +520,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_coarse_gemv(Dims d, const T* __restrict__ Binv, int n, const T* __restrict__ b,
                                                      T* __restrict__ x, const T* __restrict__ dsc, const int* skip) {
   if (skipped(skip)) return;
-  extern __shared__ unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   gemv_tile<T>(d, Binv, n, b, x, dsc, blockIdx.x, (T*)smraw);
 }
 template <typename T>

@@ -973,7 +973,10 @@ __device__ __forceinline__ void prolong_tile(const Dims& f, const uint8_t* __res
 }
 
 // Rows 8 rb .. 8 rb + 7 of x = Binv (D b) over the packed interior (one warp
-// per row), b staged in sb (n values of T); dsc nullable.
+// per row), b staged in sb (n values of T, 16-byte aligned); dsc nullable.
+// When n is a multiple of a 16-byte vector, a lane reads its row entries and
+// b in 16-byte vectors (entries 4q .. 4q + 3 of FP32, lanes striding by 32
+// vectors) and adds them in that order; otherwise one entry at a time.
 template <typename T>
 __device__ __forceinline__ void gemv_tile(const Dims& d, const T* __restrict__ Binv, int n, const T* __restrict__ b,
                                           T* __restrict__ x, const T* __restrict__ dsc, int rb, T* sb) {
@@ -989,7 +992,27 @@ __device__ __forceinline__ void gemv_tile(const Dims& d, const T* __restrict__ B
   if (row >= n) return;
   const T* Br = Binv + (size_t)row * n;
   T s = T(0);
-  for (int col = lane; col < n; col += 32) s = fma(Br[col], sb[col], s);
+  constexpr int V = 16 / (int)sizeof(T);
+  if (n % V == 0) {
+    using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    const VT* Bv = reinterpret_cast<const VT*>(Br);
+    const VT* sv = reinterpret_cast<const VT*>(sb);
+#pragma unroll 4
+    for (int q = lane; q < n / V; q += 32) {
+      const VT a = __ldg(Bv + q), c = sv[q];
+      if constexpr (sizeof(T) == 4) {
+        s = fma(a.x, c.x, s);
+        s = fma(a.y, c.y, s);
+        s = fma(a.z, c.z, s);
+        s = fma(a.w, c.w, s);
+      } else {
+        s = fma(a.x, c.x, s);
+        s = fma(a.y, c.y, s);
+      }
+    }
+  } else {
+    for (int col = lane; col < n; col += 32) s = fma(Br[col], sb[col], s);
+  }
   s = warp_sum(s);
   if (lane == 0) {
     const int i = 1 + row % ni, j = 1 + (row / ni) % nj, k = 1 + row / (ni * nj);
