@@ -35,3 +35,16 @@ def test_library_is_built_for_sm103a():
     assert os.path.exists(path)
     assert "sm_103a" in " ".join(capi._build.ARCH)
     ctypes.CDLL(path)
+
+
+def test_default_params_and_unknown_fields():
+    """vfs_default_params (host only) and the binding's refusal of a field
+    vfs_solve_params does not have (a misspelt option would otherwise be
+    set on the Python object and ignored by the library)."""
+    import pytest
+
+    p = capi.default_params(precision="mixed")
+    assert p.precision == capi.VFS_MIXED and p.mg_stage == 0 and p.mg_grouped == 0 and p.mg_half == 0
+    assert capi.default_params(mg_stage=1).mg_stage == 1
+    with pytest.raises(AttributeError):
+        capi.default_params(mg_tma=1)
