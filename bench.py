@@ -281,12 +281,13 @@ def run_reference(args):
             pool = [s.case for s in serve.serving_streams(16)]
         pool.sort(key=lambda c: c.grid.nvert.size)
         sample = pool[len(pool) // 2 - 1:len(pool) // 2 + 1]
-        runs = [cpu_baseline(c, args, steps=1) for c in sample]
+        nwarm = max(1, args.warmup)
+        runs = [cpu_baseline(c, args, steps=1, warmup=nwarm) for c in sample]
         rates = [r[0] for r in runs]
         val = float(len(rates) / sum(1.0 / r for r in rates))
         cores = os.cpu_count()
         line = {"metric": METRIC, "value": val, "unit": "solves/s",
-                "impl": "reference", "n_gpus": args.gpus, "steps": len(sample), "warmup": 1,
+                "impl": "reference", "n_gpus": args.gpus, "steps": len(sample), "warmup": nwarm,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD[args.config], "rtol": args.rtol, "div_tol": args.div_tol,
@@ -295,7 +296,8 @@ def run_reference(args):
                                        "GPU arm's stopping rule)"},
                 "divmax": max(r[2]["divmax"] for r in runs),
                 "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
-                                 "sample": "two median-size grids of the workload, one step each after a warm-up"},
+                                 "sample": f"two median-size grids of the workload, one step each after {nwarm} "
+                                           f"warm-up steps"},
                 "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference links PETSc/HYPRE/MPI, absent here: its CPU algorithm is timed as the "
                         "oracle restatement, which matches the reference's own compiled path functions bit for bit"}
