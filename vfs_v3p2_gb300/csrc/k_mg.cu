@@ -99,12 +99,19 @@ int launch_apply_mg(const OpView<T>& A, const T* x, const T* b, T* y, cudaStream
 // y = A x with the FP32 face form (11-slot levels; testing hook).
 __global__ void __launch_bounds__(TX* TY) k_apply_face(OpView<float> A, const float* __restrict__ x,
                                                        float* __restrict__ y) {
+  const bool all = A.ffc != nullptr;  // the general face form (set on levels with i-j or j-k cross terms)
   TILE_LOOP(A.d) {
     if (!_in) continue;
     FaceData f;
     float xv[19];
-    face_gather(A, x, i, j, k, f, xv);
-    y[cidx(A.d, i, j, k)] = face_row(f, xv);
+    if (all) {
+      FaceX e;
+      face_gather_all(A, x, i, j, k, f, e, xv);
+      y[cidx(A.d, i, j, k)] = face_row_all(f, e, xv);
+    } else {
+      face_gather(A, x, i, j, k, f, xv);
+      y[cidx(A.d, i, j, k)] = face_row(f, xv);
+    }
   }
 }
 int launch_apply_face(const OpView<float>& A, const float* x, float* y, cudaStream_t s) {
@@ -179,6 +186,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
       smooth_attrs<MASK_CH, T, __half, true>();
       smooth_attrs<MASK_ALL, T, __half, true>();
       smooth_attrs<MASK_CH, T, FaceOp, false>();
+      smooth_attrs<MASK_ALL, T, FaceOp, false>();
     }
     attr = true;
   }
@@ -205,6 +213,9 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
       done = true;
     } else if (A.ffi && ch) {
       smooth_launch<MASK_CH, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+      done = true;
+    } else if (A.ffi && A.ffc) {  // the general face form
+      smooth_launch<MASK_ALL, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
       done = true;
     } else if (A.hcoef) {
       if (!ch) smooth_launch<MASK_ALL, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
@@ -434,9 +445,10 @@ int launch_residual_restrict(const OpView<T>& A, const T* x, const T* b, const T
                              const double* nvc, int si, int sj, int sk, T* bc, T* xc, cudaStream_t s) {
   bool done = false;
   if constexpr (sizeof(T) == 4) {
-    if (A.ffi && fits_ch(A.mask) && !si && !sj && !sk) {
+    if (A.ffi && (fits_ch(A.mask) || A.ffc) && !si && !sj && !sk) {
       dim3 g((c.mx - 2 + 31) / 32, (c.my - 2 + 3) / 4, c.mz - 2);
-      k_resrestrict_tiled<MASK_CH, T, FaceOp><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+      if (fits_ch(A.mask)) k_resrestrict_tiled<MASK_CH, T, FaceOp><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
+      else k_resrestrict_tiled<MASK_ALL, T, FaceOp><<<g, 256, 0, s>>>(A, x, b, rw, c, nvc, bc, xc);
       done = true;
     } else if (A.hcoef) {
       launch_resrestrict_tc<T, __half>(A, x, b, rw, c, nvc, si, sj, sk, bc, xc, s);

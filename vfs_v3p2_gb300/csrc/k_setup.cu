@@ -546,17 +546,51 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
 // (24 bytes) instead of 11 FP32 coefficients (44 bytes), as FP32 arrays
 // only (no byte array, whose rows a tensor copy could not tile).
 // ---------------------------------------------------------------------------
+// A cross weight with its own two code bits in its low mantissa bits.
+__device__ __forceinline__ float face_coded(double w, unsigned code) {
+  return __int_as_float((__float_as_int((float)w) & ~3) | (int)code);
+}
+// The regime of a cross term whose pairs lie beside the face at +1 / -1
+// along another axis: up / dn are the nvert sums of the pairs there,
+// at_hi / at_lo the non-periodic walls, first whether the cell is at index
+// 1 of that axis (the backward difference is never taken there, periodic or
+// not), as in poisson.c:1184-1231 and the same tests for every face and
+// cross term.  Returns the weight factor (0.25 centred, 0.5 one-sided, 0
+// none) and sets the code bits.
+__device__ __forceinline__ double face_regime(double up, double dn, bool at_hi, bool at_lo, bool first,
+                                              unsigned& code) {
+  const double THR = VFS_THR;
+  code = 0;
+  if (at_hi || up > THR) {
+    if (dn < THR && !first) {
+      code = 1u;  // backward: the upper pair is the centre pair
+      return 0.5;
+    }
+    return 0.;
+  }
+  if (at_lo || dn > THR) {
+    if (up < THR) {
+      code = 2u;  // forward: the lower pair is the centre pair
+      return 0.5;
+    }
+    return 0.;
+  }
+  return 0.25;
+}
+
 __global__ void k_face_operator(Dims d, const double* __restrict__ g, const double* __restrict__ nvert,
                                 const double* __restrict__ aj, float2* __restrict__ fi, float2* __restrict__ fk,
-                                float* __restrict__ fj, float* __restrict__ faj) {
+                                float* __restrict__ fj, float* __restrict__ faj, float4* __restrict__ fc) {
   const size_t N = ncell(d);
   const int mx = d.mx, my = d.my, mz = d.mz, ip = d.ip, jp = d.jp, kp = d.kp;
   const double *g11 = g, *g13 = g + 2 * N, *g22 = g + 4 * N, *g31 = g + 6 * N, *g33 = g + 8 * N;
+  const double *g12 = g + N, *g21 = g + 3 * N, *g23 = g + 5 * N, *g32 = g + 7 * N;
   const double THR = VFS_THR;
   GRID_LOOP(d) {
     DECOMP(d, i, j, k);
     float2 vi = make_float2(0.f, 0.f), vk = make_float2(0.f, 0.f);
     float vj = 0.f;
+    float4 vc = make_float4(0.f, 0.f, 0.f, 0.f);
     unsigned cb = 0;
     const bool row = interior(d, i, j, k) && !(nvert[_t] > THR);
     if (row) {
@@ -578,8 +612,22 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
           s = 0.25;
         }
         vi = make_float2((float)g11[c], (float)(g13[c] * s));
+        unsigned q;  // the j cross term (g12): pairs (C, E) at j+1 / j-1
+        const double t = face_regime(NV(i, j + 1, k) + NV(i + 1, j + 1, k), NV(i, j - 1, k) + NV(i + 1, j - 1, k),
+                                     j == my - 2 && !jp, j == 1 && !jp, j == 1, q);
+        vc.x = face_coded(g12[c] * t, q);
       }
-      if (NV(i, j + 1, k) < THR && (j != my - 2 || jp)) vj = (float)g22[c];  // j+1/2 face
+      if (NV(i, j + 1, k) < THR && (j != my - 2 || jp)) {  // j+1/2 face, poisson.c:1295-1352
+        vj = (float)g22[c];
+        unsigned q;  // the i cross term (g21): pairs (C, N) at i+1 / i-1
+        double t = face_regime(NV(i + 1, j, k) + NV(i + 1, j + 1, k), NV(i - 1, j, k) + NV(i - 1, j + 1, k),
+                               i == mx - 2 && !ip, i == 1 && !ip, i == 1, q);
+        vc.y = face_coded(g21[c] * t, q);
+        // the k cross term (g23): pairs (C, N) at k+1 / k-1
+        t = face_regime(NV(i, j, k + 1) + NV(i, j + 1, k + 1), NV(i, j, k - 1) + NV(i, j + 1, k - 1),
+                        k == mz - 2 && !kp, k == 1 && !kp, k == 1, q);
+        vc.z = face_coded(g23[c] * t, q);
+      }
       if (NV(i, j, k + 1) < THR && (k != mz - 2 || kp)) {                   // k+1/2 face, poisson.c:1421-1488
         double s = 0.;
         if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > THR) {
@@ -596,6 +644,10 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
           s = 0.25;
         }
         vk = make_float2((float)g33[c], (float)(g31[c] * s));
+        unsigned q;  // the j cross term (g32): pairs (C, T) at j+1 / j-1
+        const double t = face_regime(NV(i, j + 1, k) + NV(i, j + 1, k + 1), NV(i, j - 1, k) + NV(i, j - 1, k + 1),
+                                     j == my - 2 && !jp, j == 1 && !jp, j == 1, q);
+        vc.w = face_coded(g32[c] * t, q);
       }
 #undef NV
     }
@@ -603,6 +655,7 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
     fk[_t] = vk;
     fj[_t] = vj;
     faj[_t] = row ? __int_as_float((__float_as_int((float)aj[_t]) & ~0xF) | (int)cb) : 0.f;
+    fc[_t] = vc;
   }
 }
 
@@ -814,8 +867,8 @@ int launch_form_metrics(const Dims& d, const double* coor, double* M, double* tm
 }
 
 int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
-                         float* fj, float* faj, cudaStream_t s) {
-  k_face_operator<<<nblk(ncell(d)), 256, 0, s>>>(d, g, nvert, aj, fi, fk, fj, faj); ++g_launches;
+                         float* fj, float* faj, float4* fc, cudaStream_t s) {
+  k_face_operator<<<nblk(ncell(d)), 256, 0, s>>>(d, g, nvert, aj, fi, fk, fj, faj, fc); ++g_launches;
   return (int)cudaGetLastError();
 }
 

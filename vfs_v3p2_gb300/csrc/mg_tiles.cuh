@@ -238,6 +238,88 @@ __device__ __forceinline__ void face_gather(const OpView<float>& A, const float*
 }
 
 
+// The general face form (levels with i-j or j-k cross terms): face_row's
+// fluxes plus the four cross terms ffc holds.  A cross weight carries its own
+// code in its two low mantissa bits (face_xw clears them, face_xc reads them).
+__device__ __forceinline__ float face_xw(float v) { return __int_as_float(__float_as_int(v) & ~3); }
+__device__ __forceinline__ unsigned face_xc(float v) { return (unsigned)__float_as_int(v) & 3u; }
+struct FaceX {
+  float ijc, ijw;  // j cross weight of the +i faces of c and c-i (with their codes)
+  float jic, jkc;  // i and k cross weights of the +j face of c
+  float jis, jks;  // the same of the +j face of c-j
+  float kjc, kjb;  // j cross weight of the +k faces of c and c-k
+};
+// w (U - L) of a cross term: U is the pair at +1 or, one-sided, the face's
+// centre pair ctr; L the pair at -1 or the centre pair.
+__device__ __forceinline__ float face_cross(float w, float ctr, float up, float dn) {
+  const unsigned q = face_xc(w);
+  return face_xw(w) * (((q & 1u) ? ctr : up) - ((q & 2u) ? ctr : dn));
+}
+// Row of the general face form from the 19 stencil values: aj times the
+// divergence of the six face fluxes, each with its normal term and both
+// cross terms (poisson.c:1173-1558: the i+1 face's g12 and g13 pairs, the
+// j+1 face's g21 and g23 pairs, the k+1 face's g31 and g32 pairs).
+__device__ __forceinline__ float face_row_all(const FaceData& f, const FaceX& e, const float* x) {
+  const float xc = x[CP], xe = x[EP], xw = x[WP], xn = x[NP], xs = x[SP], xt = x[TP], xb = x[BP];
+  const float xte = x[TE], xbe = x[BE], xtw = x[TW], xbw = x[BW];
+  const float xne = x[NE], xse = x[SE], xnw = x[NW], xsw = x[SW], xtn = x[TN], xbn = x[BN], xts = x[TS], xbs = x[BS];
+  // +i face of c: the pair (C, E) at k+1 / k-1 and at j+1 / j-1
+  const float ce = xc + xe, te = xt + xte, be = xb + xbe;
+  const float Fic = f.fic.x * (xe - xc) + f.fic.y * (((f.cc & 1u) ? ce : te) - ((f.cc & 2u) ? ce : be)) +
+                    face_cross(e.ijc, ce, xn + xne, xs + xse);
+  // +i face of c-i: the pair (W, C)
+  const float wc = xw + xc, tw = xtw + xt, bw = xbw + xb;
+  const float Fiw = f.fiw.x * (xc - xw) + f.fiw.y * (((f.cw & 1u) ? wc : tw) - ((f.cw & 2u) ? wc : bw)) +
+                    face_cross(e.ijw, wc, xnw + xn, xsw + xs);
+  // +j face of c: the pair (C, N) at i+1 / i-1 and at k+1 / k-1
+  const float cn = xc + xn;
+  const float Fjc = f.gjc * (xn - xc) + face_cross(e.jic, cn, xe + xne, xw + xnw) + face_cross(e.jkc, cn, xt + xtn, xb + xbn);
+  // +j face of c-j: the pair (S, C)
+  const float sc = xs + xc;
+  const float Fjs = f.gjs * (xc - xs) + face_cross(e.jis, sc, xse + xe, xsw + xw) + face_cross(e.jks, sc, xts + xt, xbs + xb);
+  // +k face of c: the pair (C, T) at i+1 / i-1 and at j+1 / j-1
+  const float ct = xc + xt, ete = xe + xte, wtw = xw + xtw;
+  const float Fkc = f.fkc.x * (xt - xc) + f.fkc.y * (((f.cc & 4u) ? ct : ete) - ((f.cc & 8u) ? ct : wtw)) +
+                    face_cross(e.kjc, ct, xn + xtn, xs + xts);
+  // +k face of c-k: the pair (B, C)
+  const float bc = xb + xc, eb = xbe + xe, wb = xbw + xw;
+  const float Fkb = f.fkb.x * (xc - xb) + f.fkb.y * (((f.cb & 4u) ? bc : eb) - ((f.cb & 8u) ? bc : wb)) +
+                    face_cross(e.kjb, bc, xbn + xn, xbs + xs);
+  return f.aj * ((Fic - Fiw) + (Fjc - Fjs) + (Fkc - Fkb));
+}
+// face_gather plus the cross weights of c, c-i, c-j, c-k and the eight x
+// values face_row leaves out (NE SE NW SW TN BN TS BS), periodic wraps as in
+// stencil_gather.
+__device__ __forceinline__ void face_gather_all(const OpView<float>& A, const float* __restrict__ x, int i, int j,
+                                                int k, FaceData& f, FaceX& e, float* xv) {
+  const Dims d = A.d;
+  const int sy = d.mx, sz = d.mx * d.my;
+  const int c = k * sz + j * sy + i;
+  const int oiW = (i == 1 && d.ip) ? d.mx - 3 : -1, oiE = (i == d.mx - 2 && d.ip) ? 3 - d.mx : 1;
+  const int ojS = ((j == 1 && d.jp) ? d.my - 3 : -1) * sy, ojN = ((j == d.my - 2 && d.jp) ? 3 - d.my : 1) * sy;
+  const int okB = ((k == 1 && d.kp) ? d.mz - 3 : -1) * sz, okT = ((k == d.mz - 2 && d.kp) ? 3 - d.mz : 1) * sz;
+  const float* __restrict__ fc = reinterpret_cast<const float*>(A.ffc);
+  const float4 own = __ldg(A.ffc + c);
+  e.ijw = __ldg(fc + 4 * (size_t)(c + oiW));
+  e.jis = __ldg(fc + 4 * (size_t)(c + ojS) + 1);
+  e.jks = __ldg(fc + 4 * (size_t)(c + ojS) + 2);
+  e.kjb = __ldg(fc + 4 * (size_t)(c + okB) + 3);
+  xv[NE] = __ldg(x + c + oiE + ojN);
+  xv[SE] = __ldg(x + c + oiE + ojS);
+  xv[NW] = __ldg(x + c + oiW + ojN);
+  xv[SW] = __ldg(x + c + oiW + ojS);
+  xv[TN] = __ldg(x + c + okT + ojN);
+  xv[BN] = __ldg(x + c + okB + ojN);
+  xv[TS] = __ldg(x + c + okT + ojS);
+  xv[BS] = __ldg(x + c + okB + ojS);
+  face_gather(A, x, i, j, k, f, xv);
+  e.ijc = own.x;
+  e.jic = own.y;
+  e.jkc = own.z;
+  e.kjc = own.w;
+}
+
+
 // ---------------------------------------------------------------------------
 // Damped y-line Jacobi sweep: xo = xi + omega * T^{-1} (b - A xi), T the
 // tridiagonal j-coupling (SP, CP, NP) of each (i, k) column.  T is constant
@@ -498,6 +580,53 @@ __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float*
   }
 }
 
+// Phase 1 on the general face form (levels with i-j or j-k cross terms):
+// the residual from face_row_all, and the line couplings from the level's
+// assembled FP32 SP and NP coefficients (the cross terms add to them, and
+// the pivots 1/m are factored from the assembled rows).  From a zero guess
+// only aj, SP, NP, b and 1/m are read.
+template <int U, bool ZG>
+__device__ __forceinline__ void face_phase1_all(const OpView<float>& A, const float* __restrict__ lf,
+                                                const float* __restrict__ xi, const float* __restrict__ b, float* su,
+                                                float* sp, float* sl, int i0, int k, int tw) {
+  const Dims d = A.d;
+  const int nj = d.my - 2, sy = d.mx, sz = d.mx * d.my;
+  const size_t N = ncell(d);
+  const float* __restrict__ csp = A.coef + (size_t)SP * N;
+  const float* __restrict__ cnp = A.coef + (size_t)NP * N;
+  for (int base = threadIdx.x; base < tw * nj; base += U * VFS_SMOOTH_NT) {
+    FaceData f[U];
+    FaceX e[U];
+    float xv[U][19], bb[U], inv[U], av[U], cv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = min(base + u * VFS_SMOOTH_NT, tw * nj - 1);
+      const int il = idx % tw, jl = idx / tw;
+      const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
+      const int c = k * sz + j * sy + i;
+      if (ZG) f[u].aj = __ldg(A.faj + c);
+      else face_gather_all(A, xi, i, j, k, f[u], e[u], xv[u]);
+      av[u] = __ldg(csp + c);
+      cv[u] = __ldg(cnp + c);
+      bb[u] = __ldg(b + c);
+      inv[u] = __ldg(lf + c);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = base + u * VFS_SMOOTH_NT;
+      if (idx >= tw * nj) break;
+      const int jl = idx / tw;
+      const float aj = face_aj(f[u].aj);
+      const bool live = (i0 + idx % tw <= d.mx - 2) && aj != 0.f;
+      const float ax = ZG ? 0.f : face_row_all(f[u], e[u], xv[u]);
+      const float a = jl > 0 ? av[u] : 0.f, cn = jl < nj - 1 ? cv[u] : 0.f;
+      su[idx] = live ? (bb[u] - ax) * inv[u] : 0.f;
+      sp[idx] = live ? a * inv[u] : 0.f;
+      sl[idx] = live ? cn * inv[u] : 0.f;
+    }
+  }
+}
+
 // UU: cells whose loads one thread issues together in phase 1 (2 on levels
 // with fewer than two blocks per SM, where the looser register budget costs
 // no occupancy and halves the serial chain of round trips).
@@ -575,8 +704,9 @@ __device__ __forceinline__ void smooth_tile(const OpView<T>& A, const T* __restr
     // levels measured faster one cell per thread at 4 blocks per SM.
     smooth_pairs<MASK, T>(A, lf, xi, b, su, sp, sl, i0, k, TW);
   } else if constexpr (FACE) {
-    static_assert(sizeof(T) == 4 && MASK == MASK_CH, "the face form is the FP32 11-slot operator");
-    face_phase1<UU, ZG>(A, lf, xi, b, su, sp, sl, i0, k, TW);
+    static_assert(sizeof(T) == 4, "the face form is FP32");
+    if constexpr (MASK == MASK_CH) face_phase1<UU, ZG>(A, lf, xi, b, su, sp, sl, i0, k, TW);
+    else face_phase1_all<UU, ZG>(A, lf, xi, b, su, sp, sl, i0, k, TW);
   } else {
     // Phase 1 in batches of U cells per thread: every load of the batch is
     // issued before any arithmetic (all addresses are interior cells: columns
@@ -898,8 +1028,14 @@ __device__ __forceinline__ void resrestrict_tile(const OpView<T>& A, const T* __
       if constexpr (std::is_same<TC, FaceOp>::value) {
         FaceData fd;
         float xv[19];
-        face_gather(A, x, fic, fjc, fk, fd, xv);
-        ax = face_row(fd, xv);
+        if constexpr (MASK == MASK_CH) {
+          face_gather(A, x, fic, fjc, fk, fd, xv);
+          ax = face_row(fd, xv);
+        } else {
+          FaceX fe;
+          face_gather_all(A, x, fic, fjc, fk, fd, fe, xv);
+          ax = face_row_all(fd, fe, xv);
+        }
       } else {
         TC cv[19];
         T xv[19];

@@ -103,6 +103,13 @@ struct OpView {
   const float2* ffk = nullptr;
   const float* ffj = nullptr;
   const float* faj = nullptr;
+  // the general face form (levels with i-j or j-k cross terms, nullable):
+  // per cell the cross weights of the i-j and j-k terms, (x) the +i face's
+  // j cross term (g12), (y, z) the +j face's i and k cross terms (g21, g23),
+  // (w) the +k face's j cross term (g32), each carrying its own one-sided
+  // code in its two low mantissa bits (bit 0: the upper pair is the face's
+  // centre pair, bit 1: the lower pair)
+  const float4* ffc = nullptr;
 };
 
 __device__ __forceinline__ bool skipped(const int* f) { return f && *(volatile const int*)f; }

@@ -142,12 +142,14 @@ struct Level {
   float* rwh = nullptr;     // its restriction weights (levels >= 1)
   float* dinvh = nullptr;   // finest level: 1 / D (input scaling)
   float* dvalh = nullptr;   // coarsest level: D (dense-solve scaling)
-  // face form of the FP32 multigrid operator (11-slot levels, mg_half = 0):
-  // +i / +k faces (normal, cross weight), +j face, aj, cross-term code bits
+  // face form of the FP32 multigrid operator (mg_half = 0): +i / +k faces
+  // (normal, cross weight), +j face, aj, cross-term code bits; on levels
+  // with i-j or j-k cross terms also their weights (ffc)
   float2* ffi = nullptr;
   float2* ffk = nullptr;
   float* ffj = nullptr;
   float* faj = nullptr;
+  float4* ffc = nullptr;
 };
 
 struct Grid {
@@ -394,11 +396,21 @@ OpView<T> mgview(Level& L, const int* skip, bool half, bool face = false) {
     A.ffk = L.ffk;
     A.ffj = L.ffj;
     A.faj = L.faj;
+    if ((L.mask & ~0x7807Fu) != 0u) A.ffc = L.ffc;  // i-j or j-k cross terms: the general face form
   }
   return A;
 }
-// The FP32 face form runs on levels whose operator fits the 11-slot set.
+// The face form of a level fits the 11-slot set (no i-j or j-k cross terms).
 bool face_level(const Level& L) { return (L.mask & ~0x7807Fu) == 0u; }
+// Operator bytes a face-form cell streams in a sweep (x != 0, or from a zero
+// guess): the 11-slot form's 5 face weights and aj (24), plus on the general
+// form the 4 cross weights (16) and the assembled SP and NP line couplings
+// (8); from a zero guess the j faces and aj (8), or aj, SP and NP (12).
+template <typename T>
+double face_sweep_bytes(const OpView<T>& A, bool x_nonzero) {
+  if (A.ffc) return x_nonzero ? 48.0 : 12.0;
+  return x_nonzero ? 24.0 : 8.0;
+}
 
 template <typename T>
 int ensure_mg(vfs_ctx* ctx, Grid& g) {
@@ -470,7 +482,8 @@ void smooth_probed(int l, const OpView<T>& A, const T* lf, const T* xi, const T*
   // face form: the 5 face weights and aj with the code bits (24 bytes) instead
   // of the slots; from a zero guess the j faces and aj (8 bytes)
   const double slot_bytes = A.hcoef ? 2.0 : (double)sizeof(T);
-  const double op_bytes = A.ffi ? (xi ? 24.0 : 8.0) : (xi ? slot_bytes * popcount(A.mask) : slot_bytes * (A.hcoef ? 2 : 3));
+  const double op_bytes = A.ffi ? face_sweep_bytes(A, xi != nullptr)
+                                 : (xi ? slot_bytes * popcount(A.mask) : slot_bytes * (A.hcoef ? 2 : 3));
   const double bytes = (double)n_interior(A.d) * (op_bytes + (xi ? 4.0 : 3.0) * sizeof(T));
   int rc;
   {
@@ -520,7 +533,7 @@ template <typename T>
 T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, cudaStream_t s) {
   Level& L = g.lev[l];
   const bool half = sizeof(T) == 4 && c.half;
-  const bool face = sizeof(T) == 4 && !half && c.face && face_level(L);
+  const bool face = sizeof(T) == 4 && !half && c.face;
   OpView<T> A = mgview<T>(L, skip, half, face);
   T* lf = lf_sel<T>(L, half);
   const int W = level_writes(g, l, c);
@@ -544,8 +557,9 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
   int q = 0;
   T* cur = nullptr;
   const bool run_probe = g_probe.kind == VFS_PROBE_SMOOTH && l == g.L - 1;
-  const double sweep_bytes = (double)n_interior(A.d) * ((A.ffi ? 24.0 : (A.hcoef ? 2.0 : (double)sizeof(T)) *
-                                                                            popcount(A.mask)) + 4.0 * sizeof(T));
+  const double sweep_bytes = (double)n_interior(A.d) * ((A.ffi ? face_sweep_bytes(A, true)
+                                                                : (A.hcoef ? 2.0 : (double)sizeof(T)) * popcount(A.mask)) +
+                                                        4.0 * sizeof(T));
   SweepRun run;
   for (; q < c.pre(l); q++) {
     T* o = bufs[q & 1];
@@ -562,7 +576,7 @@ T* vcycle(Grid& g, int l, T* b, T* xa, T* xb, const MGCfg& c, const int* skip, c
     // side and the cleared coarse x written
     const bool face_rr = A.ffi && !g.si && !g.sj && !g.sk;  // the face form's restriction (tiled form only)
     Probed pr(VFS_PROBE_ALL, s, "k_resrestrict", l,
-              nf * ((face_rr ? 24.0 : slot_bytes * popcount(A.mask)) + 3.0 * sizeof(T)) +
+              nf * ((face_rr ? (A.ffc ? 40.0 : 24.0) : slot_bytes * popcount(A.mask)) + 3.0 * sizeof(T)) +
                   2.0 * n_interior(C.d) * sizeof(T));
     dbg("residual_restrict", l,
         launch_residual_restrict<T>(A, cur, b, rw_sel<T>(L, half), C.d, C.nvert, g.si, g.sj, g.sk, bbuf<T>(C), xc[0],
@@ -1481,10 +1495,17 @@ std::string group_key(const Job& J) {
          std::to_string((int)std::lround(std::log2(std::max(cells, 1.))));
 }
 
-// Members whose V-cycle may run grouped.
+// Members whose V-cycle may run grouped (the grouped kernels run the 11-slot
+// face form only: a mixed grid with i-j or j-k cross terms on some level,
+// whose own V-cycle uses the general face form there, runs ungrouped).
 bool groupable(const Job& J) {
   const Grid& g = *J.g;
-  return J.p.mg_grouped != 0 && !g.si && !g.sj && !g.sk && !mgcfg(J.p, g.L - 1, g.half_ok).half;
+  const MGCfg c = mgcfg(J.p, g.L - 1, g.half_ok);
+  if (J.p.mg_grouped == 0 || g.si || g.sj || g.sk || c.half) return false;
+  if (J.mixed() && c.face)
+    for (int l = 0; l < g.L; l++)
+      if (!face_level(g.lev[l])) return false;
+  return true;
 }
 
 // Uploads a grouped plan's table (a device buffer owned by bg) and returns
@@ -1771,7 +1792,7 @@ size_t level_bytes(const Dims& d, bool finest) {
   const size_t N = ncell(d);
   size_t b = N * (3 + 1 + MP_TOTAL + 19 + 19 + 1 + 1) * 8 + N * (19 + 1 + 1) * 4 + N;  // coor nvert M coef mcoef lf64 rw64 mcoef32 lf32 rw32 pcode
   b += 19 * 2 * hslot(d) + N * (4 + 4 + 4);  // hcoef lfh rwh, and dinvh (finest) or dvalh (coarsest)
-  b += N * (8 + 8 + 4 + 4);                   // face form: ffi ffk ffj faj (with the code bits)
+  b += N * (8 + 8 + 4 + 4 + 16);              // face form: ffi ffk ffj faj (with the code bits), ffc
   b += N * (3 * 4 + 3 * 8);                                            // MG work vectors, both precisions
   if (finest) b += N * 8 * (9 + 9 + 9 + 3 + 3 + 3 + 3 + 3) + N * 3;  // pd pw minv u ustar p phi b ucat aos, nb8 pc
   return b;
@@ -1948,6 +1969,7 @@ int vfs_grid_create(vfs_ctx* ctx, const vfs_grid_desc* desc, int* grid_id) {
     GAB(Lv.ffk, Lv.N);
     GAB(Lv.ffj, Lv.N);
     GAB(Lv.faj, Lv.N);
+    GAB(Lv.ffc, Lv.N);
     GAB(Lv.lfh, Lv.N);
     GAB(Lv.rwh, Lv.N);
     if (l == L - 1) GAB(Lv.dinvh, Lv.N);
@@ -2113,7 +2135,7 @@ int vfs_poisson_lhs(vfs_ctx* ctx, int grid) {
     Level& Lv = g.lev[l];
     launch_gtensor(Lv.d, Lv.M, gt, g.s);
     launch_assemble(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.coef, Lv.mcoef, Lv.mcoef32, dmask, g.s);
-    launch_face_operator(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.ffi, Lv.ffk, Lv.ffj, Lv.faj, g.s);
+    launch_face_operator(Lv.d, gt, Lv.nvert, Lv.M + Lv.N * MP_AJ, Lv.ffi, Lv.ffk, Lv.ffj, Lv.faj, Lv.ffc, g.s);
     CK(cudaMemcpyAsync(&Lv.mask, dmask, sizeof(unsigned), cudaMemcpyDeviceToHost, g.s));
     if (l > 0) launch_prolong_codes(Lv.d, g.lev[l - 1].d, g.si, g.sj, g.sk, Lv.nvert, g.lev[l - 1].nvert, Lv.pcode, g.s);
     launch_line_factors<float>(Lv.d, Lv.mcoef, Lv.lf32, g.s);
@@ -2909,8 +2931,8 @@ int vfs_apply_op(vfs_ctx* ctx, int grid, int level, int which, const double* x, 
     cudaFree(dy);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "apply");
   } else if (which == 4) {
-    // the FP32 face form (11-slot levels) applied to x rounded to FP32
-    if (!face_level(L)) return fail(ctx, VFS_ERR_ARG, "the face form needs an 11-slot level");
+    // the FP32 face form (the general one on levels with i-j or j-k cross
+    // terms) applied to x rounded to FP32
     std::vector<float> hx(N), hy(N);
     for (size_t q = 0; q < N; q++) hx[q] = (float)x[q];
     float *dx, *dy;

@@ -27,9 +27,10 @@ int launch_assemble(const Dims& d, const double* g, const double* nvert, const d
 // face form of the aj-scaled operator (11-slot levels), FP32: per cell its
 // +i face (g11, k-cross weight), +k face (g33, i-cross weight), +j face
 // (g22), and aj with the one-sided code bits of the two cross terms in its
-// four low mantissa bits
+// four low mantissa bits; fc: the i-j and j-k cross weights of the general
+// face form (OpView::ffc), zero on 11-slot levels
 int launch_face_operator(const Dims& d, const double* g, const double* nvert, const double* aj, float2* fi, float2* fk,
-                         float* fj, float* faj, cudaStream_t s);
+                         float* fj, float* faj, float4* fc, cudaStream_t s);
 int launch_coarsen(const Dims& f, const Dims& c, int si, int sj, int sk, const double* coor_f, const double* nv_f,
                    double* coor_c, double* nv_c, cudaStream_t s);
 int launch_prolong_codes(const Dims& f, const Dims& c, int si, int sj, int sk, const double* nv_f, const double* nv_c,
