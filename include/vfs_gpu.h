@@ -97,15 +97,17 @@ typedef struct {
                                   256x128x128); the Chebyshev damping needs
                                   none beyond nu1 / nu2 */
   int mg_half;  /* VFS_MIXED only: storage of the multigrid levels' operator.
-                   0 (the default): FP32; on levels whose cross terms are the
-                   i-k ones only (the 11-slot operator: channel and sphere
-                   grids) in face form: per cell its three faces' FP32
-                   weights (g11, g22, g33 and the cross weights with the
-                   one-sided regime folded in) and aj carrying the regime
-                   code bits in its four low mantissa bits, the row
-                   being aj times the divergence of the face fluxes (a sweep
-                   streams 40 instead of 60 bytes per cell); elsewhere the 19
-                   assembled FP32 coefficients.  2: the assembled FP32
+                   0 (the default): FP32 in face form, the row being aj times
+                   the divergence of the cell's six face fluxes: per cell its
+                   three faces' FP32 weights (g11, g22, g33 and the cross
+                   weights with the one-sided regime folded in) and aj
+                   carrying the i-k cross terms' regime code bits in its four
+                   low mantissa bits (channel and sphere grids, whose only
+                   cross terms are the i-k ones: a sweep streams 40 instead of
+                   60 bytes per cell); on levels with i-j or j-k cross terms
+                   (terrain) also the four other cross weights, each with its
+                   own code in its two low mantissa bits, and the assembled
+                   line couplings (64 instead of 92 bytes per cell).  2: the assembled FP32
                    coefficients on every level.  1: FP16 normalised by the
                    diagonal, with an FP16 centre-slot correction that keeps
                    every row sum.  The arithmetic is FP32 in every case, and
