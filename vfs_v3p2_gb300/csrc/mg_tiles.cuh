@@ -287,6 +287,21 @@ __device__ __forceinline__ float face_row_all(const FaceData& f, const FaceX& e,
                     face_cross(e.kjb, bc, xbn + xn, xbs + xs);
   return f.aj * ((Fic - Fiw) + (Fjc - Fjs) + (Fkc - Fkb));
 }
+// The row's S and N coefficients (its j-line couplings) over aj: the
+// coefficients of x_S and x_N in face_row_all's divergence -- the j faces'
+// normal weights, the j cross terms of the i and k faces (the pair at j-1 or
+// j+1 unless the regime takes the centre pair) and the j faces' cross terms
+// whose centre pair is the pair they take.
+__device__ __forceinline__ void face_row_sn(const FaceData& f, const FaceX& e, float& s, float& n) {
+  auto nq1 = [](float w) { return (face_xc(w) & 1u) ? 0.f : face_xw(w); };  // upper pair at +1
+  auto nq2 = [](float w) { return (face_xc(w) & 2u) ? 0.f : face_xw(w); };  // lower pair at -1
+  auto ctr = [](float w) {  // the centre pair: +w as the upper pair, -w as the lower one
+    const unsigned q = face_xc(w);
+    return ((q & 1u) ? face_xw(w) : 0.f) - ((q & 2u) ? face_xw(w) : 0.f);
+  };
+  s = f.gjs - nq2(e.ijc) + nq2(e.ijw) - nq2(e.kjc) + nq2(e.kjb) - ctr(e.jis) - ctr(e.jks);
+  n = f.gjc + nq1(e.ijc) - nq1(e.ijw) + nq1(e.kjc) - nq1(e.kjb) + ctr(e.jic) + ctr(e.jkc);
+}
 // face_gather plus the cross weights of c, c-i, c-j, c-k and the eight x
 // values face_row leaves out (NE SE NW SW TN BN TS BS), periodic wraps as in
 // stencil_gather.
@@ -581,10 +596,10 @@ __device__ __forceinline__ void face_phase1(const OpView<float>& A, const float*
 }
 
 // Phase 1 on the general face form (levels with i-j or j-k cross terms):
-// the residual from face_row_all, and the line couplings from the level's
-// assembled FP32 SP and NP coefficients (the cross terms add to them, and
-// the pivots 1/m are factored from the assembled rows).  From a zero guess
-// only aj, SP, NP, b and 1/m are read.
+// the residual from face_row_all and the line couplings aj times
+// face_row_sn's coefficients (the cross terms add to them; the pivots 1/m are
+// factored from the assembled rows).  From a zero guess only aj, the
+// assembled FP32 SP and NP, b and 1/m are read.
 template <int U, bool ZG>
 __device__ __forceinline__ void face_phase1_all(const OpView<float>& A, const float* __restrict__ lf,
                                                 const float* __restrict__ xi, const float* __restrict__ b, float* su,
@@ -604,10 +619,13 @@ __device__ __forceinline__ void face_phase1_all(const OpView<float>& A, const fl
       const int il = idx % tw, jl = idx / tw;
       const int i = min(i0 + il, d.mx - 2), j = 1 + jl;
       const int c = k * sz + j * sy + i;
-      if (ZG) f[u].aj = __ldg(A.faj + c);
-      else face_gather_all(A, xi, i, j, k, f[u], e[u], xv[u]);
-      av[u] = __ldg(csp + c);
-      cv[u] = __ldg(cnp + c);
+      if (ZG) {
+        f[u].aj = __ldg(A.faj + c);
+        av[u] = __ldg(csp + c);
+        cv[u] = __ldg(cnp + c);
+      } else {
+        face_gather_all(A, xi, i, j, k, f[u], e[u], xv[u]);
+      }
       bb[u] = __ldg(b + c);
       inv[u] = __ldg(lf + c);
     }
@@ -618,7 +636,13 @@ __device__ __forceinline__ void face_phase1_all(const OpView<float>& A, const fl
       const int jl = idx / tw;
       const float aj = face_aj(f[u].aj);
       const bool live = (i0 + idx % tw <= d.mx - 2) && aj != 0.f;
-      const float ax = ZG ? 0.f : face_row_all(f[u], e[u], xv[u]);
+      float ax = 0.f;
+      if (!ZG) {
+        ax = face_row_all(f[u], e[u], xv[u]);
+        face_row_sn(f[u], e[u], av[u], cv[u]);
+        av[u] *= aj;
+        cv[u] *= aj;
+      }
       const float a = jl > 0 ? av[u] : 0.f, cn = jl < nj - 1 ? cv[u] : 0.f;
       su[idx] = live ? (bb[u] - ax) * inv[u] : 0.f;
       sp[idx] = live ? a * inv[u] : 0.f;

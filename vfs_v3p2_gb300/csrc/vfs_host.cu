@@ -404,11 +404,11 @@ OpView<T> mgview(Level& L, const int* skip, bool half, bool face = false) {
 bool face_level(const Level& L) { return (L.mask & ~0x7807Fu) == 0u; }
 // Operator bytes a face-form cell streams in a sweep (x != 0, or from a zero
 // guess): the 11-slot form's 5 face weights and aj (24), plus on the general
-// form the 4 cross weights (16) and the assembled SP and NP line couplings
-// (8); from a zero guess the j faces and aj (8), or aj, SP and NP (12).
+// form the 4 cross weights (16); from a zero guess the j faces and aj (8),
+// or aj and the assembled SP and NP (12).
 template <typename T>
 double face_sweep_bytes(const OpView<T>& A, bool x_nonzero) {
-  if (A.ffc) return x_nonzero ? 48.0 : 12.0;
+  if (A.ffc) return x_nonzero ? 40.0 : 12.0;
   return x_nonzero ? 24.0 : 8.0;
 }
 
