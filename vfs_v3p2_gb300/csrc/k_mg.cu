@@ -214,8 +214,8 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
     } else if (A.ffi && ch) {
       smooth_launch<MASK_CH, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
       done = true;
-    } else if (A.ffi && A.ffc) {  // the general face form
-      smooth_launch<MASK_ALL, T, FaceOp, false>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
+    } else if (A.ffi && A.ffc) {  // the general face form (one cell per batch: two would spill)
+      smooth_launch<MASK_ALL, T, FaceOp, false>(false, g, sm, s, A, lf, xi, b, xo, omega, tw);
       done = true;
     } else if (A.hcoef) {
       if (!ch) smooth_launch<MASK_ALL, T, __half, true>(small, g, sm, s, A, lf, xi, b, xo, omega, tw);
