@@ -106,9 +106,9 @@ typedef struct {
                    cross terms are the i-k ones: a sweep streams 40 instead of
                    60 bytes per cell); on levels with i-j or j-k cross terms
                    (terrain) also the four other cross weights, each with its
-                   own code in its two low mantissa bits, and the assembled
-                   line couplings (64 instead of 92 bytes per cell).  2: the assembled FP32
-                   coefficients on every level.  1: FP16 normalised by the
+                   own code in its two low mantissa bits (56 instead of 92
+                   bytes per cell).  2: the assembled FP32 coefficients on
+                   every level.  1: FP16 normalised by the
                    diagonal, with an FP16 centre-slot correction that keeps
                    every row sum.  The arithmetic is FP32 in every case, and
                    the FP64 FGMRES operator is the same. */
