@@ -4,8 +4,9 @@ normal term and both cross terms (poisson.c:1173-1558), with the cross
 weights' one-sided regimes in their low mantissa bits.  Checked against the
 assembled operator on every level -- over the hill with walls in j and
 periodic i and k, with immersed bodies on the terrain (one-sided regimes of
-every cross term next to solid cells), and with every axis periodic -- and
-through a whole mixed-precision projection step against the FP64 one."""
+every cross term next to solid cells), and with every axis periodic --
+through a whole mixed-precision projection step against the FP64 one (also
+with semi-coarsening), and in a grouped batch."""
 import math
 
 import numpy as np
@@ -80,3 +81,58 @@ def test_general_face_form_step(gpu_ctx, name):
         assert np.linalg.norm(a - r) <= 1e-8 * np.linalg.norm(r)
     finally:
         gpu_ctx.grid_destroy(gid)
+
+
+def test_general_face_form_semi_coarsened(gpu_ctx):
+    """Semi-coarsening in j (the face form's sweeps; the restriction falls
+    back to the assembled coefficients): the mixed step reaches the FP64
+    step's phi and divergence bar."""
+    (case, per) = _terrain(64, 32, 32, spheres=[(math.pi, 0.45, math.pi / 2, 0.25)])
+    g = case.grid
+    gid = gpu_ctx.grid_create(g.coor, g.nvert, 3, case.immersed, periodic=per, semi=(0, 1, 0))
+    try:
+        gpu_ctx.poisson_lhs(gid)
+        phi = {}
+        for prec in ("fp64", "mixed"):
+            u = np.ascontiguousarray(case.ucont.copy())
+            p = np.zeros(g.nvert.shape)
+            info, dm = gpu_ctx.projection_step(gid, capi.default_params(precision=prec, rtol=1e-11, div_tol=1e-8), u, p)
+            assert info["converged"] and dm < 1e-8, (prec, info, dm)
+            phi[prec] = gpu_ctx.get_field(gid, capi.FIELD_PHI, p.shape)
+        fl = g.nvert < 0.1
+        fl[0], fl[-1], fl[:, 0], fl[:, -1], fl[:, :, 0], fl[:, :, -1] = (False,) * 6
+        a, r = phi["mixed"][fl], phi["fp64"][fl]
+        a, r = a - a.mean(), r - r.mean()
+        assert np.linalg.norm(a - r) <= 1e-8 * np.linalg.norm(r)
+    finally:
+        gpu_ctx.grid_destroy(gid)
+
+
+def test_grouped_batch_with_a_terrain_grid(gpu_ctx):
+    """A batch holding a grid on the general face form runs it ungrouped
+    under mg_grouped = 1 (the grouped kernels take the 11-slot form): the
+    batch's results are those of mg_grouped = 0 bit for bit."""
+    cases = [_terrain(32, 32, 32)[0]] + list(synth.c4_batch(count=3, seed=79, lo=(16, 16, 16), hi=(32, 32, 32)))
+    ids = []
+    try:
+        for c in cases:
+            gg = c.grid
+            gid = gpu_ctx.grid_create(gg.coor, gg.nvert, c.levels, c.immersed)
+            gpu_ctx.poisson_lhs(gid)
+            ids.append(gid)
+        out = {}
+        for grouped in (0, 1):
+            for gid, c in zip(ids, cases):
+                gpu_ctx.set_field(gid, capi.FIELD_USTAR, c.ucont)
+                gpu_ctx.set_field(gid, capi.FIELD_P, np.zeros(c.grid.nvert.shape))
+            plist = [capi.default_params(precision="mixed", rtol=1e-9, div_tol=1e-8, mg_grouped=grouped)] * len(cases)
+            infos, dm = gpu_ctx.projection_step_batch(ids, plist)
+            assert all(i["converged"] for i in infos) and (dm < 1e-8).all()
+            out[grouped] = ([i["iterations"] for i in infos], dm.copy(),
+                            [gpu_ctx.get_field(gid, capi.FIELD_PHI, c.grid.nvert.shape) for gid, c in zip(ids, cases)])
+        assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+        for a, b in zip(out[0][2], out[1][2]):
+            assert np.array_equal(a, b)
+    finally:
+        for gid in ids:
+            gpu_ctx.grid_destroy(gid)
