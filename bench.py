@@ -101,7 +101,8 @@ def make_case(args):
 
 
 # storage of the FP32 multigrid's level operators (vfs_solve_params.mg_half)
-OPERATOR = {0: "fp32 (face form on 11-slot levels: 3 face weights + 2 cross weights + aj carrying 4 code bits per cell)",
+OPERATOR = {0: "fp32 face form (3 face weights + 2 cross weights + aj carrying 4 code bits per cell; on levels with "
+                "i-j or j-k cross terms 4 more cross weights carrying their own codes)",
             1: "fp16 diagonal-normalised, row sums kept (fp32 arithmetic)",
             2: "fp32 assembled coefficients (11 or 19 slots)"}
 
@@ -752,7 +753,10 @@ def main():
     avg_ms = pms / plaunch if plaunch else None
     achieved = alg / (avg_ms / 1e3) / 1e9 if plaunch else None
     kname = {0: "k_smooth<float, FaceOp>", 1: "k_smooth<float, __half>", 2: "k_smooth<float, float>"}[args.mg_half]
-    if args.mg_half == 0:
+    if args.mg_half == 0 and args.config == "terrain":
+        # i-j and j-k cross terms (the hill): the general face form
+        kname = "k_smooth<float, FaceOp, general>"
+    elif args.mg_half == 0:
         # the face form's full-width sweeps run the warp-row kernel (30-column
         # tiles), or with --mg-stage 1 the tensor-copy one
         kname = "k_smooth_tma" if args.mg_stage else "k_smooth_w<2>"
