@@ -191,7 +191,7 @@ int launch_smooth(const OpView<T>& A, const T* lf, const T* xi, const T* b, T* x
     attr = true;
   }
   const int nj = A.d.my - 2, ni = A.d.mx - 2, nk = A.d.mz - 2;
-  const int tw = smooth_tw<T>(ni, nj, nk, cols);
+  const int tw = smooth_tw<T>(ni, nj, nk, cols, solo || VFS_SMOOTH_NARROW_SHARED);
   const size_t sm = smooth_smem<T>(tw, nj);
   dim3 g((ni + tw - 1) / tw, nk);
   const bool ch = fits_ch(A.mask);

@@ -1013,16 +1013,22 @@ __device__ __forceinline__ void smooth_tile_w(const OpView<float>& A, const floa
 // three staged line arrays exceed 48 KB or the tile is twice the width of
 // the level; automatically also narrowed (down to 8) while the sweep has
 // fewer than VFS_SMOOTH_MINBLK blocks (one per SM), so small levels keep
-// the machine busy.
+// the machine busy -- when the grid solves alone (narrow): in a batch or
+// under serving other grids' kernels fill the machine, and the full-width
+// tiles (and their warp-row kernel) measured faster (64-grid batch: 806-830
+// -> 877-883 solves/s mixed, 428 -> 443 FP64).
 template <typename T>
-inline int smooth_tw(int ni, int nj, int nk, int cols) {
+inline int smooth_tw(int ni, int nj, int nk, int cols, bool narrow = true) {
   int tw = cols > 0 ? cols : VFS_SMOOTH_TWMAX;
   while (tw > 4 && (size_t)3 * tw * nj * sizeof(T) > 48 * 1024) tw >>= 1;
   while (tw > 4 && tw / 2 >= ni) tw >>= 1;
-  if (cols == 0)
+  if (cols == 0 && narrow)
     while (tw > VFS_SMOOTH_TWMIN && (size_t)((ni + tw - 1) / tw) * nk < VFS_SMOOTH_MINBLK) tw >>= 1;
   return tw;
 }
+#ifndef VFS_SMOOTH_NARROW_SHARED
+#define VFS_SMOOTH_NARROW_SHARED 0  // 1: narrow for parallelism also when other grids share the GPU
+#endif
 
 
 // One tile of the residual restriction (see k_resrestrict_tiled): coarse
