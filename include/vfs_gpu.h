@@ -143,7 +143,7 @@ typedef struct {
                          bit for bit the per-grid launches' results.  0 (the
                          default): each grid's own launches, each grid a branch
                          of the tick's graph, which measured faster on GB300
-                         (64-grid batch: 801 against 683 solves/s).  Single
+                         (64-grid batch: 877 against 754 solves/s).  Single
                          solves and served requests ignore it. */
   int mg_stage;       /* How the finest level's sweeps on the FP32 face form
                          (levels of at least 2^20 interior cells) stage their

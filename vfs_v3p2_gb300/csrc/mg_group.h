@@ -9,7 +9,7 @@
 // is the per-grid one bit for bit; what changes is the number of graph
 // nodes (a group's V-cycle is one chain of about 33 launches whatever the
 // number of its grids).  Measured on GB300 it is slower than a graph branch
-// per grid (64-grid batch: 683 against 801 solves/s): graph nodes cost about
+// per grid (64-grid batch: 754 against 877 solves/s): graph nodes cost about
 // 1 us each, and a grouped stage waits on every grid of its group, so it is
 // an option (mg_grouped), off by default.
 #pragma once

@@ -1398,7 +1398,7 @@ void group_item(Grid& g, const GOp<T>& op, const MGCfg& c, const int* skip, int*
   switch (op.kind) {
     case GOP_SMOOTH: {
       t.lf = lf_sel<T>(L, false);
-      t.tw = smooth_tw<T>(ni, nj, nk, c.cols);
+      t.tw = smooth_tw<T>(ni, nj, nk, c.cols, VFS_SMOOTH_NARROW_SHARED != 0);  // grouped grids share the GPU
       t.gx = (ni + t.tw - 1) / t.tw;
       t.gy = nk;
       *blocks = t.gx * nk;
