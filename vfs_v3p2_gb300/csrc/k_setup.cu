@@ -525,11 +525,12 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
 }
 
 // ---------------------------------------------------------------------------
-// Face form of a level's aj-scaled operator for the FP32 multigrid (levels
-// whose i-j and j-k cross terms vanish: the 11-slot operator).  The assembly
-// above builds every row from six face fluxes, each computed identically by
-// the two cells that share the face (poisson.c:1173-1558: the i+1 branch of
-// cell c and the i-1 branch of cell c+1 test the same cells and walls), so
+// Face form of a level's aj-scaled operator for the FP32 multigrid.  The
+// assembly above builds every row from six face fluxes, each computed
+// identically by the two cells that share the face (poisson.c:1173-1558: the
+// i+1 branch of cell c and the i-1 branch of cell c+1 test the same cells and
+// walls), so on a level whose i-j and j-k cross terms vanish (the 11-slot
+// operator)
 //   (A x)_c = F_i(c) - F_i(c-i) + F_j(c) - F_j(c-j) + F_k(c) - F_k(c-k),
 //   F_i(c) = gi (x_E - x_C) + gik (U - L)      (the k cross term of g13)
 //   F_j(c) = gj (x_N - x_C)
@@ -544,7 +545,12 @@ __global__ void k_assemble(Dims d, const double* __restrict__ g, const double* _
 // the FP32 aj (a relative change of at most 2^-19 of aj; the bits are
 // cleared before aj is used), so a row streams 5 FP32 face weights and aj
 // (24 bytes) instead of 11 FP32 coefficients (44 bytes), as FP32 arrays
-// only (no byte array, whose rows a tensor copy could not tile).
+// only (no byte array, whose rows a tensor copy could not tile).  Every level
+// also gets fc: the i face's j cross term (g12), the j face's i and k cross
+// terms (g21, g23) and the k face's j cross term (g32), each weight with its
+// own two code bits (face_coded): on levels with those terms (terrain) the
+// general face form adds them to F_i, F_j, F_k; elsewhere they are zero.  All
+// six cross terms take their regime from face_regime.
 // ---------------------------------------------------------------------------
 // A cross weight with its own two code bits in its low mantissa bits.
 __device__ __forceinline__ float face_coded(double w, unsigned code) {
@@ -597,20 +603,10 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
 #define NV(ii, jj, kk) nvert[cidx(d, ii, jj, kk)]
       const size_t c = _t;
       if (NV(i + 1, j, k) < THR && (i != mx - 2 || ip)) {  // i+1/2 face, poisson.c:1173-1232
-        double s = 0.;
-        if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > THR) {
-          if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < THR && k != 1) {
-            s = 0.5;  // backward: U = centre pair
-            cb |= 1u;
-          }
-        } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > THR) {
-          if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < THR) {
-            s = 0.5;  // forward: L = centre pair
-            cb |= 2u;
-          }
-        } else {
-          s = 0.25;
-        }
+        unsigned qk;  // the k cross term (g13): pairs (C, E) at k+1 / k-1, code bits 0-1 of aj
+        const double s = face_regime(NV(i, j, k + 1) + NV(i + 1, j, k + 1), NV(i, j, k - 1) + NV(i + 1, j, k - 1),
+                                     k == mz - 2 && !kp, k == 1 && !kp, k == 1, qk);
+        cb |= qk;
         vi = make_float2((float)g11[c], (float)(g13[c] * s));
         unsigned q;  // the j cross term (g12): pairs (C, E) at j+1 / j-1
         const double t = face_regime(NV(i, j + 1, k) + NV(i + 1, j + 1, k), NV(i, j - 1, k) + NV(i + 1, j - 1, k),
@@ -629,20 +625,10 @@ __global__ void k_face_operator(Dims d, const double* __restrict__ g, const doub
         vc.z = face_coded(g23[c] * t, q);
       }
       if (NV(i, j, k + 1) < THR && (k != mz - 2 || kp)) {                   // k+1/2 face, poisson.c:1421-1488
-        double s = 0.;
-        if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > THR) {
-          if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < THR && i != 1) {
-            s = 0.5;  // backward: R = centre pair
-            cb |= 4u;
-          }
-        } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > THR) {
-          if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < THR) {
-            s = 0.5;  // forward: Lf = centre pair
-            cb |= 8u;
-          }
-        } else {
-          s = 0.25;
-        }
+        unsigned qi;  // the i cross term (g31): pairs (C, T) at i+1 / i-1, code bits 2-3 of aj
+        const double s = face_regime(NV(i + 1, j, k) + NV(i + 1, j, k + 1), NV(i - 1, j, k) + NV(i - 1, j, k + 1),
+                                     i == mx - 2 && !ip, i == 1 && !ip, i == 1, qi);
+        cb |= qi << 2;
         vk = make_float2((float)g33[c], (float)(g31[c] * s));
         unsigned q;  // the j cross term (g32): pairs (C, T) at j+1 / j-1
         const double t = face_regime(NV(i, j + 1, k) + NV(i, j + 1, k + 1), NV(i, j - 1, k) + NV(i, j - 1, k + 1),
